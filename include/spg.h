@@ -1,0 +1,142 @@
+/*
+ * spg.h — C ABI of the GB300 sparse engine (libspg.so).
+ *
+ * This is the drop-in boundary for Spira's sparse hot path. Spira itself is a
+ * header-only C++23 template library with no C ABI; each entry point below
+ * names the Spira interface (file:line inside the Spira source tree) whose
+ * behaviour it carries. The C++23 facade in include/spira_gb300/ maps these
+ * calls back onto Spira's own class and function names and turns status codes
+ * into Spira's exception types.
+ *
+ * Conventions
+ *   - Plain C: opaque handles, plain pointers and sizes, int status codes.
+ *   - Device-resident CSR, Spira's SoA layout: uint64 offsets[n_rows+1]
+ *     (Spira uses std::size_t), uint32 cols[capacity], double vals[capacity]
+ *     (csr_storage_soa.hpp:17-77).
+ *   - `stream` arguments are cudaStream_t passed as void*; NULL selects the
+ *     context's own stream. Calls with a `stream` argument are asynchronous
+ *     on that stream; every other call returns after its work is complete.
+ *   - Handles are not thread-safe; use one context per host thread.
+ *   - No call falls back to the CPU: without a usable GB300 every compute
+ *     call fails with SPG_ERR_CUDA.
+ */
+#ifndef SPG_H
+#define SPG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes; the facade maps them to Spira's exceptions ---------- */
+enum spg_status {
+    SPG_OK = 0,
+    SPG_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument: shape/size mismatch, malformed CSR */
+    SPG_ERR_LOGIC = 2,            /* std::logic_error: wrong mode (e.g. spmv before lock) */
+    SPG_ERR_OUT_OF_RANGE = 3,     /* std::out_of_range: row/col index beyond the shape */
+    SPG_ERR_NO_MEMORY = 4,        /* std::bad_alloc: device allocation failed */
+    SPG_ERR_CUDA = 5,             /* CUDA runtime error (no device, launch failure, ...) */
+    SPG_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up; context stays usable */
+    SPG_ERR_UNSUPPORTED = 7       /* valid request this build does not serve */
+};
+
+/* ---- SpMV variants (spg_spmv `variant`) --------------------------------- */
+enum spg_spmv_variant {
+    SPG_SPMV_AUTO = -1,     /* learned selector, exhaustive-autotune fallback */
+    SPG_SPMV_SCALAR = 0,    /* one thread per row, CSR order (the plain path) */
+    SPG_SPMV_VECTOR2 = 1,   /* 2 lanes per row, shuffle reduction */
+    SPG_SPMV_VECTOR4 = 2,
+    SPG_SPMV_VECTOR8 = 3,
+    SPG_SPMV_VECTOR16 = 4,
+    SPG_SPMV_VECTOR32 = 5,  /* one warp per row, 16-byte vector loads */
+    SPG_SPMV_STREAM = 6,    /* CTA row blocks: coalesced nnz staging in shared memory */
+    SPG_SPMV_MERGE = 7,     /* merge-path: equal (rows + nnz) per CTA, carry fix-up */
+    SPG_SPMV_N_VARIANTS = 8
+};
+
+typedef struct spg_ctx spg_ctx; /* one device + one stream + memory pool */
+typedef struct spg_csr spg_csr; /* a device-resident CSR matrix */
+
+typedef struct spg_csr_info {
+    uint64_t n_rows;
+    uint64_t n_cols;
+    uint64_t nnz;
+    uint64_t capacity; /* Spira's csr_storage::capacity (>= nnz) */
+    int built;         /* 0 until the first lock / load */
+} spg_csr_info;
+
+/* ---- errors / library --------------------------------------------------- */
+const char *spg_strerror(int status);
+/* Detail message of the last failing call on this host thread. */
+const char *spg_last_error(void);
+/* ABI version, major*10000 + minor*100 + patch. */
+int spg_version(void);
+
+/* ---- context ------------------------------------------------------------ */
+int spg_ctx_create(int device, spg_ctx **out);
+int spg_ctx_destroy(spg_ctx *ctx);
+/* The context's own stream (cudaStream_t as void*). */
+int spg_ctx_stream(spg_ctx *ctx, void **stream);
+int spg_ctx_sync(spg_ctx *ctx);
+
+/* ---- CSR handles ---------------------------------------------------------
+ * spg_csr_create: an unbuilt n_rows x n_cols matrix (matrix.hpp:197-209). */
+int spg_csr_create(spg_ctx *ctx, uint64_t n_rows, uint64_t n_cols, spg_csr **out);
+int spg_csr_destroy(spg_csr *A);
+int spg_csr_info_get(const spg_csr *A, spg_csr_info *info);
+/* Device pointers of the CSR arrays (valid until the next lock of A). */
+int spg_csr_device_arrays(const spg_csr *A, const uint64_t **offsets,
+                          const uint32_t **cols, const double **vals);
+/* Copy the CSR to host arrays sized n_rows+1 / nnz / nnz; NULL skips an array
+ * (matrix.hpp:88-91 csr()). */
+int spg_csr_download(spg_ctx *ctx, const spg_csr *A, uint64_t *offsets,
+                     uint32_t *cols, double *vals);
+/* Validate and install a host CSR (matrix.hpp:520-605 load_csr): offsets[0]
+ * == 0, offsets[n_rows] == nnz, non-decreasing, in-range and strictly
+ * ascending columns per row; SPG_ERR_INVALID_ARGUMENT otherwise. */
+int spg_csr_load(spg_ctx *ctx, spg_csr *A, const uint64_t *offsets,
+                 const uint32_t *cols, const double *vals, uint64_t nnz);
+/* Deep copy into dst (reshaped to src's shape); tight, capacity == nnz
+ * (csr_storage_soa.hpp:44-56). */
+int spg_csr_copy(spg_ctx *ctx, const spg_csr *src, spg_csr *dst);
+/* Locked-mode point lookup (row.hpp:192-206 via csr_slice::binary_search,
+ * csr_storage_soa.hpp:94-104). */
+int spg_csr_get(spg_ctx *ctx, const spg_csr *A, uint64_t row, uint32_t col,
+                double *value, int *found);
+/* [begin, end) of one row in the CSR arrays (matrix.hpp row_nnz). */
+int spg_csr_row_range(spg_ctx *ctx, const spg_csr *A, uint64_t row,
+                      uint64_t *begin, uint64_t *end);
+
+/* ---- lock(): merge one epoch of staged inserts ---------------------------
+ * rows/cols/vals are the epoch's inserts in insertion order. Per (row, col)
+ * the last insert wins; a last value of +-0.0 deletes the entry; NaN is kept.
+ * First lock builds the CSR, later locks merge into it (matrix.hpp:277-342,
+ * aos_array_buffer.hpp:76-101, csr_build.hpp:32-98 and 126-488). Indices are
+ * range-checked on the device: SPG_ERR_OUT_OF_RANGE leaves A unchanged. */
+int spg_lock(spg_ctx *ctx, spg_csr *A, const uint32_t *rows,
+             const uint32_t *cols, const double *vals, uint64_t n_staged);
+/* Same with device-resident staging arrays. */
+int spg_lock_device(spg_ctx *ctx, spg_csr *A, const uint32_t *d_rows,
+                    const uint32_t *d_cols, const double *d_vals,
+                    uint64_t n_staged);
+
+/* ---- SpMV y = A x ----------------------------------------------------------
+ * spg_spmv: device x[n_cols], y[n_rows]; asynchronous on `stream`
+ * (serial/spmv.hpp:141-186, parallel/algorithms/spmv.hpp:125-161,
+ * kernel::sparse_dot_double kernels.h:5). SPG_ERR_LOGIC before the first lock. */
+int spg_spmv(spg_ctx *ctx, const spg_csr *A, const double *d_x, double *d_y,
+             int variant, void *stream);
+/* Host vectors with their lengths, as spmv(mat, x, y) takes std::vector:
+ * copies x in, runs, copies y out. x_len != n_cols or y_len != n_rows gives
+ * SPG_ERR_INVALID_ARGUMENT (serial/spmv.hpp:150-155). */
+int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
+                  uint64_t x_len, double *y, uint64_t y_len, int variant);
+/* The variant SPG_SPMV_AUTO resolves to for A. */
+int spg_spmv_selected(spg_ctx *ctx, const spg_csr *A, int *variant);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPG_H */

@@ -1,0 +1,286 @@
+"""spira_gb300 — Python binding of libspg.so, the GB300 engine behind Spira's
+sparse hot path (lock / SpMV / transpose / SpGEMM on device-resident CSR).
+
+The engine's public boundary is the C ABI in include/spg.h; the C++23 facade
+in include/spira_gb300/ mirrors Spira's own classes over it. This module is a
+thin ctypes binding of the same ABI for tests and the benchmark. There is no
+CPU fallback: importing works anywhere, but every compute call needs libspg.so
+and a GB300, and raises otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from collections import namedtuple
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libspg.so"
+
+SPMV_AUTO, SPMV_SCALAR, SPMV_VECTOR2, SPMV_VECTOR4, SPMV_VECTOR8, SPMV_VECTOR16, SPMV_VECTOR32, \
+    SPMV_STREAM, SPMV_MERGE = -1, 0, 1, 2, 3, 4, 5, 6, 7
+SPMV_VARIANTS = {
+    "scalar": 0, "vector2": 1, "vector4": 2, "vector8": 3, "vector16": 4, "vector32": 5,
+    "stream": 6, "merge": 7,
+}
+SPMV_NAMES = {v: k for k, v in SPMV_VARIANTS.items()}
+
+CsrHost = namedtuple("CsrHost", "n_rows n_cols off cols vals capacity")
+
+
+class SpgError(RuntimeError):
+    code = -1
+
+
+class InvalidArgument(SpgError, ValueError):
+    """std::invalid_argument in Spira."""
+    code = 1
+
+
+class LogicError(SpgError):
+    """std::logic_error in Spira."""
+    code = 2
+
+
+class OutOfRange(SpgError, IndexError):
+    """std::out_of_range in Spira."""
+    code = 3
+
+
+class NoMemory(SpgError, MemoryError):
+    code = 4
+
+
+class CudaError(SpgError):
+    code = 5
+
+
+class DeviceTimeout(SpgError):
+    code = 6
+
+
+class Unsupported(SpgError):
+    code = 7
+
+
+_ERRORS = {c.code: c for c in (InvalidArgument, LogicError, OutOfRange, NoMemory, CudaError, DeviceTimeout,
+                               Unsupported)}
+
+
+class _Info(C.Structure):
+    _fields_ = [("n_rows", C.c_uint64), ("n_cols", C.c_uint64), ("nnz", C.c_uint64),
+                ("capacity", C.c_uint64), ("built", C.c_int)]
+
+
+_lib = None
+
+# (name, restype, argtypes) of every symbol include/spg.h declares.
+_P = C.c_void_p
+_U64, _U32, _I = C.c_uint64, C.c_uint32, C.c_int
+_SIGS = [
+    ("spg_strerror", C.c_char_p, [_I]),
+    ("spg_last_error", C.c_char_p, []),
+    ("spg_version", _I, []),
+    ("spg_ctx_create", _I, [_I, C.POINTER(_P)]),
+    ("spg_ctx_destroy", _I, [_P]),
+    ("spg_ctx_stream", _I, [_P, C.POINTER(_P)]),
+    ("spg_ctx_sync", _I, [_P]),
+    ("spg_csr_create", _I, [_P, _U64, _U64, C.POINTER(_P)]),
+    ("spg_csr_destroy", _I, [_P]),
+    ("spg_csr_info_get", _I, [_P, C.POINTER(_Info)]),
+    ("spg_csr_device_arrays", _I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    ("spg_csr_download", _I, [_P, _P, _P, _P, _P]),
+    ("spg_csr_load", _I, [_P, _P, _P, _P, _P, _U64]),
+    ("spg_csr_copy", _I, [_P, _P, _P]),
+    ("spg_csr_get", _I, [_P, _P, _U64, _U32, C.POINTER(C.c_double), C.POINTER(_I)]),
+    ("spg_csr_row_range", _I, [_P, _P, _U64, C.POINTER(_U64), C.POINTER(_U64)]),
+    ("spg_lock", _I, [_P, _P, _P, _P, _P, _U64]),
+    ("spg_lock_device", _I, [_P, _P, _P, _P, _P, _U64]),
+    ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
+    ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
+    ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
+    # spg_gen.h
+    ("spg_gen_draw", _I, [_P, _U64, _U64, _U64, _U64, _I, _U64, _P]),
+    ("spg_gen_expand_rows", _I, [_P, _P, _U64, _P, C.POINTER(_U64)]),
+]
+
+
+def exported_symbols() -> list[str]:
+    return [s[0] for s in _SIGS]
+
+
+def lib():
+    """Load libspg.so (raises if it was not built: no fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(str(LIB_PATH))
+        for name, res, args in _SIGS:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != 0:
+        msg = lib().spg_last_error().decode(errors="replace")
+        raise _ERRORS.get(status, SpgError)(f"[{lib().spg_strerror(status).decode()}] {msg}")
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensors
+
+
+class Context:
+    """One device, one stream, the device memory pool (spg_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = _P()
+        _check(lib().spg_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().spg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        s = _P()
+        _check(lib().spg_ctx_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def sync(self):
+        _check(lib().spg_ctx_sync(self.h))
+
+
+class Csr:
+    """A device-resident CSR matrix handle (spg_csr)."""
+
+    def __init__(self, ctx: Context, n_rows: int, n_cols: int):
+        self.ctx = ctx
+        h = _P()
+        _check(lib().spg_csr_create(ctx.h, n_rows, n_cols, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().spg_csr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        i = _Info()
+        _check(lib().spg_csr_info_get(self.h, C.byref(i)))
+        return {"n_rows": i.n_rows, "n_cols": i.n_cols, "nnz": i.nnz, "capacity": i.capacity,
+                "built": bool(i.built)}
+
+    @property
+    def n_rows(self):
+        return self.info()["n_rows"]
+
+    @property
+    def n_cols(self):
+        return self.info()["n_cols"]
+
+    @property
+    def nnz(self):
+        return self.info()["nnz"]
+
+    def lock(self, rows, cols, vals):
+        """Merge one epoch of host-staged inserts (insertion order)."""
+        rows = np.ascontiguousarray(rows, dtype=np.uint32)
+        cols = np.ascontiguousarray(cols, dtype=np.uint32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        if not (len(rows) == len(cols) == len(vals)):
+            raise InvalidArgument("rows/cols/vals length mismatch")
+        _check(lib().spg_lock(self.ctx.h, self.h, _ptr(rows), _ptr(cols), _ptr(vals), len(rows)))
+
+    def lock_device(self, d_rows, d_cols, d_vals, n: int):
+        _check(lib().spg_lock_device(self.ctx.h, self.h, _ptr(d_rows), _ptr(d_cols), _ptr(d_vals), n))
+
+    def load(self, off, cols, vals):
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        cols = np.ascontiguousarray(cols, dtype=np.uint32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        _check(lib().spg_csr_load(self.ctx.h, self.h, _ptr(off), _ptr(cols), _ptr(vals), len(cols)))
+
+    def download(self) -> CsrHost:
+        i = self.info()
+        off = np.empty(i["n_rows"] + 1, np.uint64)
+        cols = np.empty(i["nnz"], np.uint32)
+        vals = np.empty(i["nnz"], np.float64)
+        _check(lib().spg_csr_download(self.ctx.h, self.h, _ptr(off), _ptr(cols), _ptr(vals)))
+        return CsrHost(i["n_rows"], i["n_cols"], off, cols, vals, i["capacity"])
+
+    def device_arrays(self):
+        o, c, v = _P(), _P(), _P()
+        _check(lib().spg_csr_device_arrays(self.h, C.byref(o), C.byref(c), C.byref(v)))
+        return o.value, c.value, v.value
+
+    def copy_from(self, other: "Csr"):
+        _check(lib().spg_csr_copy(self.ctx.h, other.h, self.h))
+
+    def get(self, row: int, col: int):
+        v, f = C.c_double(), C.c_int()
+        _check(lib().spg_csr_get(self.ctx.h, self.h, row, col, C.byref(v), C.byref(f)))
+        return (v.value if f.value else None)
+
+    def row_range(self, row: int):
+        b, e = C.c_uint64(), C.c_uint64()
+        _check(lib().spg_csr_row_range(self.ctx.h, self.h, row, C.byref(b), C.byref(e)))
+        return b.value, e.value
+
+    def spmv(self, d_x, d_y, variant: int = SPMV_AUTO, stream: int | None = None):
+        """Asynchronous y = A x on device pointers (ints or torch tensors)."""
+        _check(lib().spg_spmv(self.ctx.h, self.h, _ptr(d_x), _ptr(d_y), variant, stream))
+
+    def spmv_host(self, x, y=None, variant: int = SPMV_AUTO):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if y is None:
+            y = np.empty(self.n_rows, np.float64)
+        _check(lib().spg_spmv_host(self.ctx.h, self.h, _ptr(x), len(x), _ptr(y), len(y), variant))
+        return y
+
+    def selected_spmv(self) -> int:
+        v = C.c_int()
+        _check(lib().spg_spmv_selected(self.ctx.h, self.h, C.byref(v)))
+        return v.value
+
+
+# ---------------------------------------------------------------- device draws
+GEN_BELOW_U32, GEN_SYM_F64, GEN_UNIT_F64 = 0, 1, 2
+
+
+def gen_draw(ctx: Context, seed: int, stream: int, n: int, kind: int, bound: int, d_out, counter0: int = 0):
+    """Seeded draws on the device, equal to spira_gb300.gen on the host."""
+    _check(lib().spg_gen_draw(ctx.h, seed, stream, counter0, n, kind, bound, _ptr(d_out)))
+
+
+def gen_expand_rows(ctx: Context, d_lengths, n_rows: int, d_rows=None) -> int:
+    tot = C.c_uint64()
+    _check(lib().spg_gen_expand_rows(ctx.h, _ptr(d_lengths), n_rows, _ptr(d_rows), C.byref(tot)))
+    return tot.value

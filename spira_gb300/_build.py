@@ -1,0 +1,85 @@
+"""Build libspg.so (the sm_103a CUDA engine + its C ABI) in-tree.
+
+Every translation unit under spira_gb300/csrc is compiled for
+`-gencode arch=compute_103a,code=sm_103a` in parallel, then linked into
+spira_gb300/libspg.so. Objects go to spira_gb300/_build/. A source is rebuilt
+only when it, a header, or this script is newer than its object.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libspg.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found: the CUDA 13 toolkit is required to build libspg.so")
+    return cand
+
+
+def _flags() -> list[str]:
+    return [
+        "-std=c++17", "-O3", "-lineinfo", *ARCH,
+        "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
+        "-I", str(ROOT / "include"), "-I", str(CSRC),
+    ]
+
+
+def _headers_mtime() -> float:
+    hs = list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h")) + [Path(__file__)]
+    return max(h.stat().st_mtime for h in hs)
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    srcs = sorted(CSRC.glob("*.cu"))
+    hdr_t = _headers_mtime()
+    cc = nvcc()
+    jobs = []
+    for s in srcs:
+        o = BUILD / (s.stem + ".o")
+        if force or not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, hdr_t):
+            jobs.append((s, o))
+
+    def compile_one(so):
+        s, o = so
+        cmd = [cc, *_flags(), "-c", str(s), "-o", str(o)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {s.name}:\n{r.stdout}\n{r.stderr}")
+        if verbose and r.stderr.strip():
+            print(r.stderr, file=sys.stderr)
+        return o
+
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            list(ex.map(compile_one, jobs))
+    objs = [BUILD / (s.stem + ".o") for s in srcs]
+    if force or jobs or not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
+        tmp = LIB.with_suffix(".so.tmp")
+        cmd = [cc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", str(tmp), *map(str, objs), "-lcudart_static"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link of libspg.so failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))

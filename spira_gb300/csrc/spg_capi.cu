@@ -1,0 +1,384 @@
+// spg_capi.cu — the extern "C" surface of libspg.so: contexts, CSR handles,
+// host<->device transfer, load_csr validation, point lookup and SpMV entry
+// points. Lock lives in spg_lock.cu; kernels in spg_spmv.cu.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "spg_internal.cuh"
+
+namespace spg {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int Ctx::ensure_pinned(size_t bytes) {
+    if (pinned_bytes >= bytes) return SPG_OK;
+    if (pinned) cudaFreeHost(pinned);
+    pinned = nullptr;
+    pinned_bytes = 0;
+    SPG_CUDA_TRY(cudaMallocHost(&pinned, bytes));
+    pinned_bytes = bytes;
+    return SPG_OK;
+}
+
+int csr_alloc(Csr *A, uint64_t capacity, cudaStream_t s) {
+    SPG_TRY(A->cols.alloc(capacity * sizeof(uint32_t), s));
+    SPG_TRY(A->vals.alloc(capacity * sizeof(double), s));
+    A->capacity = capacity;
+    return SPG_OK;
+}
+
+namespace {
+
+__global__ void csr_get_kernel(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                               const double *__restrict__ vals, uint64_t row, uint32_t col,
+                               double *out_val, int *out_found) {
+    // csr_slice::binary_search (csr_storage_soa.hpp:94-104): lower_bound on
+    // the row's strictly ascending columns.
+    uint64_t lo = off[row], hi = off[row + 1];
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (cols[mid] < col) lo = mid + 1;
+        else hi = mid;
+    }
+    const bool found = lo < off[row + 1] && cols[lo] == col;
+    *out_found = found ? 1 : 0;
+    *out_val = found ? vals[lo] : 0.0;
+}
+
+}  // namespace
+}  // namespace spg
+
+using namespace spg;
+
+extern "C" {
+
+const char *spg_strerror(int status) {
+    switch (status) {
+        case SPG_OK: return "ok";
+        case SPG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case SPG_ERR_LOGIC: return "logic error (wrong mode)";
+        case SPG_ERR_OUT_OF_RANGE: return "index out of range";
+        case SPG_ERR_NO_MEMORY: return "out of device memory";
+        case SPG_ERR_CUDA: return "CUDA runtime error";
+        case SPG_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+        case SPG_ERR_UNSUPPORTED: return "unsupported";
+        default: return "unknown status";
+    }
+}
+
+const char *spg_last_error(void) { return g_last_error.c_str(); }
+
+int spg_version(void) { return 10000; }
+
+int spg_ctx_create(int device, spg_ctx **out) {
+    if (!out) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_create: out is null");
+    *out = nullptr;
+    int n = 0;
+    SPG_CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_create: device %d of %d", device, n);
+    SPG_CUDA_TRY(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    SPG_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    if (prop.major < 10)
+        return set_error(SPG_ERR_UNSUPPORTED, "spg_ctx_create: device %d is sm_%d%d; this build targets sm_103a",
+                         device, prop.major, prop.minor);
+    spg_ctx *c = new (std::nothrow) spg_ctx();
+    if (!c) return set_error(SPG_ERR_NO_MEMORY, "spg_ctx_create: host allocation failed");
+    c->device = device;
+    c->n_sms = prop.multiProcessorCount;
+    c->l2_bytes = prop.l2CacheSize;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&c->pool, device);
+    if (e == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+        e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->d_status) cudaFree(c->d_status);
+        delete c;
+        return set_error(SPG_ERR_CUDA, "spg_ctx_create: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return SPG_OK;
+}
+
+int spg_ctx_destroy(spg_ctx *c) {
+    if (!c) return SPG_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    c->xbuf.release();
+    c->ybuf.release();
+    cudaStreamSynchronize(c->stream);
+    if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->d_status) cudaFree(c->d_status);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SPG_OK;
+}
+
+int spg_ctx_stream(spg_ctx *c, void **stream) {
+    if (!c || !stream) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_stream: null argument");
+    *stream = c->stream;
+    return SPG_OK;
+}
+
+int spg_ctx_sync(spg_ctx *c) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_sync: null context");
+    SPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SPG_OK;
+}
+
+int spg_csr_create(spg_ctx *c, uint64_t n_rows, uint64_t n_cols, spg_csr **out) {
+    if (!c || !out) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_create: null argument");
+    if (n_rows > 0xFFFFFFFFull || n_cols > 0xFFFFFFFFull + 1ull)
+        return set_error(SPG_ERR_INVALID_ARGUMENT,
+                         "spg_csr_create: %llu x %llu exceeds uint32 row/column indices",
+                         (unsigned long long)n_rows, (unsigned long long)n_cols);
+    spg_csr *A = new (std::nothrow) spg_csr();
+    if (!A) return set_error(SPG_ERR_NO_MEMORY, "spg_csr_create: host allocation failed");
+    A->ctx = c;
+    A->n_rows = n_rows;
+    A->n_cols = n_cols;
+    *out = A;
+    return SPG_OK;
+}
+
+int spg_csr_destroy(spg_csr *A) {
+    if (!A) return SPG_OK;
+    cudaSetDevice(A->ctx->device);
+    delete A;  // DevBufs free stream-ordered
+    return SPG_OK;
+}
+
+int spg_csr_info_get(const spg_csr *A, spg_csr_info *info) {
+    if (!A || !info) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_info_get: null argument");
+    info->n_rows = A->n_rows;
+    info->n_cols = A->n_cols;
+    info->nnz = A->nnz;
+    info->capacity = A->capacity;
+    info->built = A->built ? 1 : 0;
+    return SPG_OK;
+}
+
+int spg_csr_device_arrays(const spg_csr *A, const uint64_t **offsets, const uint32_t **cols,
+                          const double **vals) {
+    if (!A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_device_arrays: null matrix");
+    if (offsets) *offsets = A->d_off();
+    if (cols) *cols = A->d_cols();
+    if (vals) *vals = A->d_vals();
+    return SPG_OK;
+}
+
+int spg_csr_download(spg_ctx *c, const spg_csr *A, uint64_t *offsets, uint32_t *cols, double *vals) {
+    if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_download: null argument");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spg_csr_download: CSR not built (lock first)");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    if (offsets)
+        SPG_CUDA_TRY(cudaMemcpyAsync(offsets, A->d_off(), (A->n_rows + 1) * sizeof(uint64_t),
+                                     cudaMemcpyDeviceToHost, s));
+    if (cols && A->nnz)
+        SPG_CUDA_TRY(cudaMemcpyAsync(cols, A->d_cols(), A->nnz * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (vals && A->nnz)
+        SPG_CUDA_TRY(cudaMemcpyAsync(vals, A->d_vals(), A->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+int spg_csr_load(spg_ctx *c, spg_csr *A, const uint64_t *offsets, const uint32_t *cols,
+                 const double *vals, uint64_t nnz) {
+    if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_load: null handle");
+    // Validation in the order of matrix::load_csr (matrix.hpp:524-575).
+    if (!offsets) return set_error(SPG_ERR_INVALID_ARGUMENT, "spira::matrix::load_csr: CSR offsets array is null");
+    if (offsets[0] != 0)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spira::matrix::load_csr: CSR offsets[0] must be zero");
+    if (offsets[A->n_rows] != nnz)
+        return set_error(SPG_ERR_INVALID_ARGUMENT,
+                         "spira::matrix::load_csr: CSR offsets[n_rows] does not equal nnz");
+    if (nnz && (!cols || !vals))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_load: cols/vals null with nnz > 0");
+    bool has_zero = false;
+    for (uint64_t i = 0; i < A->n_rows; ++i) {
+        const uint64_t beg = offsets[i], end = offsets[i + 1];
+        if (beg > end)
+            return set_error(SPG_ERR_INVALID_ARGUMENT,
+                             "spira::matrix::load_csr: CSR offsets are not non-decreasing");
+        if (end > nnz)
+            return set_error(SPG_ERR_INVALID_ARGUMENT,
+                             "spira::matrix::load_csr: CSR offsets are not non-decreasing");
+        for (uint64_t k = beg; k < end; ++k) {
+            if ((uint64_t)cols[k] >= A->n_cols)
+                return set_error(SPG_ERR_INVALID_ARGUMENT,
+                                 "spira::matrix::load_csr: column index out of bounds");
+            if (k > beg && cols[k] <= cols[k - 1])
+                return set_error(SPG_ERR_INVALID_ARGUMENT,
+                                 "spira::matrix::load_csr: CSR row entries are not strictly sorted by column");
+            if (vals[k] == 0.0) has_zero = true;
+        }
+    }
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    DevBuf off, cb, vb;
+    SPG_TRY(off.alloc((A->n_rows + 1) * sizeof(uint64_t), s));
+    SPG_TRY(cb.alloc(nnz * sizeof(uint32_t), s));
+    SPG_TRY(vb.alloc(nnz * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, offsets, (A->n_rows + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    if (nnz) {
+        SPG_CUDA_TRY(cudaMemcpyAsync(cb.ptr, cols, nnz * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(vb.ptr, vals, nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    A->invalidate_derived();
+    A->off = std::move(off);
+    A->cols = std::move(cb);
+    A->vals = std::move(vb);
+    A->nnz = nnz;
+    A->capacity = nnz;
+    A->built = true;
+    A->may_have_zeros = has_zero;
+    return SPG_OK;
+}
+
+int spg_csr_copy(spg_ctx *c, const spg_csr *src, spg_csr *dst) {
+    if (!c || !src || !dst) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_copy: null handle");
+    if (src == dst) return SPG_OK;
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    dst->invalidate_derived();
+    dst->n_rows = src->n_rows;
+    dst->n_cols = src->n_cols;
+    dst->built = src->built;
+    dst->nnz = src->nnz;
+    dst->may_have_zeros = src->may_have_zeros;
+    if (!src->built) {
+        dst->off.release();
+        dst->cols.release();
+        dst->vals.release();
+        dst->capacity = 0;
+        return SPG_OK;
+    }
+    DevBuf off, cb, vb;
+    SPG_TRY(off.alloc((src->n_rows + 1) * sizeof(uint64_t), s));
+    SPG_TRY(cb.alloc(src->nnz * sizeof(uint32_t), s));
+    SPG_TRY(vb.alloc(src->nnz * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, src->d_off(), (src->n_rows + 1) * sizeof(uint64_t),
+                                 cudaMemcpyDeviceToDevice, s));
+    if (src->nnz) {
+        SPG_CUDA_TRY(cudaMemcpyAsync(cb.ptr, src->d_cols(), src->nnz * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(vb.ptr, src->d_vals(), src->nnz * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    dst->off = std::move(off);
+    dst->cols = std::move(cb);
+    dst->vals = std::move(vb);
+    dst->capacity = src->nnz;
+    return SPG_OK;
+}
+
+int spg_csr_get(spg_ctx *c, const spg_csr *A, uint64_t row, uint32_t col, double *value, int *found) {
+    if (!c || !A || !value || !found) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_get: null argument");
+    if (row >= A->n_rows) return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: row_index out of range");
+    if ((uint64_t)col >= A->n_cols) return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: col_index out of range");
+    if (!A->built) {
+        *value = 0.0;
+        *found = 0;
+        return SPG_OK;
+    }
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    DevBuf out;
+    SPG_TRY(out.alloc(16, s));
+    csr_get_kernel<<<1, 1, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), row, col, out.as<double>(),
+                                   reinterpret_cast<int *>(out.as<char>() + 8));
+    SPG_LAUNCH_CHECK();
+    char h[16];
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, out.ptr, 16, cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    memcpy(value, h, 8);
+    memcpy(found, h + 8, 4);
+    return SPG_OK;
+}
+
+int spg_csr_row_range(spg_ctx *c, const spg_csr *A, uint64_t row, uint64_t *begin, uint64_t *end) {
+    if (!c || !A || !begin || !end) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_row_range: null argument");
+    if (row >= A->n_rows) return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: row_index out of range");
+    if (!A->built) {
+        *begin = *end = 0;
+        return SPG_OK;
+    }
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    uint64_t h[2];
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, A->d_off() + row, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, c->stream));
+    SPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    *begin = h[0];
+    *end = h[1];
+    return SPG_OK;
+}
+
+int spg_spmv(spg_ctx *c, const spg_csr *Ac, const double *d_x, double *d_y, int variant, void *stream) {
+    if (!c || !Ac) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv: null handle");
+    spg_csr *A = const_cast<spg_csr *>(Ac);  // plans are cached on the handle
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    if ((A->n_cols && !d_x) || (A->n_rows && !d_y))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv: null vector");
+    if (variant < SPG_SPMV_AUTO || variant >= SPG_SPMV_N_VARIANTS)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv: unknown variant %d", variant);
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (variant == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &variant));
+    return spmv_launch(c, A, d_x, d_y, variant, pick_stream(c, stream));
+}
+
+int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,
+                  int variant) {
+    if (!c || !Ac) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: null handle");
+    // Checks in the order of serial/spmv.hpp:150-158.
+    if (x_len != Ac->n_cols)
+        return set_error(SPG_ERR_INVALID_ARGUMENT,
+                         "The size of the input vector x does not match the number of columns of the matrix");
+    if (y_len != Ac->n_rows)
+        return set_error(SPG_ERR_INVALID_ARGUMENT,
+                         "The size of the output vector y does not match the number of rows of the matrix");
+    if (!Ac->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    if ((x_len && !x) || (y_len && !y)) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: null vector");
+    spg_csr *A = const_cast<spg_csr *>(Ac);
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    if (variant == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &variant));
+    if (variant < 0 || variant >= SPG_SPMV_N_VARIANTS)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: unknown variant %d", variant);
+    if (c->xbuf.bytes < x_len * sizeof(double)) SPG_TRY(c->xbuf.alloc(x_len * sizeof(double), s));
+    if (c->ybuf.bytes < y_len * sizeof(double)) SPG_TRY(c->ybuf.alloc(y_len * sizeof(double), s));
+    if (x_len)
+        SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
+    SPG_TRY(spmv_launch(c, A, c->xbuf.as<double>(), c->ybuf.as<double>(), variant, s));
+    if (y_len)
+        SPG_CUDA_TRY(cudaMemcpyAsync(y, c->ybuf.ptr, y_len * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+int spg_spmv_selected(spg_ctx *c, const spg_csr *Ac, int *variant) {
+    if (!c || !Ac || !variant) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_selected: null argument");
+    if (!Ac->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return spmv_resolve_auto(c, const_cast<spg_csr *>(Ac), variant);
+}
+
+}  // extern "C"

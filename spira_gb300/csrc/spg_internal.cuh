@@ -1,0 +1,180 @@
+// spg_internal.cuh — shared internals of libspg.so: handles, error plumbing,
+// device buffers and the device-wide primitives (scan, radix sort) that the
+// lock / transpose / SpGEMM kernels are built from.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/spg.h"
+
+namespace spg {
+
+// ---------------------------------------------------------------------------
+// Errors. Every C entry point returns a status; the detail text goes to a
+// thread-local string read back by spg_last_error().
+// ---------------------------------------------------------------------------
+int set_error(int code, const char *fmt, ...);
+void clear_error();
+
+struct Status {
+    int code = SPG_OK;
+    bool ok() const { return code == SPG_OK; }
+};
+
+#define SPG_CUDA_TRY(expr)                                                          \
+    do {                                                                            \
+        cudaError_t _e = (expr);                                                    \
+        if (_e != cudaSuccess) {                                                    \
+            if (_e == cudaErrorMemoryAllocation) {                                  \
+                cudaGetLastError();                                                 \
+                return ::spg::set_error(SPG_ERR_NO_MEMORY, "%s: %s (%s:%d)", #expr, \
+                                        cudaGetErrorString(_e), __FILE__, __LINE__); \
+            }                                                                       \
+            return ::spg::set_error(SPG_ERR_CUDA, "%s: %s (%s:%d)", #expr,          \
+                                    cudaGetErrorString(_e), __FILE__, __LINE__);    \
+        }                                                                           \
+    } while (0)
+
+#define SPG_TRY(expr)                      \
+    do {                                   \
+        int _s = (expr);                   \
+        if (_s != SPG_OK) return _s;       \
+    } while (0)
+
+#define SPG_LAUNCH_CHECK() SPG_CUDA_TRY(cudaPeekAtLastError())
+
+// ---------------------------------------------------------------------------
+// Handles
+// ---------------------------------------------------------------------------
+struct Ctx;
+
+// Stream-ordered device buffer from the context's memory pool.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept { *this = std::move(o); }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) {
+            release();
+            ptr = o.ptr; bytes = o.bytes; stream = o.stream;
+            o.ptr = nullptr; o.bytes = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    int alloc(size_t n, cudaStream_t s);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// Cached SpMV plan (row blocks for the stream / merge variants).
+struct SpmvPlan {
+    int kind = -1;           // variant the plan belongs to
+    uint64_t n_items = 0;    // number of work items (blocks / tiles)
+    DevBuf items;            // variant-specific item descriptors
+    DevBuf aux;              // variant-specific scratch (carry-outs)
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    int n_sms = 0;
+    size_t l2_bytes = 0;
+    // Device status word written by kernels with bounded waits; 0 = ok.
+    unsigned int *d_status = nullptr;
+    // Pinned host staging for the *_host entry points.
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+    int ensure_pinned(size_t bytes);
+    // Device vectors reused by spg_spmv_host.
+    DevBuf xbuf, ybuf;
+};
+
+struct Csr {
+    Ctx *ctx = nullptr;
+    uint64_t n_rows = 0, n_cols = 0;
+    uint64_t nnz = 0, capacity = 0;
+    bool built = false;
+    // True when load_csr installed explicit +-0.0 values (only load_csr can:
+    // lock and SpGEMM never store zeros). The merge then drops them from the
+    // rows it touches, as csr_build.hpp:274-301 does.
+    bool may_have_zeros = false;
+    DevBuf off;   // uint64_t[n_rows + 1]
+    DevBuf cols;  // uint32_t[capacity]
+    DevBuf vals;  // double[capacity]
+    // Row-length statistics for the selector (computed lazily).
+    bool stats_valid = false;
+    uint64_t max_row = 0;
+    int selected_spmv = -1;
+    SpmvPlan plan_stream, plan_merge;
+    void invalidate_derived() {
+        stats_valid = false;
+        selected_spmv = -1;
+        plan_stream = SpmvPlan{};
+        plan_merge = SpmvPlan{};
+    }
+    const uint64_t *d_off() const { return off.as<uint64_t>(); }
+    const uint32_t *d_cols() const { return cols.as<uint32_t>(); }
+    const double *d_vals() const { return vals.as<double>(); }
+};
+
+inline cudaStream_t pick_stream(Ctx *c, void *s) {
+    return s ? static_cast<cudaStream_t>(s) : c->stream;
+}
+
+inline int bits_for(uint64_t n) {  // bits needed to represent 0..n-1
+    int b = 0;
+    while (b < 64 && (n - 1) >> b) ++b;
+    return n <= 1 ? 0 : b;
+}
+
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 1u << 30) {
+    uint64_t g = (n + block - 1) / block;
+    if (g == 0) g = 1;
+    if (g > cap) g = cap;
+    return static_cast<unsigned>(g);
+}
+
+// ---------------------------------------------------------------------------
+// Device-wide primitives (spg_prims.cu)
+// ---------------------------------------------------------------------------
+// Exclusive scan of n uint64 values in place; writes the total to *d_total
+// (device pointer, may be null). Temporary memory from the context pool.
+int exclusive_scan_u64(Ctx *c, uint64_t *d_data, uint64_t n, uint64_t *d_total,
+                       cudaStream_t s);
+// Exclusive scan of int64 (signed) values in place.
+int exclusive_scan_i64(Ctx *c, int64_t *d_data, uint64_t n, cudaStream_t s);
+// Stable LSD radix sort of 64-bit keys carrying a 32-bit payload, on the low
+// `key_bits` bits. Inputs are consumed; results land in (keys, vals) again.
+int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
+                         int key_bits, cudaStream_t s);
+// Device reduction: max over uint32 array (returns through *h_max, syncs).
+int reduce_max_u32(Ctx *c, const uint32_t *d, uint64_t n, uint32_t *h_max,
+                   cudaStream_t s);
+
+// CSR helpers used by several ops (spg_lock.cu).
+int csr_alloc(Csr *A, uint64_t capacity, cudaStream_t s);
+int csr_row_stats(Ctx *c, Csr *A, cudaStream_t s);
+
+// SpMV dispatch (spg_spmv.cu).
+int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant,
+                cudaStream_t s);
+int spmv_resolve_auto(Ctx *c, Csr *A, int *variant);
+
+}  // namespace spg
+
+// Opaque C handle types are the internal structs.
+struct spg_ctx : spg::Ctx {};
+struct spg_csr : spg::Csr {};

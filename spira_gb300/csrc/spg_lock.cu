@@ -1,0 +1,424 @@
+// spg_lock.cu — lock(): merge one epoch of staged inserts into the CSR.
+//
+// Spira's lock (matrix.hpp:277-342) sorts and dedups every row buffer keeping
+// the last write and keeping zeros (aos_array_buffer.hpp:76-101: reverse +
+// stable_sort + first-of-run), then either builds the CSR dropping zeros
+// (csr_build.hpp:32-98) or two-pointer-merges each dirty row with its old CSR
+// slice, the buffer winning on equal columns and a zero deleting
+// (csr_build.hpp:126-488). The GPU formulation computes the same CSR:
+//
+//   1. keys (row << cbits | col) with the staging index as payload go through
+//      a stable LSD radix sort; the last element of each equal-key run is the
+//      last write (stability keeps insertion order within a run);
+//   2. the deduplicated delta D (sorted by row, col; zeros kept) gets row
+//      offsets doff by lower_bound per row;
+//   3. every delta entry j finds its insertion point ins[j] in its old row and
+//      whether it collides; contrib[j] = +1 (new non-zero), -1 (zero that
+//      deletes an old entry) or 0; P = exclusive scan of contrib;
+//   4. new row counts = old count + P[doff[r+1]] - P[doff[r]]; scan -> offsets;
+//   5. old entry (row r, position p, column c): dropped if D holds (r, c),
+//      else written to new_off[r] + p + (P[j] - P[doff[r]]) with j the first
+//      delta entry of row r with column >= c; delta entry j (non-zero) to
+//      new_off[r] + ins[j] + (P[j] - P[doff[r]]).
+// Everything is integer work or a copy of the value bits, so structure and
+// values are bit-exact against Spira. The first lock is the same pass with an
+// empty old CSR. Capacity follows Spira's rule: the first build is tight;
+// a merge keeps the old capacity when old nnz + |D| fits, else grows to 1.5x
+// that bound (csr_build.hpp:139-145).
+#include "spg_internal.cuh"
+
+namespace spg {
+namespace {
+
+constexpr int LB = 256;
+
+__device__ __forceinline__ bool is_zero(double v) { return fabs(v) <= 0.0; }  // traits.hpp:73-80
+
+__global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
+                               uint64_t m, int cbits, uint64_t *__restrict__ keys,
+                               uint32_t *__restrict__ idx) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        keys[i] = ((uint64_t)rows[i] << cbits) | cols[i];
+        idx[i] = (uint32_t)i;
+    }
+}
+
+// flag[i] = 1 iff sorted key i is the last of its run (the last write).
+__global__ void lock_last_flags(const uint64_t *__restrict__ keys, uint64_t m, uint64_t *__restrict__ flag) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        flag[i] = (i + 1 == m || keys[i] != keys[i + 1]) ? 1 : 0;
+}
+
+__global__ void lock_gather_delta(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx,
+                                  const uint64_t *__restrict__ pos, uint64_t m, int cbits,
+                                  const double *__restrict__ vals, uint32_t *__restrict__ drow,
+                                  uint32_t *__restrict__ dcol, double *__restrict__ dval) {
+    const uint64_t cmask = cbits ? ((1ull << cbits) - 1) : 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i + 1 == m || keys[i] != keys[i + 1]) {
+            const uint64_t j = pos[i];
+            drow[j] = (uint32_t)(keys[i] >> cbits);
+            dcol[j] = (uint32_t)(keys[i] & cmask);
+            dval[j] = vals[idx[i]];
+        }
+    }
+}
+
+// off[r] = lower_bound(sorted_rows[0..u), r) for r in [0, n_rows].
+__global__ void offsets_from_sorted_rows(const uint32_t *__restrict__ srows, uint64_t u, uint64_t n_rows,
+                                         uint64_t *__restrict__ off) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r <= n_rows;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t lo = 0, hi = u;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if ((uint64_t)srows[mid] < r) lo = mid + 1;
+            else hi = mid;
+        }
+        off[r] = lo;
+    }
+}
+
+// Step 3: insertion point / collision / contribution of every delta entry.
+__global__ void merge_delta_probe(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                                  bool has_old, const uint32_t *__restrict__ drow,
+                                  const uint32_t *__restrict__ dcol, const double *__restrict__ dval,
+                                  uint64_t u, uint32_t *__restrict__ ins, int64_t *__restrict__ contrib) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < u;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const bool z = is_zero(dval[j]);
+        bool coll = false;
+        uint64_t p = 0;
+        if (has_old) {
+            const uint64_t b = off[drow[j]], e = off[drow[j] + 1];
+            const uint32_t c = dcol[j];
+            uint64_t lo = b, hi = e;
+            while (lo < hi) {
+                const uint64_t mid = (lo + hi) >> 1;
+                if (cols[mid] < c) lo = mid + 1;
+                else hi = mid;
+            }
+            coll = lo < e && cols[lo] == c;
+            p = lo - b;
+        }
+        ins[j] = (uint32_t)p;
+        contrib[j] = (!z && !coll) ? 1 : ((z && coll) ? -1 : 0);
+    }
+}
+
+// Step 4 (before the scan): new row counts; cnt[n_rows] = 0.
+__global__ void merge_row_counts(const uint64_t *__restrict__ off, bool has_old,
+                                 const uint64_t *__restrict__ doff, const int64_t *__restrict__ P,
+                                 uint64_t n_rows, uint64_t *__restrict__ cnt) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r <= n_rows;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        if (r == n_rows) {
+            cnt[r] = 0;
+            continue;
+        }
+        const int64_t old_cnt = has_old ? (int64_t)(off[r + 1] - off[r]) : 0;
+        cnt[r] = (uint64_t)(old_cnt + (P[doff[r + 1]] - P[doff[r]]));
+    }
+}
+
+// Step 5a: old entries, CTA chunks of MO_CHUNK; the row of each entry is found
+// by binary search inside the chunk's row window.
+constexpr int MO_CHUNK = 2048;
+
+__device__ __forceinline__ uint64_t row_of(const uint64_t *__restrict__ off, uint64_t lo, uint64_t hi,
+                                           uint64_t k) {
+    // largest r in [lo, hi] with off[r] <= k
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= k) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(LB)
+merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                const double *__restrict__ vals, uint64_t n_rows, uint64_t nnz_old,
+                const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dcol,
+                const int64_t *__restrict__ P, const uint64_t *__restrict__ new_off,
+                uint32_t *__restrict__ out_cols, double *__restrict__ out_vals) {
+    __shared__ uint64_t win[2];
+    const uint64_t k0 = (uint64_t)blockIdx.x * MO_CHUNK;
+    const uint64_t k1 = min(k0 + (uint64_t)MO_CHUNK, nnz_old);
+    if (threadIdx.x == 0) {
+        win[0] = row_of(off, 0, n_rows, k0);
+        win[1] = row_of(off, win[0], n_rows, k1 - 1);
+    }
+    __syncthreads();
+    const uint64_t rlo = win[0], rhi = win[1];
+    for (uint64_t k = k0 + threadIdx.x; k < k1; k += LB) {
+        const uint64_t r = row_of(off, rlo, rhi, k);
+        const uint64_t p = k - off[r];
+        const uint32_t c = cols[k];
+        const uint64_t ds = doff[r], de = doff[r + 1];
+        uint64_t dst = new_off[r] + p;
+        if (ds != de) {
+            uint64_t lo = ds, hi = de;
+            while (lo < hi) {
+                const uint64_t mid = (lo + hi) >> 1;
+                if (dcol[mid] < c) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo < de && dcol[lo] == c) continue;  // replaced or deleted by the delta
+            dst += (uint64_t)(P[lo] - P[ds]);
+        }
+        out_cols[dst] = c;
+        out_vals[dst] = vals[k];
+    }
+}
+
+// Step 5b: non-zero delta entries.
+__global__ void merge_write_delta(const uint32_t *__restrict__ drow, const uint32_t *__restrict__ dcol,
+                                  const double *__restrict__ dval, const uint32_t *__restrict__ ins,
+                                  const uint64_t *__restrict__ doff, const int64_t *__restrict__ P, uint64_t u,
+                                  const uint64_t *__restrict__ new_off, uint32_t *__restrict__ out_cols,
+                                  double *__restrict__ out_vals) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < u;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const double v = dval[j];
+        if (is_zero(v)) continue;
+        const uint32_t r = drow[j];
+        const uint64_t dst = new_off[r] + ins[j] + (uint64_t)(P[j] - P[doff[r]]);
+        out_cols[dst] = dcol[j];
+        out_vals[dst] = v;
+    }
+}
+
+// Explicit zeros of a loaded CSR inside rows the delta touches: Spira's merge
+// drops them (csr_build.hpp:274-276, 292-296). They become synthetic zero
+// inserts placed before the real ones, so a real insert on the same column
+// still wins the last-write dedup.
+__global__ void zero_entries_in_dirty_rows(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                                           const double *__restrict__ vals, uint64_t n_rows,
+                                           const uint64_t *__restrict__ doff, uint64_t *__restrict__ flag,
+                                           uint32_t *__restrict__ zrow, uint32_t *__restrict__ zcol,
+                                           const uint64_t *__restrict__ pos, int pass) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n_rows;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        const bool dirty = doff[r] != doff[r + 1];
+        for (uint64_t k = off[r]; k < off[r + 1]; ++k) {
+            const bool z = dirty && is_zero(vals[k]);
+            if (pass == 0) {
+                flag[k] = z ? 1 : 0;
+            } else if (z) {
+                zrow[pos[k]] = (uint32_t)r;
+                zcol[pos[k]] = cols[k];
+            }
+        }
+    }
+}
+
+__global__ void fill_f64(double *p, uint64_t n, double v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// Delta arrays (sorted by (row, col), one entry per key, zeros kept).
+struct Delta {
+    uint64_t u = 0;
+    DevBuf row, col, val;
+};
+
+int sort_dedup(Ctx *c, const uint32_t *rows, const uint32_t *cols, const double *vals, uint64_t m,
+               uint64_t n_rows, uint64_t n_cols, Delta &D, cudaStream_t s) {
+    const int cbits = bits_for(n_cols), rbits = bits_for(n_rows);
+    const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
+    DevBuf keys, idx, pos;
+    SPG_TRY(keys.alloc(m * sizeof(uint64_t), s));
+    SPG_TRY(idx.alloc(m * sizeof(uint32_t), s));
+    lock_make_keys<<<g, LB, 0, s>>>(rows, cols, m, cbits, keys.as<uint64_t>(), idx.as<uint32_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(radix_sort_pairs_u64(c, keys.as<uint64_t>(), idx.as<uint32_t>(), m, rbits + cbits, s));
+    SPG_TRY(pos.alloc((m + 1) * sizeof(uint64_t), s));
+    lock_last_flags<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, pos.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_u64(c, pos.as<uint64_t>(), m, pos.as<uint64_t>() + m, s));
+    uint64_t u = 0;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&u, pos.as<uint64_t>() + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    D.u = u;
+    SPG_TRY(D.row.alloc(u * sizeof(uint32_t), s));
+    SPG_TRY(D.col.alloc(u * sizeof(uint32_t), s));
+    SPG_TRY(D.val.alloc(u * sizeof(double), s));
+    lock_gather_delta<<<g, LB, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), pos.as<uint64_t>(), m, cbits,
+                                       vals, D.row.as<uint32_t>(), D.col.as<uint32_t>(), D.val.as<double>());
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int row_offsets(Ctx *c, const uint32_t *srows, uint64_t u, uint64_t n_rows, DevBuf &doff, cudaStream_t s) {
+    SPG_TRY(doff.alloc((n_rows + 1) * sizeof(uint64_t), s));
+    offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+        srows, u, n_rows, doff.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+}  // namespace
+
+// The lock proper, on device-resident staging arrays.
+static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const double *vals,
+                            uint64_t m, cudaStream_t s) {
+    // Range checks first: a failure leaves A untouched (matrix.hpp:161-171).
+    if (m) {
+        uint32_t mr = 0, mc = 0;
+        SPG_TRY(reduce_max_u32(c, rows, m, &mr, s));
+        SPG_TRY(reduce_max_u32(c, cols, m, &mc, s));
+        if ((uint64_t)mr >= A->n_rows)
+            return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: row_index out of range (%u >= %llu)", mr,
+                             (unsigned long long)A->n_rows);
+        if ((uint64_t)mc >= A->n_cols)
+            return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: col_index out of range (%u >= %llu)", mc,
+                             (unsigned long long)A->n_cols);
+    }
+    if (m >= (1ull << 32))
+        return set_error(SPG_ERR_UNSUPPORTED, "lock: %llu staged inserts exceed 2^32-1 per epoch",
+                         (unsigned long long)m);
+    const uint64_t n = A->n_rows;
+    const bool has_old = A->built;
+    if (has_old && m == 0) return SPG_OK;  // no dirty row: Spira's merge leaves the CSR as it is
+
+    Delta D;
+    if (m) SPG_TRY(sort_dedup(c, rows, cols, vals, m, n, A->n_cols, D, s));
+    DevBuf doff;
+    SPG_TRY(row_offsets(c, D.row.as<uint32_t>(), D.u, n, doff, s));
+
+    if (has_old && A->may_have_zeros && A->nnz) {
+        // Fold explicit old zeros of dirty rows into the delta as deletes.
+        DevBuf zpos;
+        SPG_TRY(zpos.alloc((A->nnz + 1) * sizeof(uint64_t), s));
+        const unsigned gz = grid_for(n, LB, (unsigned)c->n_sms * 32);
+        zero_entries_in_dirty_rows<<<gz, LB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), n, doff.as<uint64_t>(),
+                                                     zpos.as<uint64_t>(), nullptr, nullptr, nullptr, 0);
+        SPG_LAUNCH_CHECK();
+        SPG_TRY(exclusive_scan_u64(c, zpos.as<uint64_t>(), A->nnz, zpos.as<uint64_t>() + A->nnz, s));
+        uint64_t nz = 0;
+        SPG_CUDA_TRY(cudaMemcpyAsync(&nz, zpos.as<uint64_t>() + A->nnz, 8, cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (nz) {
+            const uint64_t m2 = nz + D.u;
+            DevBuf r2, c2, v2;
+            SPG_TRY(r2.alloc(m2 * sizeof(uint32_t), s));
+            SPG_TRY(c2.alloc(m2 * sizeof(uint32_t), s));
+            SPG_TRY(v2.alloc(m2 * sizeof(double), s));
+            zero_entries_in_dirty_rows<<<gz, LB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), n,
+                                                         doff.as<uint64_t>(), nullptr, r2.as<uint32_t>(),
+                                                         c2.as<uint32_t>(), zpos.as<uint64_t>(), 1);
+            SPG_LAUNCH_CHECK();
+            fill_f64<<<grid_for(nz, LB, 4096), LB, 0, s>>>(v2.as<double>(), nz, 0.0);
+            SPG_LAUNCH_CHECK();
+            if (D.u) {
+                SPG_CUDA_TRY(cudaMemcpyAsync(r2.as<uint32_t>() + nz, D.row.ptr, D.u * 4, cudaMemcpyDeviceToDevice, s));
+                SPG_CUDA_TRY(cudaMemcpyAsync(c2.as<uint32_t>() + nz, D.col.ptr, D.u * 4, cudaMemcpyDeviceToDevice, s));
+                SPG_CUDA_TRY(cudaMemcpyAsync(v2.as<double>() + nz, D.val.ptr, D.u * 8, cudaMemcpyDeviceToDevice, s));
+            }
+            Delta D2;
+            SPG_TRY(sort_dedup(c, r2.as<uint32_t>(), c2.as<uint32_t>(), v2.as<double>(), m2, n, A->n_cols, D2, s));
+            D = std::move(D2);
+            SPG_TRY(row_offsets(c, D.row.as<uint32_t>(), D.u, n, doff, s));
+        }
+    }
+
+    const uint64_t u = D.u;
+    DevBuf ins, P;
+    SPG_TRY(ins.alloc((u ? u : 1) * sizeof(uint32_t), s));
+    SPG_TRY(P.alloc((u + 1) * sizeof(int64_t), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(P.as<int64_t>() + u, 0, sizeof(int64_t), s));
+    if (u) {
+        merge_delta_probe<<<grid_for(u, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+            A->d_off(), A->d_cols(), has_old, D.row.as<uint32_t>(), D.col.as<uint32_t>(), D.val.as<double>(), u,
+            ins.as<uint32_t>(), P.as<int64_t>());
+        SPG_LAUNCH_CHECK();
+    }
+    SPG_TRY(exclusive_scan_i64(c, P.as<int64_t>(), u + 1, s));
+
+    DevBuf new_off;
+    SPG_TRY(new_off.alloc((n + 1) * sizeof(uint64_t), s));
+    merge_row_counts<<<grid_for(n + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+        A->d_off(), has_old, doff.as<uint64_t>(), P.as<int64_t>(), n, new_off.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_u64(c, new_off.as<uint64_t>(), n + 1, nullptr, s));
+    uint64_t new_nnz = 0;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&new_nnz, new_off.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+
+    uint64_t cap;
+    if (!has_old) {
+        cap = new_nnz;  // build_csr: exact
+    } else {
+        const uint64_t total_ub = A->nnz + u;
+        cap = (total_ub <= A->capacity) ? A->capacity : total_ub + total_ub / 2;
+    }
+    DevBuf out_cols, out_vals;
+    SPG_TRY(out_cols.alloc(cap * sizeof(uint32_t), s));
+    SPG_TRY(out_vals.alloc(cap * sizeof(double), s));
+    if (has_old && A->nnz) {
+        const uint64_t chunks = (A->nnz + MO_CHUNK - 1) / MO_CHUNK;
+        merge_write_old<<<(unsigned)chunks, LB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), n, A->nnz,
+                                                        doff.as<uint64_t>(), D.col.as<uint32_t>(), P.as<int64_t>(),
+                                                        new_off.as<uint64_t>(), out_cols.as<uint32_t>(),
+                                                        out_vals.as<double>());
+        SPG_LAUNCH_CHECK();
+    }
+    if (u) {
+        merge_write_delta<<<grid_for(u, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+            D.row.as<uint32_t>(), D.col.as<uint32_t>(), D.val.as<double>(), ins.as<uint32_t>(), doff.as<uint64_t>(),
+            P.as<int64_t>(), u, new_off.as<uint64_t>(), out_cols.as<uint32_t>(), out_vals.as<double>());
+        SPG_LAUNCH_CHECK();
+    }
+    A->invalidate_derived();
+    A->off = std::move(new_off);
+    A->cols = std::move(out_cols);
+    A->vals = std::move(out_vals);
+    A->nnz = new_nnz;
+    A->capacity = cap;
+    A->built = true;
+    // Zeros of dirty rows were consumed; clean rows may still hold loaded zeros.
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+}  // namespace spg
+
+using namespace spg;
+
+extern "C" {
+
+int spg_lock_device(spg_ctx *c, spg_csr *A, const uint32_t *d_rows, const uint32_t *d_cols, const double *d_vals,
+                    uint64_t n_staged) {
+    if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock_device: null handle");
+    if (n_staged && (!d_rows || !d_cols || !d_vals))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock_device: null staging array");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return lock_device_impl(c, A, d_rows, d_cols, d_vals, n_staged, c->stream);
+}
+
+int spg_lock(spg_ctx *c, spg_csr *A, const uint32_t *rows, const uint32_t *cols, const double *vals,
+             uint64_t n_staged) {
+    if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock: null handle");
+    if (n_staged && (!rows || !cols || !vals))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock: null staging array");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    DevBuf r, cl, v;
+    if (n_staged) {
+        SPG_TRY(r.alloc(n_staged * sizeof(uint32_t), s));
+        SPG_TRY(cl.alloc(n_staged * sizeof(uint32_t), s));
+        SPG_TRY(v.alloc(n_staged * sizeof(double), s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(r.ptr, rows, n_staged * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(cl.ptr, cols, n_staged * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(v.ptr, vals, n_staged * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    return lock_device_impl(c, A, r.as<uint32_t>(), cl.as<uint32_t>(), v.as<double>(), n_staged, s);
+}
+
+}  // extern "C"

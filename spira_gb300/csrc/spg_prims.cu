@@ -1,0 +1,345 @@
+// spg_prims.cu — device-wide building blocks: exclusive scan (reduce-then-
+// scan, recursive over tile sums) and a stable LSD radix sort of 64-bit keys
+// with a 32-bit payload. The lock, transpose and SpGEMM paths are built on
+// these; the stability of the sort is what carries Spira's "last write wins"
+// and "ascending source row" orders onto the GPU.
+#include "spg_internal.cuh"
+
+namespace spg {
+
+// ---------------------------------------------------------------------------
+// Device buffers
+// ---------------------------------------------------------------------------
+int DevBuf::alloc(size_t n, cudaStream_t s) {
+    release();
+    stream = s;
+    bytes = n;
+    if (n == 0) return SPG_OK;
+    cudaError_t e = cudaMallocAsync(&ptr, n, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ptr = nullptr;
+        bytes = 0;
+        return set_error(e == cudaErrorMemoryAllocation ? SPG_ERR_NO_MEMORY : SPG_ERR_CUDA,
+                         "device allocation of %zu bytes failed: %s", n, cudaGetErrorString(e));
+    }
+    return SPG_OK;
+}
+
+void DevBuf::release() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int SCAN_BLOCK = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;
+
+template <typename T>
+__device__ __forceinline__ T warp_inclusive_scan(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += o;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and the block total.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T &total) {
+    constexpr int NW = SCAN_BLOCK / 32;
+    __shared__ T warp_tot[NW];
+    __shared__ T block_total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T w = (lane < NW) ? warp_tot[lane] : T(0);
+        T wi = warp_inclusive_scan(w);
+        if (lane < NW) warp_tot[lane] = wi - w;
+        if (lane == NW - 1) block_total = wi;
+    }
+    __syncthreads();
+    T res = warp_tot[warp] + inc - v;
+    total = block_total;
+    __syncthreads();
+    return res;
+}
+
+template <typename T>
+__global__ void scan_tile_reduce(const T *__restrict__ d, uint64_t n, T *__restrict__ tile_sums) {
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        uint64_t k = base + (uint64_t)i * SCAN_BLOCK + threadIdx.x;
+        if (k < n) s += d[k];
+    }
+    T total;
+    block_exclusive_scan(s, total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// Scan each tile (blocked arrangement: thread t owns items t*ITEMS..), adding
+// the tile's exclusive prefix. Loads go through shared memory to stay coalesced.
+template <typename T>
+__global__ void scan_tile_apply(T *__restrict__ d, uint64_t n, const T *__restrict__ tile_prefix,
+                                T *__restrict__ d_total) {
+    __shared__ T tile[SCAN_TILE];
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        int j = i * SCAN_BLOCK + threadIdx.x;
+        uint64_t k = base + j;
+        tile[j] = (k < n) ? d[k] : T(0);
+    }
+    __syncthreads();
+    T v[SCAN_ITEMS];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = tile[threadIdx.x * SCAN_ITEMS + i];
+        s += v[i];
+    }
+    T total;
+    T pre = block_exclusive_scan(s, total) + (tile_prefix ? tile_prefix[blockIdx.x] : T(0));
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        tile[threadIdx.x * SCAN_ITEMS + i] = pre;
+        pre += v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        int j = i * SCAN_BLOCK + threadIdx.x;
+        uint64_t k = base + j;
+        if (k < n) d[k] = tile[j];
+    }
+    if (d_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_BLOCK - 1) {
+        // last thread of last tile: its running prefix after all items
+        *d_total = pre;
+    }
+}
+
+template <typename T>
+int exclusive_scan_impl(Ctx *c, T *d, uint64_t n, T *d_total, cudaStream_t s) {
+    if (n == 0) {
+        if (d_total) SPG_CUDA_TRY(cudaMemsetAsync(d_total, 0, sizeof(T), s));
+        return SPG_OK;
+    }
+    const uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles == 1) {
+        scan_tile_apply<T><<<1, SCAN_BLOCK, 0, s>>>(d, n, nullptr, d_total);
+        SPG_LAUNCH_CHECK();
+        return SPG_OK;
+    }
+    DevBuf sums;
+    SPG_TRY(sums.alloc(tiles * sizeof(T), s));
+    scan_tile_reduce<T><<<(unsigned)tiles, SCAN_BLOCK, 0, s>>>(d, n, sums.as<T>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_impl<T>(c, sums.as<T>(), tiles, nullptr, s));
+    scan_tile_apply<T><<<(unsigned)tiles, SCAN_BLOCK, 0, s>>>(d, n, sums.as<T>(), d_total);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+}  // namespace
+
+int exclusive_scan_u64(Ctx *c, uint64_t *d, uint64_t n, uint64_t *d_total, cudaStream_t s) {
+    return exclusive_scan_impl<unsigned long long>(c, reinterpret_cast<unsigned long long *>(d), n,
+                                                   reinterpret_cast<unsigned long long *>(d_total), s);
+}
+
+int exclusive_scan_i64(Ctx *c, int64_t *d, uint64_t n, cudaStream_t s) {
+    return exclusive_scan_impl<long long>(c, reinterpret_cast<long long *>(d), n, nullptr, s);
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort (8-bit digits, reduce-then-scan per pass)
+//
+// Tile of 4096 keys = 8 warps x 16 iterations x 32 lanes. Warp w owns keys
+// [w*512, w*512+512) of the tile and walks them in order (iteration-major,
+// lane-minor), so the within-tile rank of every key is its order among equal
+// digits: stability follows, and with it the insertion-order tie-break.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int RS_WARPS = 8;
+constexpr int RS_BLOCK = RS_WARPS * 32;
+constexpr int RS_ITERS = 16;
+constexpr int RS_TILE = RS_BLOCK * RS_ITERS;  // 4096
+constexpr int RS_RADIX = 256;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__global__ void __launch_bounds__(RS_BLOCK)
+radix_upsweep(const uint64_t *__restrict__ keys, uint64_t n, int shift, unsigned n_tiles,
+              unsigned *__restrict__ hist /* [RADIX][n_tiles] */) {
+    __shared__ unsigned cnt[RS_WARPS][RS_RADIX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&cnt[0][0])[i] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)warp * (RS_ITERS * 32);
+#pragma unroll 4
+    for (int j = 0; j < RS_ITERS; ++j) {
+        uint64_t k = base + j * 32 + lane;
+        unsigned d = (k < n) ? (unsigned)((keys[k] >> shift) & 0xFF) : RS_RADIX;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (d < RS_RADIX && (peers & lanemask_lt()) == 0) cnt[warp][d] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) {
+        unsigned s = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) s += cnt[w][d];
+        hist[(uint64_t)d * n_tiles + blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(RS_BLOCK)
+radix_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+              uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, uint64_t n,
+              int shift, unsigned n_tiles, const unsigned long long *__restrict__ offs /* scanned */) {
+    __shared__ unsigned cnt[RS_WARPS][RS_RADIX];
+    __shared__ unsigned long long gbase[RS_RADIX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&cnt[0][0])[i] = 0;
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK)
+        gbase[d] = offs[(uint64_t)d * n_tiles + blockIdx.x];
+    __syncthreads();
+
+    const uint64_t base = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)warp * (RS_ITERS * 32);
+    uint64_t key[RS_ITERS];
+    uint32_t val[RS_ITERS];
+    unsigned rank[RS_ITERS];
+#pragma unroll
+    for (int j = 0; j < RS_ITERS; ++j) {
+        uint64_t k = base + j * 32 + lane;
+        key[j] = (k < n) ? keys_in[k] : 0;
+        val[j] = (k < n) ? vals_in[k] : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < RS_ITERS; ++j) {
+        uint64_t k = base + j * 32 + lane;
+        unsigned d = (k < n) ? (unsigned)((key[j] >> shift) & 0xFF) : RS_RADIX;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        unsigned before = 0;
+        if (d < RS_RADIX) before = cnt[warp][d];
+        __syncwarp();
+        rank[j] = before + __popc(peers & lanemask_lt());
+        if (d < RS_RADIX && (peers & lanemask_lt()) == 0) cnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // Exclusive prefix over warps for every digit (warp order = key order).
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) {
+        unsigned s = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) {
+            unsigned t = cnt[w][d];
+            cnt[w][d] = s;
+            s += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < RS_ITERS; ++j) {
+        uint64_t k = base + j * 32 + lane;
+        if (k < n) {
+            unsigned d = (unsigned)((key[j] >> shift) & 0xFF);
+            unsigned long long pos = gbase[d] + cnt[warp][d] + rank[j];
+            keys_out[pos] = key[j];
+            vals_out[pos] = val[j];
+        }
+    }
+}
+
+__global__ void scan_u32_to_u64_copy(const unsigned *in, unsigned long long *out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+}  // namespace
+
+int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n, int key_bits,
+                         cudaStream_t s) {
+    if (n <= 1 || key_bits <= 0) return SPG_OK;
+    if (n >= (1ull << 32))
+        return set_error(SPG_ERR_UNSUPPORTED, "radix sort of %llu keys exceeds 2^32-1",
+                         (unsigned long long)n);
+    const unsigned n_tiles = (unsigned)((n + RS_TILE - 1) / RS_TILE);
+    const uint64_t hist_n = (uint64_t)RS_RADIX * n_tiles;
+    DevBuf kalt, valt, hist, offs;
+    SPG_TRY(kalt.alloc(n * sizeof(uint64_t), s));
+    SPG_TRY(valt.alloc(n * sizeof(uint32_t), s));
+    SPG_TRY(hist.alloc(hist_n * sizeof(unsigned), s));
+    SPG_TRY(offs.alloc(hist_n * sizeof(unsigned long long), s));
+    uint64_t *kin = d_keys, *kout = kalt.as<uint64_t>();
+    uint32_t *vin = d_vals, *vout = valt.as<uint32_t>();
+    const int passes = (key_bits + 7) / 8;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = p * 8;
+        radix_upsweep<<<n_tiles, RS_BLOCK, 0, s>>>(kin, n, shift, n_tiles, hist.as<unsigned>());
+        SPG_LAUNCH_CHECK();
+        scan_u32_to_u64_copy<<<grid_for(hist_n, 256, 4096), 256, 0, s>>>(
+            hist.as<unsigned>(), offs.as<unsigned long long>(), hist_n);
+        SPG_LAUNCH_CHECK();
+        SPG_TRY(exclusive_scan_u64(c, offs.as<uint64_t>(), hist_n, nullptr, s));
+        radix_scatter<<<n_tiles, RS_BLOCK, 0, s>>>(kin, vin, kout, vout, n, shift, n_tiles,
+                                                   offs.as<unsigned long long>());
+        SPG_LAUNCH_CHECK();
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    if (kin != d_keys) {
+        SPG_CUDA_TRY(cudaMemcpyAsync(d_keys, kin, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(d_vals, vin, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    }
+    return SPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Max reduction (used for device-side index range checks)
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void max_u32_kernel(const uint32_t *__restrict__ d, uint64_t n, unsigned *out) {
+    unsigned m = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        m = max(m, d[i]);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+}  // namespace
+
+int reduce_max_u32(Ctx *c, const uint32_t *d, uint64_t n, uint32_t *h_max, cudaStream_t s) {
+    DevBuf out;
+    SPG_TRY(out.alloc(sizeof(unsigned), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(out.ptr, 0, sizeof(unsigned), s));
+    if (n) {
+        max_u32_kernel<<<grid_for(n, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(d, n, out.as<unsigned>());
+        SPG_LAUNCH_CHECK();
+    }
+    SPG_CUDA_TRY(cudaMemcpyAsync(h_max, out.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+}  // namespace spg

@@ -1,0 +1,440 @@
+// spg_spmv.cu — FP64 CSR SpMV y = A x on sm_103a.
+//
+// Spira computes each row as a sparse dot product over the row's CSR slice
+// (serial/spmv.hpp:44-55 scalar loop, serial/spmv.hpp:141-186 and
+// parallel/algorithms/spmv.hpp:125-161 through kernel::sparse_dot_double,
+// whose SIMD bodies keep 4 blocked accumulators, dot_avx512.cpp:7-56,
+// dot_neon.cpp:7-56). The kernels below compute the same row sums with GPU
+// reduction trees; the per-row result agrees with Spira's within the FP64
+// reassociation bound, not bit for bit (bit-exact only for SCALAR, which
+// keeps Spira's left-to-right order with fused multiply-adds).
+//
+// Variants (one family each for the row-, warp- and merge-path shapes):
+//   SCALAR     one thread per row (the plain path);
+//   VECTOR<G>  G lanes per row, shuffle reduction; G = 32 uses 16-byte
+//              (double2 / uint2) loads of vals / cols;
+//   STREAM     row blocks of <= 2047 nnz (or one long row) per CTA; the block's
+//              vals/cols/x products are staged in shared memory with coalesced
+//              loads and reduced with an adaptive number of lanes per row;
+//   MERGE      merge-path split of (row ends + nnz) into equal CTA tiles,
+//              carry-out fix-up in tile order (deterministic).
+// All bandwidth-bound; the roofline is HBM (12 B/nnz + 8 B/row offsets +
+// 8 B/col x + 8 B/row y).
+#include "spg_internal.cuh"
+
+namespace spg {
+namespace {
+
+constexpr int BLOCK = 256;
+
+__device__ __forceinline__ double ldx(const double *__restrict__ x, uint32_t c) { return __ldg(x + c); }
+
+// ---------------------------------------------------------------------------
+// SCALAR: thread per row, fma chain in CSR order (Spira's scalar order with
+// contraction: acc = fma(x[c], v, acc)).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BLOCK)
+spmv_scalar(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+            const double *__restrict__ vals, const double *__restrict__ x,
+            double *__restrict__ y, uint64_t n_rows) {
+    const uint64_t r = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+    if (r >= n_rows) return;
+    const uint64_t b = off[r], e = off[r + 1];
+    double acc = 0.0;
+    for (uint64_t k = b; k < e; ++k) acc = fma(ldx(x, cols[k]), vals[k], acc);
+    y[r] = acc;
+}
+
+// Dot over [b, e) by NL cooperating lanes (lane in [0, NL)), lane-strided,
+// 16-byte loads over the even-aligned interior, scalar head/tail.
+template <int NL>
+__device__ __forceinline__ double seg_dot_vec2(const uint32_t *__restrict__ cols,
+                                               const double *__restrict__ vals,
+                                               const double *__restrict__ x, uint64_t b,
+                                               uint64_t e, int lane) {
+    double acc = 0.0;
+    uint64_t a = (b + 1) & ~1ull;
+    if (a > e) a = e;
+    const uint64_t ae = e & ~1ull;
+    if (b < a && lane == 0) acc = fma(ldx(x, cols[b]), vals[b], acc);
+    for (uint64_t i = a + 2ull * lane; i < ae; i += 2ull * NL) {
+        const double2 v = *reinterpret_cast<const double2 *>(vals + i);
+        const uint2 c = *reinterpret_cast<const uint2 *>(cols + i);
+        acc = fma(ldx(x, c.x), v.x, acc);
+        acc = fma(ldx(x, c.y), v.y, acc);
+    }
+    if (ae < e && ae >= a && lane == NL - 1) acc = fma(ldx(x, cols[ae]), vals[ae], acc);
+    return acc;
+}
+
+template <int G>
+__device__ __forceinline__ double group_reduce(double v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// VECTOR<G>: G lanes per row.
+// ---------------------------------------------------------------------------
+template <int G>
+__global__ void __launch_bounds__(BLOCK)
+spmv_vector(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+            const double *__restrict__ vals, const double *__restrict__ x,
+            double *__restrict__ y, uint64_t n_rows) {
+    const uint64_t t = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+    const uint64_t r = t / G;
+    const int lane = (int)(t % G);
+    // Whole groups are inside or outside the range (BLOCK % G == 0), so the
+    // shuffles below never miss a partner.
+    if (r >= n_rows) return;
+    const uint64_t b = off[r], e = off[r + 1];
+    double acc;
+    if (G == 32) {
+        acc = seg_dot_vec2<32>(cols, vals, x, b, e, lane);
+    } else {
+        acc = 0.0;
+        for (uint64_t k = b + lane; k < e; k += G) acc = fma(ldx(x, cols[k]), vals[k], acc);
+    }
+    acc = group_reduce<G>(acc);
+    if (lane == 0) y[r] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// STREAM: plan of row blocks.
+// A row r starts a block iff r == 0, r % ROWCAP == 0, its start offset falls in
+// a different BIN-sized nnz bin than row r-1's, or r or r-1 is a long row
+// (> LONG nnz). Hence a block is either one long row or <= ROWCAP short rows
+// whose starts share a bin: nnz <= (BIN - 1) + LONG.
+// ---------------------------------------------------------------------------
+constexpr int ST_LOG_BIN = 10;
+constexpr uint64_t ST_BIN = 1ull << ST_LOG_BIN;
+constexpr uint64_t ST_LONG = 1024;
+constexpr int ST_ROWCAP = 1024;
+constexpr int ST_MAX_NNZ = (int)(ST_BIN - 1 + ST_LONG);  // 2047
+
+__global__ void stream_plan_flags(const uint64_t *__restrict__ off, uint64_t n_rows,
+                                  uint64_t *__restrict__ flag) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    bool f = (r == 0) || (r % ST_ROWCAP == 0);
+    if (!f) {
+        const uint64_t o0 = off[r - 1], o1 = off[r], o2 = off[r + 1];
+        f = ((o0 >> ST_LOG_BIN) != (o1 >> ST_LOG_BIN)) || (o1 - o0 > ST_LONG) || (o2 - o1 > ST_LONG);
+    }
+    flag[r] = f ? 1 : 0;
+}
+
+__global__ void stream_plan_scatter(const uint64_t *__restrict__ pos, uint64_t n_rows,
+                                    uint64_t *__restrict__ blk) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    const uint64_t p = pos[r];
+    const uint64_t q = pos[r + 1];  // pos has n_rows + 1 entries (total at the end)
+    if (q != p) blk[p] = r;
+    if (r == n_rows - 1) blk[q] = n_rows;
+}
+
+__device__ __forceinline__ double block_reduce_sum(double v, double *red) {
+    v = group_reduce<32>(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (warp == 0) {
+        s = (lane < BLOCK / 32) ? red[lane] : 0.0;
+        s = group_reduce<32>(s);
+    }
+    return s;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(BLOCK)
+spmv_stream(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+            const double *__restrict__ vals, const double *__restrict__ x,
+            double *__restrict__ y, const uint64_t *__restrict__ blk) {
+    __shared__ double prod[ST_MAX_NNZ + 1];
+    __shared__ uint32_t soff[ST_ROWCAP + 1];
+    __shared__ double red[BLOCK / 32];
+    const uint64_t r0 = blk[blockIdx.x], r1 = blk[blockIdx.x + 1];
+    const uint64_t k0 = off[r0], k1 = off[r1];
+    const uint32_t nrows = (uint32_t)(r1 - r0);
+    const uint64_t nz = k1 - k0;
+    if (nz > (uint64_t)ST_MAX_NNZ) {  // a single long row
+        double acc = seg_dot_vec2<BLOCK>(cols, vals, x, k0, k1, threadIdx.x);
+        acc = block_reduce_sum(acc, red);
+        if (threadIdx.x == 0) y[r0] = acc;
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i <= nrows; i += BLOCK) soff[i] = (uint32_t)(off[r0 + i] - k0);
+    for (uint32_t i = threadIdx.x; i < nz; i += BLOCK) prod[i] = vals[k0 + i] * ldx(x, cols[k0 + i]);
+    __syncthreads();
+    // lanes per row: as many as fit, power of two, <= 32
+    int L = 1;
+    while (L < 32 && (uint32_t)(L * 2) * nrows <= BLOCK) L *= 2;
+    const int lane = threadIdx.x % L;
+    const uint32_t grp = threadIdx.x / L, ngrp = BLOCK / L;
+    for (uint32_t base = 0; base < nrows; base += ngrp) {
+        const uint32_t rr = base + grp;  // all lanes of a group share rr
+        double acc = 0.0;
+        if (rr < nrows) {
+            const uint32_t b = soff[rr], e = soff[rr + 1];
+            for (uint32_t k = b + lane; k < e; k += L) acc += prod[k];
+        }
+        // reduce within the group of L lanes (L is block-uniform)
+        for (int o = L / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, L);
+        if (rr < nrows && lane == 0) y[r0 + rr] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MERGE: merge-path over the two sorted lists A = row end offsets
+// (off[1..n]) and B = nnz indices (0..nnz-1). Diagonal d splits at (i, j) with
+// i + j = d; tile t covers diagonals [t*TILE, (t+1)*TILE). Each thread walks
+// ITEMS consecutive path steps sequentially (rows it finishes are written
+// directly), its trailing partial row is combined across threads with a
+// segmented block scan, and the tile's last partial row goes to a carry-out
+// fixed up in tile order by a second kernel.
+// ---------------------------------------------------------------------------
+constexpr int MG_ITEMS = 7;
+constexpr int MG_TILE = BLOCK * MG_ITEMS;
+
+__device__ __forceinline__ void merge_path_search(uint64_t diag, const uint64_t *__restrict__ row_end,
+                                                  uint64_t n_rows, uint64_t nnz, uint64_t &ri,
+                                                  uint64_t &ki) {
+    // Find the first i such that row_end[i] > diag - i - 1 ... standard form:
+    // largest i in [lo, hi] with row_end[i-1] <= diag - i  (A items consumed first on ties)
+    uint64_t lo = diag > nnz ? diag - nnz : 0;
+    uint64_t hi = diag < n_rows ? diag : n_rows;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        // A[mid] = row_end[mid] (end offset of row mid); B[diag - mid - 1] = diag - mid - 1
+        if (row_end[mid] <= diag - mid - 1) lo = mid + 1;
+        else hi = mid;
+    }
+    ri = lo;
+    ki = diag - lo;
+}
+
+__global__ void merge_tile_starts(const uint64_t *__restrict__ off, uint64_t n_rows, uint64_t nnz,
+                                  uint64_t n_tiles, uint64_t *__restrict__ starts /* 2*(n_tiles+1) */) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > n_tiles) return;
+    uint64_t diag = t * MG_TILE;
+    const uint64_t total = n_rows + nnz;
+    if (diag > total) diag = total;
+    uint64_t ri, ki;
+    merge_path_search(diag, off + 1, n_rows, nnz, ri, ki);
+    starts[2 * t] = ri;
+    starts[2 * t + 1] = ki;
+}
+
+struct Carry {
+    uint64_t row;
+    double val;
+};
+
+// Block-wide exclusive segmented scan of (head, value) pairs in thread
+// order: a head starts a new segment at that thread's value. Returns the
+// exclusive result; *incl_last receives the inclusive result of the last
+// thread (the tile's carry-out value). Fixed tree: deterministic.
+__device__ __forceinline__ double block_seg_excl_scan(bool head, double v, double *incl_last) {
+    __shared__ double w_val[BLOCK / 32];
+    __shared__ int w_head[BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int h = head;
+    double p = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int hh = __shfl_up_sync(0xffffffffu, h, o);
+        const double pp = __shfl_up_sync(0xffffffffu, p, o);
+        if (lane >= o) {
+            if (!h) p = pp + p;
+            h |= hh;
+        }
+    }
+    if (lane == 31) {
+        w_val[warp] = p;
+        w_head[warp] = h;
+    }
+    __syncthreads();
+    // carry into this warp from the warps before it, in order
+    double wc = 0.0;
+    for (int w = 0; w < warp; ++w) wc = w_head[w] ? w_val[w] : wc + w_val[w];
+    double incl = h ? p : wc + p;
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = wc;
+    if (threadIdx.x == BLOCK - 1) *incl_last = incl;
+    return excl;
+}
+
+__global__ void __launch_bounds__(BLOCK)
+spmv_merge(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+           const double *__restrict__ vals, const double *__restrict__ x, double *__restrict__ y,
+           uint64_t n_rows, const uint64_t *__restrict__ starts, Carry *__restrict__ carry) {
+    __shared__ uint64_t s_rowend[MG_TILE];
+    __shared__ double s_prod[MG_TILE];
+    __shared__ double s_carry_val;
+    const uint64_t t = blockIdx.x;
+    const uint64_t r_begin = starts[2 * t], k_begin = starts[2 * t + 1];
+    const uint64_t r_end = starts[2 * t + 2], k_end = starts[2 * t + 3];
+    const uint32_t nr = (uint32_t)(r_end - r_begin), nk = (uint32_t)(k_end - k_begin);
+    for (uint32_t i = threadIdx.x; i < nr; i += BLOCK) s_rowend[i] = off[r_begin + i + 1];
+    for (uint32_t i = threadIdx.x; i < nk; i += BLOCK)
+        s_prod[i] = vals[k_begin + i] * ldx(x, cols[k_begin + i]);
+    __syncthreads();
+    // This thread's start on the tile's merge path (diagonal d).
+    const uint32_t tile_len = nr + nk;
+    const uint32_t d = min((uint32_t)threadIdx.x * MG_ITEMS, tile_len);
+    uint32_t lo = d > nk ? d - nk : 0, hi = min(d, nr);
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_rowend[mid] <= k_begin + (d - mid - 1)) lo = mid + 1;
+        else hi = mid;
+    }
+    const uint32_t ri0 = lo;
+    uint32_t ri = lo, ki = d - lo;
+    const uint32_t dend = min(d + (uint32_t)MG_ITEMS, tile_len);
+    double acc = 0.0, first = 0.0;
+    for (uint32_t step = d; step < dend; ++step) {
+        if (ri < nr && s_rowend[ri] <= k_begin + ki) {  // row ri ends here
+            if (ri == ri0) first = acc;
+            else y[r_begin + ri] = acc;
+            acc = 0.0;
+            ++ri;
+        } else {
+            acc += s_prod[ki];
+            ++ki;
+        }
+    }
+    const bool head = (ri != ri0);
+    // the value this thread contributes to the segment it ends in
+    const double carry_in = block_seg_excl_scan(head, acc, &s_carry_val);
+    if (head) y[r_begin + ri0] = carry_in + first;
+    __syncthreads();
+    if (threadIdx.x == BLOCK - 1) {
+        carry[t].row = r_begin + ri;
+        carry[t].val = s_carry_val;
+    }
+}
+
+// Adds each tile's carry-out to its row. A run of consecutive tiles carrying
+// into the same row (a row spanning tiles) is summed by the run's first tile
+// in tile order, so the result is deterministic.
+__global__ void merge_fixup(const Carry *__restrict__ carry, uint64_t n_tiles, uint64_t n_rows,
+                            double *__restrict__ y) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const uint64_t r = carry[t].row;
+    if (r >= n_rows) return;
+    if (t > 0 && carry[t - 1].row == r) return;
+    double s = carry[t].val;
+    for (uint64_t u = t + 1; u < n_tiles && carry[u].row == r; ++u) s += carry[u].val;
+    y[r] += s;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Plans
+// ---------------------------------------------------------------------------
+static int build_stream_plan(Ctx *c, Csr *A, cudaStream_t s) {
+    if (A->plan_stream.kind == SPG_SPMV_STREAM) return SPG_OK;
+    const uint64_t n = A->n_rows;
+    DevBuf flag;
+    SPG_TRY(flag.alloc((n + 1) * sizeof(uint64_t), s));
+    stream_plan_flags<<<grid_for(n, 256), 256, 0, s>>>(A->d_off(), n, flag.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    DevBuf total;
+    SPG_TRY(total.alloc(sizeof(uint64_t), s));
+    SPG_TRY(exclusive_scan_u64(c, flag.as<uint64_t>(), n, flag.as<uint64_t>() + n, s));
+    uint64_t nb = 0;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&nb, flag.as<uint64_t>() + n, sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SpmvPlan p;
+    SPG_TRY(p.items.alloc((nb + 1) * sizeof(uint64_t), s));
+    stream_plan_scatter<<<grid_for(n, 256), 256, 0, s>>>(flag.as<uint64_t>(), n, p.items.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    p.kind = SPG_SPMV_STREAM;
+    p.n_items = nb;
+    A->plan_stream = std::move(p);
+    return SPG_OK;
+}
+
+static int build_merge_plan(Ctx *c, Csr *A, cudaStream_t s) {
+    if (A->plan_merge.kind == SPG_SPMV_MERGE) return SPG_OK;
+    const uint64_t total = A->n_rows + A->nnz;
+    const uint64_t n_tiles = (total + MG_TILE - 1) / MG_TILE;
+    SpmvPlan p;
+    SPG_TRY(p.items.alloc(2 * (n_tiles + 1) * sizeof(uint64_t), s));
+    SPG_TRY(p.aux.alloc((n_tiles ? n_tiles : 1) * sizeof(Carry), s));
+    merge_tile_starts<<<grid_for(n_tiles + 1, 256), 256, 0, s>>>(A->d_off(), A->n_rows, A->nnz, n_tiles,
+                                                                 p.items.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    p.kind = SPG_SPMV_MERGE;
+    p.n_items = n_tiles;
+    A->plan_merge = std::move(p);
+    (void)c;
+    return SPG_OK;
+}
+
+int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s) {
+    const uint64_t n = A->n_rows;
+    if (n == 0) return SPG_OK;
+    const uint64_t *off = A->d_off();
+    const uint32_t *cols = A->d_cols();
+    const double *vals = A->d_vals();
+    switch (variant) {
+        case SPG_SPMV_SCALAR:
+            spmv_scalar<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(off, cols, vals, x, y, n);
+            break;
+#define SPG_VEC_CASE(ID, G)                                                                   \
+    case ID:                                                                                  \
+        spmv_vector<G><<<grid_for(n * G, BLOCK), BLOCK, 0, s>>>(off, cols, vals, x, y, n);    \
+        break;
+        SPG_VEC_CASE(SPG_SPMV_VECTOR2, 2)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR4, 4)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR8, 8)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR16, 16)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR32, 32)
+#undef SPG_VEC_CASE
+        case SPG_SPMV_STREAM: {
+            SPG_TRY(build_stream_plan(c, A, s));
+            const uint64_t nb = A->plan_stream.n_items;
+            if (nb == 0) break;
+            spmv_stream<<<(unsigned)nb, BLOCK, 0, s>>>(off, cols, vals, x, y,
+                                                       A->plan_stream.items.as<uint64_t>());
+            break;
+        }
+        case SPG_SPMV_MERGE: {
+            SPG_TRY(build_merge_plan(c, A, s));
+            const uint64_t nt = A->plan_merge.n_items;
+            if (nt == 0) break;
+            spmv_merge<<<(unsigned)nt, BLOCK, 0, s>>>(off, cols, vals, x, y, n,
+                                                      A->plan_merge.items.as<uint64_t>(),
+                                                      A->plan_merge.aux.as<Carry>());
+            SPG_LAUNCH_CHECK();
+            merge_fixup<<<grid_for(nt, 256), 256, 0, s>>>(A->plan_merge.aux.as<Carry>(), nt, n, y);
+            break;
+        }
+        default:
+            return set_error(SPG_ERR_INVALID_ARGUMENT, "spmv: unknown variant %d", variant);
+    }
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int spmv_resolve_auto(Ctx *c, Csr *A, int *variant) {
+    // Placeholder policy until the selector lands: long-row-heavy matrices go
+    // to STREAM, short regular rows to VECTOR4.
+    (void)c;
+    if (A->selected_spmv >= 0) {
+        *variant = A->selected_spmv;
+        return SPG_OK;
+    }
+    *variant = SPG_SPMV_STREAM;
+    A->selected_spmv = *variant;
+    return SPG_OK;
+}
+
+}  // namespace spg

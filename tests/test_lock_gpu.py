@@ -1,0 +1,149 @@
+"""lock() on the GPU: bit-exact against the oracle (structure, value bits and
+Spira's capacity) and Spira's golden fixtures; error behaviour."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+import spira_gb300 as sg
+from spira_gb300 import gen
+from conftest import assert_csr_equal
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.loads((Path(__file__).parent / "golden" / "golden.json").read_text())
+
+
+def _epochs(ep):
+    out = []
+    for e in ep:
+        out.append((np.array([t[0] for t in e], np.uint32), np.array([t[1] for t in e], np.uint32),
+                    np.array([float.fromhex(t[2]) for t in e], np.float64)))
+    return out
+
+
+def _gold_csr(d):
+    return oracle.Csr(d["n_rows"], d["n_cols"], np.array(d["off"], np.uint64), np.array(d["cols"], np.uint32),
+                      np.array([float.fromhex(v) for v in d["vals"]], np.float64), d["capacity"])
+
+
+def gpu_lock(ctx, n_rows, n_cols, epochs):
+    A = sg.Csr(ctx, n_rows, n_cols)
+    for r, c, v in epochs:
+        A.lock(r, c, v)
+    return A
+
+
+@pytest.mark.parametrize("kat", GOLD["kats"], ids=[k["name"] for k in GOLD["kats"]])
+def test_lock_kats_match_spira(ctx, kat):
+    A = gpu_lock(ctx, kat["n_rows"], kat["n_cols"], _epochs(kat["epochs"]))
+    assert_csr_equal(A.download(), _gold_csr(kat["csr"]))
+
+
+def _random_epochs(n_rows, n_cols, sizes, seed, zero_every=11, nan_every=0):
+    eps = []
+    for e, m in enumerate(sizes):
+        ctr = np.arange(m, dtype=np.uint64)
+        r = gen.below(gen.hash3(seed + e, 1, ctr), n_rows)
+        c = gen.below(gen.hash3(seed + e, 2, ctr), n_cols)
+        v = gen.sym_unit(gen.hash3(seed + e, 3, ctr))
+        if zero_every:
+            v[::zero_every] = 0.0
+            v[5::zero_every * 3] = -0.0
+        if nan_every:
+            v[::nan_every] = np.nan
+        eps.append((r, c, v))
+    return eps
+
+
+@pytest.mark.parametrize("n_rows,n_cols,sizes", [
+    (1, 1, [5, 5]),
+    (7, 3, [40, 0, 40]),
+    (1000, 1000, [20_000, 3_000, 3_000, 500]),
+    (3000, 50, [100_000, 10_000]),          # heavy duplicates (last write wins)
+    (50, 100_000, [30_000, 30_000]),         # wide rows
+    (200_000, 200_000, [300_000, 30_000]),   # many empty rows
+])
+def test_lock_random_epochs_bit_exact(ctx, n_rows, n_cols, sizes):
+    eps = _random_epochs(n_rows, n_cols, sizes, seed=n_rows + 7, nan_every=997)
+    A = gpu_lock(ctx, n_rows, n_cols, eps)
+    assert_csr_equal(A.download(), oracle.lock_epochs(n_rows, n_cols, eps))
+
+
+def test_lock_config1_full(ctx):
+    r, c, v = gen.random_rows(10_000, 10_000, 10, seed=42)
+    A = gpu_lock(ctx, 10_000, 10_000, [(r, c, v)])
+    rec = {w["name"]: w for w in GOLD["workloads"]}["random_10k_10_per_row"]
+    assert oracle.csr_digest(A.download()) == rec["csr_sha256"]
+
+
+def test_lock_laplacian_relock_matches_oracle(ctx):
+    r, c, v = gen.laplacian_2d(400)
+    n = 400 * 400
+    b = gen.relock_batch(n, n, len(r), seed=3, zero_frac=0.2)
+    A = gpu_lock(ctx, n, n, [(r, c, v), b])
+    assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(r, c, v), b]))
+
+
+def test_lock_zipf_long_rows(ctx):
+    r, c, v = gen.zipf_rows(100_000, seed=9)
+    b = gen.relock_batch(100_000, 100_000, len(r), seed=10, zero_frac=0.05)
+    A = gpu_lock(ctx, 100_000, 100_000, [(r, c, v), b])
+    assert_csr_equal(A.download(), oracle.lock_epochs(100_000, 100_000, [(r, c, v), b]))
+
+
+def test_out_of_range_leaves_matrix_unchanged(ctx):
+    A = gpu_lock(ctx, 4, 4, [(np.array([0, 1], np.uint32), np.array([1, 2], np.uint32), np.array([1.0, 2.0]))])
+    before = A.download()
+    with pytest.raises(sg.OutOfRange):
+        A.lock(np.array([4], np.uint32), np.array([0], np.uint32), np.array([1.0]))
+    with pytest.raises(sg.OutOfRange):
+        A.lock(np.array([0], np.uint32), np.array([4], np.uint32), np.array([1.0]))
+    assert_csr_equal(A.download(), before)
+
+
+def test_load_csr_validation(ctx):
+    A = sg.Csr(ctx, 2, 3)
+    with pytest.raises(sg.InvalidArgument, match="offsets\\[0\\]"):
+        A.load([1, 1, 1], [0], [1.0])
+    with pytest.raises(sg.InvalidArgument, match="does not equal nnz"):
+        A.load([0, 1, 1], [0, 1], [1.0, 2.0])
+    with pytest.raises(sg.InvalidArgument, match="non-decreasing"):
+        A.load([0, 2, 1], [0], [1.0])
+    with pytest.raises(sg.InvalidArgument, match="out of bounds"):
+        A.load([0, 1, 1], [3], [1.0])
+    with pytest.raises(sg.InvalidArgument, match="strictly sorted"):
+        A.load([0, 2, 2], [1, 1], [1.0, 2.0])
+    A.load([0, 2, 3], [0, 2, 1], [1.0, 2.0, 3.0])
+    assert A.info()["built"] and A.nnz == 3 and A.get(1, 1) == 3.0 and A.get(1, 0) is None
+
+
+def test_relock_after_load_with_explicit_zeros(ctx):
+    """A loaded CSR may hold explicit zeros; Spira's merge drops them from the
+    rows it touches (csr_build.hpp:274-276) and keeps them elsewhere."""
+    off = np.array([0, 3, 5], np.uint64)
+    cols = np.array([0, 1, 2, 0, 2], np.uint32)
+    vals = np.array([0.0, 2.0, -0.0, 0.0, 5.0])
+    A = sg.Csr(ctx, 2, 3)
+    A.load(off, cols, vals)
+    A.lock(np.array([0, 0], np.uint32), np.array([1, 2], np.uint32), np.array([7.0, 8.0]))
+    got = A.download()
+    # row 0 touched: its zero at col 0 is dropped, col 2 (-0.0) replaced by 8.0;
+    # row 1 untouched: keeps its explicit zero
+    np.testing.assert_array_equal(got.off, [0, 2, 4])
+    np.testing.assert_array_equal(got.cols, [1, 2, 0, 2])
+    np.testing.assert_array_equal(got.vals, [7.0, 8.0, 0.0, 5.0])
+
+
+def test_spmv_before_lock_is_logic_error(ctx):
+    A = sg.Csr(ctx, 3, 3)
+    with pytest.raises(sg.LogicError):
+        A.spmv_host(np.zeros(3))
+    A.lock(np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0))
+    np.testing.assert_array_equal(A.spmv_host(np.ones(3)), np.zeros(3))
+    with pytest.raises(sg.InvalidArgument):
+        A.spmv_host(np.zeros(2))

@@ -1,0 +1,138 @@
+"""SpMV on the GPU, every variant, against the oracle and Spira's golden
+outputs. FP64 tolerance (written here, from the benchmark spec's bound): per row
+|y - y_ref| <= 1e-12 * sum_k |a_rk x_k|; the compensated oracle gives y_ref
+to ~2 ulp, and Spira's own SIMD path is held to the same bound."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+import spira_gb300 as sg
+from spira_gb300 import gen
+from conftest import SPMV_TOL, spmv_rel_err
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.loads((Path(__file__).parent / "golden" / "golden.json").read_text())
+GOLD_Y = np.load(Path(__file__).parent / "golden" / "golden_y.npz")
+VARIANTS = list(sg.SPMV_VARIANTS.items()) + [("auto", sg.SPMV_AUTO)]
+
+
+def build(ctx, n_rows, n_cols, epochs):
+    A = sg.Csr(ctx, n_rows, n_cols)
+    for r, c, v in epochs:
+        A.lock(r, c, v)
+    return A
+
+
+def check_all_variants(A, x, host=None):
+    host = host or A.download()
+    y_ref, scale = oracle.spmv_compensated(host, x)
+    errs = {}
+    for name, v in VARIANTS:
+        y = A.spmv_host(x, variant=v)
+        errs[name] = spmv_rel_err(y, y_ref, scale)
+        assert errs[name] <= SPMV_TOL, (name, errs[name])
+    return errs
+
+
+def _csr_from_rows(lengths, n_cols, seed):
+    lengths = np.asarray(lengths, np.int64)
+    rows = np.repeat(np.arange(len(lengths), dtype=np.uint32), lengths)
+    ctr = np.arange(len(rows), dtype=np.uint64)
+    cols = gen.below(gen.hash3(seed, 1, ctr), n_cols)
+    vals = gen.sym_unit(gen.hash3(seed, 2, ctr))
+    return rows, cols, vals
+
+
+@pytest.mark.parametrize("lengths", [
+    [0],
+    [1],
+    [0, 0, 0, 5, 0],
+    [3] * 1000,
+    [5000],                                  # one long row
+    [1023, 1024, 1025, 2046, 2047, 2048, 2049, 1, 0, 7],  # around the STREAM thresholds
+    [0] * 5000 + [40_000] + [0] * 5000,      # a long row between empty stretches
+    list(range(0, 3000, 7)),                 # ramp
+    [1] * 3000 + [10_000] * 3 + [2] * 3000,
+])
+def test_spmv_edge_shapes(ctx, lengths):
+    n_cols = 70_000
+    r, c, v = _csr_from_rows(lengths, n_cols, seed=len(lengths))
+    A = build(ctx, len(lengths), n_cols, [(r, c, v)])
+    x = gen.dense_x(n_cols, 1)
+    check_all_variants(A, x)
+
+
+def test_spmv_empty_rows_give_exact_zero(ctx):
+    r, c, v = _csr_from_rows([0, 3, 0, 0, 2, 0], 10, seed=3)
+    A = build(ctx, 6, 10, [(r, c, v)])
+    for name, var in VARIANTS:
+        y = A.spmv_host(np.full(10, 2.5), variant=var)
+        assert y[0] == 0.0 and y[2] == 0.0 and y[3] == 0.0 and y[5] == 0.0, name
+
+
+@pytest.mark.parametrize("rec", GOLD["workloads"], ids=[w["name"] for w in GOLD["workloads"]])
+def test_spmv_matches_spira_golden(ctx, rec):
+    """Against y produced by Spira's own sparse_dot_double path."""
+    from test_oracle_pin import _workloads
+    name, nr, nc, ep, x = _workloads()[rec["name"]]
+    A = build(ctx, nr, nc, ep)
+    host = A.download()
+    assert oracle.csr_digest(host) == rec["csr_sha256"]
+    y_spira = GOLD_Y[rec["name"] + "__y"]
+    _, scale = oracle.spmv_compensated(host, x)
+    for vname, v in VARIANTS:
+        y = A.spmv_host(x, variant=v)
+        assert spmv_rel_err(y, y_spira, scale) <= 2 * SPMV_TOL, vname
+
+
+def test_spmv_scalar_is_bit_exact_with_fused_scalar_order(ctx):
+    r, c, v = gen.zipf_rows(20_000, seed=4)
+    A = build(ctx, 20_000, 20_000, [(r, c, v)])
+    x = gen.dense_x(20_000, 5)
+    y = A.spmv_host(x, variant=sg.SPMV_SCALAR)
+    np.testing.assert_array_equal(y, oracle.spmv_scalar(A.download(), x, fused=True))
+
+
+def test_spmv_laplacian_2a_full(ctx):
+    """Config 2a at full size: 5-point Laplacian on 1414^2, re-lock, SpMV."""
+    r, c, v = gen.laplacian_2d(1414)
+    n = 1414 * 1414
+    assert n == 1_999_396 and len(r) == 9_991_324
+    b = gen.relock_batch(n, n, len(r), seed=21)
+    A = build(ctx, n, n, [(r, c, v), b])
+    x = gen.dense_x(n, 22)
+    errs = check_all_variants(A, x)
+    assert max(errs.values()) <= SPMV_TOL
+
+
+def test_spmv_zipf_2b_full(ctx):
+    """Config 2b at full size: 4M x 4M, Zipf(1.8) rows capped at 10 000."""
+    from spira_gb300 import gen_device
+    n = 4_000_000
+    r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
+    A = sg.Csr(ctx, n, n)
+    A.lock_device(r, c, v, m)
+    A.lock(*gen.relock_batch(n, n, m, seed=32))
+    x = gen.dense_x(n, 33)
+    check_all_variants(A, x)
+
+
+def test_spmv_device_pointers_and_stream(ctx):
+    import torch
+    r, c, v = gen.random_rows(5000, 4000, 10, seed=8)
+    A = build(ctx, 5000, 4000, [(r, c, v)])
+    x = gen.dense_x(4000, 9)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty(5000, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        A.spmv(xd, yd, sg.SPMV_MERGE, stream=s.cuda_stream)
+    s.synchronize()
+    y_ref, scale = oracle.spmv_compensated(A.download(), x)
+    assert spmv_rel_err(yd.cpu().numpy(), y_ref, scale) <= SPMV_TOL
