@@ -136,6 +136,19 @@ int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
 /* The variant SPG_SPMV_AUTO resolves to for A. */
 int spg_spmv_selected(spg_ctx *ctx, const spg_csr *A, int *variant);
 
+/* ---- transpose / SpGEMM ----------------------------------------------------
+ * spg_transpose: AT <- A^T (AT is reshaped to n_cols x n_rows, capacity ==
+ * nnz); each output row lists its source rows in ascending order
+ * (serial/transpose.hpp:35-156, parallel/algorithms/transpose.hpp:36-70).
+ * SPG_ERR_LOGIC before A's first lock. */
+int spg_transpose(spg_ctx *ctx, const spg_csr *A, spg_csr *AT);
+/* spg_spgemm: C <- A * B (C reshaped to A.n_rows x B.n_cols). Each C(i, j)
+ * is the left-to-right sum over ascending k of the rounded products
+ * a_ik * b_kj from 0.0; exact-zero sums are dropped (serial/spgemm.hpp:12-53,
+ * parallel/algorithms/spgemm.hpp:27-69). A.n_cols != B.n_rows gives
+ * SPG_ERR_INVALID_ARGUMENT, an unlocked A or B SPG_ERR_LOGIC. */
+int spg_spgemm(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, spg_csr *C);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,8 @@ _SIGS = [
     ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
     ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
     ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
+    ("spg_transpose", _I, [_P, _P, _P]),
+    ("spg_spgemm", _I, [_P, _P, _P, _P]),
     # spg_gen.h
     ("spg_gen_draw", _I, [_P, _U64, _U64, _U64, _U64, _I, _U64, _P]),
     ("spg_gen_expand_rows", _I, [_P, _P, _U64, _P, C.POINTER(_U64)]),
@@ -269,6 +271,18 @@ class Csr:
         v = C.c_int()
         _check(lib().spg_spmv_selected(self.ctx.h, self.h, C.byref(v)))
         return v.value
+
+    def transpose(self) -> "Csr":
+        """A new device matrix holding A^T."""
+        T = Csr(self.ctx, 0, 0)
+        _check(lib().spg_transpose(self.ctx.h, self.h, T.h))
+        return T
+
+    def spgemm(self, B: "Csr") -> "Csr":
+        """A new device matrix holding self * B."""
+        Cm = Csr(self.ctx, 0, 0)
+        _check(lib().spg_spgemm(self.ctx.h, self.h, B.h, Cm.h))
+        return Cm
 
 
 # ---------------------------------------------------------------- device draws

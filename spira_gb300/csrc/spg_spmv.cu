@@ -52,19 +52,41 @@ __device__ __forceinline__ double seg_dot_vec2(const uint32_t *__restrict__ cols
                                                const double *__restrict__ vals,
                                                const double *__restrict__ x, uint64_t b,
                                                uint64_t e, int lane) {
-    double acc = 0.0;
+    double acc = 0.0, acc1 = 0.0;
     uint64_t a = (b + 1) & ~1ull;
     if (a > e) a = e;
     const uint64_t ae = e & ~1ull;
     if (b < a && lane == 0) acc = fma(ldx(x, cols[b]), vals[b], acc);
-    for (uint64_t i = a + 2ull * lane; i < ae; i += 2ull * NL) {
+    uint64_t i = a + 2ull * lane;
+    // 4 pairs in flight per lane: all loads issue before the gathers.
+    for (; i + 6ull * NL < ae; i += 8ull * NL) {
+        double2 v[4];
+        uint2 c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = *reinterpret_cast<const double2 *>(vals + i + 2ull * NL * u);
+            c[u] = *reinterpret_cast<const uint2 *>(cols + i + 2ull * NL * u);
+        }
+        double g[8];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            g[2 * u] = ldx(x, c[u].x);
+            g[2 * u + 1] = ldx(x, c[u].y);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            acc = fma(g[2 * u], v[u].x, acc);
+            acc1 = fma(g[2 * u + 1], v[u].y, acc1);
+        }
+    }
+    for (; i < ae; i += 2ull * NL) {
         const double2 v = *reinterpret_cast<const double2 *>(vals + i);
         const uint2 c = *reinterpret_cast<const uint2 *>(cols + i);
         acc = fma(ldx(x, c.x), v.x, acc);
-        acc = fma(ldx(x, c.y), v.y, acc);
+        acc1 = fma(ldx(x, c.y), v.y, acc1);
     }
     if (ae < e && ae >= a && lane == NL - 1) acc = fma(ldx(x, cols[ae]), vals[ae], acc);
-    return acc;
+    return acc + acc1;
 }
 
 template <int G>
@@ -94,7 +116,16 @@ spmv_vector(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
         acc = seg_dot_vec2<32>(cols, vals, x, b, e, lane);
     } else {
         acc = 0.0;
-        for (uint64_t k = b + lane; k < e; k += G) acc = fma(ldx(x, cols[k]), vals[k], acc);
+        double acc1 = 0.0;
+        uint64_t k = b + lane;
+        for (; k + G < e; k += 2 * G) {
+            const uint32_t c0 = cols[k], c1 = cols[k + G];
+            const double v0 = vals[k], v1 = vals[k + G];
+            acc = fma(ldx(x, c0), v0, acc);
+            acc1 = fma(ldx(x, c1), v1, acc1);
+        }
+        if (k < e) acc = fma(ldx(x, cols[k]), vals[k], acc);
+        acc += acc1;
     }
     acc = group_reduce<G>(acc);
     if (lane == 0) y[r] = acc;
@@ -166,7 +197,25 @@ spmv_stream(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
         return;
     }
     for (uint32_t i = threadIdx.x; i <= nrows; i += BLOCK) soff[i] = (uint32_t)(off[r0 + i] - k0);
-    for (uint32_t i = threadIdx.x; i < nz; i += BLOCK) prod[i] = vals[k0 + i] * ldx(x, cols[k0 + i]);
+    {
+        // ST_ITEMS loads per thread issued before any gather (coalesced).
+        constexpr int ST_ITEMS = (ST_MAX_NNZ + BLOCK) / BLOCK;
+        double v[ST_ITEMS];
+        uint32_t c[ST_ITEMS];
+#pragma unroll
+        for (int u = 0; u < ST_ITEMS; ++u) {
+            const uint32_t i = u * BLOCK + threadIdx.x;
+            if (i < nz) {
+                v[u] = vals[k0 + i];
+                c[u] = cols[k0 + i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < ST_ITEMS; ++u) {
+            const uint32_t i = u * BLOCK + threadIdx.x;
+            if (i < nz) prod[i] = v[u] * ldx(x, c[u]);
+        }
+    }
     __syncthreads();
     // lanes per row: as many as fit, power of two, <= 32
     int L = 1;
@@ -278,9 +327,26 @@ spmv_merge(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
     const uint64_t r_begin = starts[2 * t], k_begin = starts[2 * t + 1];
     const uint64_t r_end = starts[2 * t + 2], k_end = starts[2 * t + 3];
     const uint32_t nr = (uint32_t)(r_end - r_begin), nk = (uint32_t)(k_end - k_begin);
-    for (uint32_t i = threadIdx.x; i < nr; i += BLOCK) s_rowend[i] = off[r_begin + i + 1];
-    for (uint32_t i = threadIdx.x; i < nk; i += BLOCK)
-        s_prod[i] = vals[k_begin + i] * ldx(x, cols[k_begin + i]);
+    {
+        double v[MG_ITEMS];
+        uint32_t c[MG_ITEMS];
+        uint64_t re[MG_ITEMS];
+#pragma unroll
+        for (int u = 0; u < MG_ITEMS; ++u) {
+            const uint32_t i = u * BLOCK + threadIdx.x;
+            if (i < nk) {
+                v[u] = vals[k_begin + i];
+                c[u] = cols[k_begin + i];
+            }
+            if (i < nr) re[u] = off[r_begin + i + 1];
+        }
+#pragma unroll
+        for (int u = 0; u < MG_ITEMS; ++u) {
+            const uint32_t i = u * BLOCK + threadIdx.x;
+            if (i < nk) s_prod[i] = v[u] * ldx(x, c[u]);
+            if (i < nr) s_rowend[i] = re[u];
+        }
+    }
     __syncthreads();
     // This thread's start on the tile's merge path (diagonal d).
     const uint32_t tile_len = nr + nk;
