@@ -34,8 +34,8 @@ int Ctx::ensure_pinned(size_t bytes) {
 }
 
 int csr_alloc(Csr *A, uint64_t capacity, cudaStream_t s) {
-    SPG_TRY(A->cols.alloc(capacity * sizeof(uint32_t), s));
-    SPG_TRY(A->vals.alloc(capacity * sizeof(double), s));
+    SPG_TRY(A->cols.alloc(csr_alloc_elems(capacity) * sizeof(uint32_t), s));
+    SPG_TRY(A->vals.alloc(csr_alloc_elems(capacity) * sizeof(double), s));
     A->capacity = capacity;
     return SPG_OK;
 }
@@ -237,8 +237,8 @@ int spg_csr_load(spg_ctx *c, spg_csr *A, const uint64_t *offsets, const uint32_t
     cudaStream_t s = c->stream;
     DevBuf off, cb, vb;
     SPG_TRY(off.alloc((A->n_rows + 1) * sizeof(uint64_t), s));
-    SPG_TRY(cb.alloc(nnz * sizeof(uint32_t), s));
-    SPG_TRY(vb.alloc(nnz * sizeof(double), s));
+    SPG_TRY(cb.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
+    SPG_TRY(vb.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, offsets, (A->n_rows + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     if (nnz) {
         SPG_CUDA_TRY(cudaMemcpyAsync(cb.ptr, cols, nnz * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
@@ -276,8 +276,8 @@ int spg_csr_copy(spg_ctx *c, const spg_csr *src, spg_csr *dst) {
     }
     DevBuf off, cb, vb;
     SPG_TRY(off.alloc((src->n_rows + 1) * sizeof(uint64_t), s));
-    SPG_TRY(cb.alloc(src->nnz * sizeof(uint32_t), s));
-    SPG_TRY(vb.alloc(src->nnz * sizeof(double), s));
+    SPG_TRY(cb.alloc(csr_alloc_elems(src->nnz) * sizeof(uint32_t), s));
+    SPG_TRY(vb.alloc(csr_alloc_elems(src->nnz) * sizeof(double), s));
     SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, src->d_off(), (src->n_rows + 1) * sizeof(uint64_t),
                                  cudaMemcpyDeviceToDevice, s));
     if (src->nnz) {

@@ -118,12 +118,15 @@ struct Csr {
     bool stats_valid = false;
     uint64_t max_row = 0;
     int selected_spmv = -1;
-    SpmvPlan plan_stream, plan_merge;
+    SpmvPlan plan_stream, plan_merge, plan_adaptive;
+    uint64_t adaptive_long_rows = 0;  // second item count of plan_adaptive
     void invalidate_derived() {
         stats_valid = false;
         selected_spmv = -1;
         plan_stream = SpmvPlan{};
         plan_merge = SpmvPlan{};
+        plan_adaptive = SpmvPlan{};
+        adaptive_long_rows = 0;
     }
     const uint64_t *d_off() const { return off.as<uint64_t>(); }
     const uint32_t *d_cols() const { return cols.as<uint32_t>(); }
@@ -139,6 +142,11 @@ inline int bits_for(uint64_t n) {  // bits needed to represent 0..n-1
     while (b < 64 && (n - 1) >> b) ++b;
     return n <= 1 ? 0 : b;
 }
+
+// Elements to allocate for CSR cols/vals of a given capacity: rounded up to a
+// multiple of 16 plus 16 more, so kernels that read whole 16-aligned chunks of
+// 16 entries (SPG_SPMV_ADAPTIVE) never touch memory past the allocation.
+inline uint64_t csr_alloc_elems(uint64_t cap) { return ((cap + 15) & ~15ull) + 16; }
 
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 1u << 30) {
     uint64_t g = (n + block - 1) / block;
@@ -172,6 +180,9 @@ int csr_row_stats(Ctx *c, Csr *A, cudaStream_t s);
 int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant,
                 cudaStream_t s);
 int spmv_resolve_auto(Ctx *c, Csr *A, int *variant);
+// SPG_SPMV_ADAPTIVE with `items` (8 or 16) nonzeros per thread chunk
+// (spg_spmv_adaptive.cu); builds and caches its plan on first use.
+int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int items, cudaStream_t s);
 
 }  // namespace spg
 

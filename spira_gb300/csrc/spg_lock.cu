@@ -359,8 +359,8 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
         cap = (total_ub <= A->capacity) ? A->capacity : total_ub + total_ub / 2;
     }
     DevBuf out_cols, out_vals;
-    SPG_TRY(out_cols.alloc(cap * sizeof(uint32_t), s));
-    SPG_TRY(out_vals.alloc(cap * sizeof(double), s));
+    SPG_TRY(out_cols.alloc(csr_alloc_elems(cap) * sizeof(uint32_t), s));
+    SPG_TRY(out_vals.alloc(csr_alloc_elems(cap) * sizeof(double), s));
     if (has_old && A->nnz) {
         const uint64_t chunks = (A->nnz + MO_CHUNK - 1) / MO_CHUNK;
         merge_write_old<<<(unsigned)chunks, LB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), n, A->nnz,

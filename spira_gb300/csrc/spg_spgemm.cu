@@ -174,8 +174,8 @@ int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
         SPG_TRY(rc);
     }
     SPG_TRY(out_off.alloc((m + 1) * sizeof(uint64_t), s));
-    SPG_TRY(out_cols.alloc(nnz * sizeof(uint32_t), s));
-    SPG_TRY(out_vals.alloc(nnz * sizeof(double), s));
+    SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
+    SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     SPG_TRY(crow.alloc((nnz ? nnz : 1) * sizeof(uint32_t), s));
     if (U) {
         sg_write<<<grid_for(U, GB, gmax), GB, 0, s>>>(begin.as<uint64_t>(), key.as<uint64_t>(), sum.as<double>(),

@@ -483,6 +483,10 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStr
             merge_fixup<<<grid_for(nt, 256), 256, 0, s>>>(A->plan_merge.aux.as<Carry>(), nt, n, y);
             break;
         }
+        case SPG_SPMV_ADAPTIVE:
+            return spmv_adaptive(c, A, x, y, 16, s);
+        case SPG_SPMV_ADAPTIVE8:
+            return spmv_adaptive(c, A, x, y, 8, s);
         default:
             return set_error(SPG_ERR_INVALID_ARGUMENT, "spmv: unknown variant %d", variant);
     }
