@@ -82,6 +82,8 @@ int spg_ctx_create(int device, spg_ctx **out);
 int spg_ctx_destroy(spg_ctx *ctx);
 /* The context's own stream (cudaStream_t as void*). */
 int spg_ctx_stream(spg_ctx *ctx, void **stream);
+/* Waits for the context stream; SPG_ERR_DEVICE_TIMEOUT if a kernel's bounded
+ * wait gave up since the last check (the context stays usable). */
 int spg_ctx_sync(spg_ctx *ctx);
 
 /* ---- CSR handles ---------------------------------------------------------

@@ -107,11 +107,17 @@ int spg_ctx_create(int device, spg_ctx **out) {
         uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
         e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    // Status word in mapped pinned memory: kernels flag timeouts there and the
+    // host reads it after a synchronisation without an extra copy.
+    if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void **>(&c->h_status), sizeof(unsigned),
+                                            cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        *c->h_status = 0;
+        e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->d_status), c->h_status, 0);
+    }
     if (e != cudaSuccess) {
         if (c->stream) cudaStreamDestroy(c->stream);
-        if (c->d_status) cudaFree(c->d_status);
+        if (c->h_status) cudaFreeHost(c->h_status);
         delete c;
         return set_error(SPG_ERR_CUDA, "spg_ctx_create: %s", cudaGetErrorString(e));
     }
@@ -127,7 +133,7 @@ int spg_ctx_destroy(spg_ctx *c) {
     c->ybuf.release();
     cudaStreamSynchronize(c->stream);
     if (c->pinned) cudaFreeHost(c->pinned);
-    if (c->d_status) cudaFree(c->d_status);
+    if (c->h_status) cudaFreeHost(c->h_status);
     cudaStreamDestroy(c->stream);
     delete c;
     return SPG_OK;
@@ -142,7 +148,7 @@ int spg_ctx_stream(spg_ctx *c, void **stream) {
 int spg_ctx_sync(spg_ctx *c) {
     if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_sync: null context");
     SPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    return SPG_OK;
+    return c->take_status();
 }
 
 int spg_csr_create(spg_ctx *c, uint64_t n_rows, uint64_t n_cols, spg_csr **out) {
@@ -236,7 +242,7 @@ int spg_csr_load(spg_ctx *c, spg_csr *A, const uint64_t *offsets, const uint32_t
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     DevBuf off, cb, vb;
-    SPG_TRY(off.alloc((A->n_rows + 1) * sizeof(uint64_t), s));
+    SPG_TRY(off.alloc(csr_off_elems(A->n_rows) * sizeof(uint64_t), s));
     SPG_TRY(cb.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(vb.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, offsets, (A->n_rows + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
@@ -275,7 +281,7 @@ int spg_csr_copy(spg_ctx *c, const spg_csr *src, spg_csr *dst) {
         return SPG_OK;
     }
     DevBuf off, cb, vb;
-    SPG_TRY(off.alloc((src->n_rows + 1) * sizeof(uint64_t), s));
+    SPG_TRY(off.alloc(csr_off_elems(src->n_rows) * sizeof(uint64_t), s));
     SPG_TRY(cb.alloc(csr_alloc_elems(src->nnz) * sizeof(uint32_t), s));
     SPG_TRY(vb.alloc(csr_alloc_elems(src->nnz) * sizeof(double), s));
     SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, src->d_off(), (src->n_rows + 1) * sizeof(uint64_t),
@@ -371,7 +377,7 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
     if (y_len)
         SPG_CUDA_TRY(cudaMemcpyAsync(y, c->ybuf.ptr, y_len * sizeof(double), cudaMemcpyDeviceToHost, s));
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
-    return SPG_OK;
+    return c->take_status();
 }
 
 int spg_spmv_selected(spg_ctx *c, const spg_csr *Ac, int *variant) {

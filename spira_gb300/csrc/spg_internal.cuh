@@ -92,8 +92,18 @@ struct Ctx {
     cudaMemPool_t pool = nullptr;
     int n_sms = 0;
     size_t l2_bytes = 0;
-    // Device status word written by kernels with bounded waits; 0 = ok.
+    // Status word written by kernels whose bounded waits ran out; 0 = ok.
+    // Mapped pinned memory: h_status is the host view, d_status the device one.
+    unsigned int *h_status = nullptr;
     unsigned int *d_status = nullptr;
+    // Returns SPG_ERR_DEVICE_TIMEOUT (and clears the word) if a kernel flagged
+    // one since the last check; call after a stream synchronisation.
+    int take_status() {
+        const unsigned v = h_status ? *(volatile unsigned *)h_status : 0u;
+        if (!v) return SPG_OK;
+        *(volatile unsigned *)h_status = 0;
+        return set_error(SPG_ERR_DEVICE_TIMEOUT, "a device-side wait gave up (status 0x%x)", v);
+    }
     // Pinned host staging for the *_host entry points.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -147,6 +157,10 @@ inline int bits_for(uint64_t n) {  // bits needed to represent 0..n-1
 // multiple of 16 plus 16 more, so kernels that read whole 16-aligned chunks of
 // 16 entries (SPG_SPMV_ADAPTIVE) never touch memory past the allocation.
 inline uint64_t csr_alloc_elems(uint64_t cap) { return ((cap + 15) & ~15ull) + 16; }
+// Entries to allocate for CSR offsets of n rows: n + 1 plus 2 spare, so a
+// 16-byte bulk copy of offsets [r0 & ~1, r1 + 1] rounded to an even count
+// stays inside the allocation.
+inline uint64_t csr_off_elems(uint64_t n_rows) { return n_rows + 3; }
 
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 1u << 30) {
     uint64_t g = (n + block - 1) / block;

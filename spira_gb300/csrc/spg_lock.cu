@@ -342,7 +342,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     SPG_TRY(exclusive_scan_i64(c, P.as<int64_t>(), u + 1, s));
 
     DevBuf new_off;
-    SPG_TRY(new_off.alloc((n + 1) * sizeof(uint64_t), s));
+    SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
     merge_row_counts<<<grid_for(n + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
         A->d_off(), has_old, doff.as<uint64_t>(), P.as<int64_t>(), n, new_off.as<uint64_t>());
     SPG_LAUNCH_CHECK();

@@ -173,7 +173,7 @@ int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
         nnz = read_u64(keep.as<uint64_t>() + U, s, &rc);
         SPG_TRY(rc);
     }
-    SPG_TRY(out_off.alloc((m + 1) * sizeof(uint64_t), s));
+    SPG_TRY(out_off.alloc(csr_off_elems(m) * sizeof(uint64_t), s));
     SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     SPG_TRY(crow.alloc((nnz ? nnz : 1) * sizeof(uint32_t), s));

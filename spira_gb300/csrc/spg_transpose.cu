@@ -65,7 +65,7 @@ int transpose_impl(Ctx *c, const Csr *A, Csr *T, cudaStream_t s) {
     if (nnz >= (1ull << 32))
         return set_error(SPG_ERR_UNSUPPORTED, "transpose: nnz %llu exceeds 2^32-1", (unsigned long long)nnz);
     DevBuf key, idx, rowid, out_off, out_cols, out_vals, rk;
-    SPG_TRY(out_off.alloc((n + 1) * sizeof(uint64_t), s));
+    SPG_TRY(out_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
     SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     if (nnz) {

@@ -15,7 +15,7 @@ AD_BLOCK, AD_LONG, AD_ROWCAP = 256, 128, 1024
 
 def plan(off, items):
     n = len(off) - 1
-    BIN = AD_BLOCK * items - items - AD_LONG
+    BIN = AD_BLOCK * items - 16 - AD_LONG
     lens = np.diff(off)
     lng = lens > AD_LONG
     brk = np.zeros(n, bool)
@@ -34,8 +34,13 @@ def run_tile(off, cols, vals, x, r0, r1, items, alloc, y, writes):
     assert 1 <= nr <= AD_ROWCAP
     k0, k1 = int(off[r0]), int(off[r1])
     s_end = [int(off[r0 + i + 1] - k0) for i in range(nr)]
-    a0 = k0 & ~(items - 1)
-    assert (k1 - a0) <= AD_BLOCK * items, "tile spans more chunks than threads"
+    a0 = k0 & ~15
+    span = ((k1 + 15) & ~15) - a0
+    assert span <= AD_BLOCK * items, "bulk-copy window larger than a stage"
+    assert a0 + span <= alloc, "bulk-copy window leaves the cols/vals allocation"
+    ro = r0 & ~1
+    nro = ((r1 + 1 - ro) + 1) & ~1
+    assert nro <= AD_ROWCAP + 2 and ro + nro <= (len(off) - 1) + 3, "offsets window leaves its allocation"
     if k1 == k0:
         for i in range(nr):
             y[r0 + i] = 0.0
