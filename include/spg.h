@@ -53,9 +53,10 @@ enum spg_spmv_variant {
     SPG_SPMV_VECTOR32 = 5,  /* one warp per row, 16-byte vector loads */
     SPG_SPMV_STREAM = 6,    /* CTA row blocks: coalesced nnz staging in shared memory */
     SPG_SPMV_MERGE = 7,     /* merge-path: equal (rows + nnz) per CTA, carry fix-up */
-    SPG_SPMV_ADAPTIVE = 8,  /* row-aligned nnz tiles, one FMA per nnz per thread chain
-                               over 16 nonzeros; rows > 128 nnz on a warp each */
-    SPG_SPMV_ADAPTIVE8 = 9, /* the same with 8 nonzeros per thread chain */
+    SPG_SPMV_ADAPTIVE = 8,  /* warp per 1024 nonzeros, 32 consecutive per lane in one
+                               FMA chain, rows closed at a row-start bitmap, segmented
+                               combine across lanes and chunks */
+    SPG_SPMV_ADAPTIVE16 = 9, /* the same with 16 nonzeros per lane */
     SPG_SPMV_N_VARIANTS = 10
 };
 

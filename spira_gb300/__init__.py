@@ -20,10 +20,10 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libspg.so"
 
 SPMV_AUTO, SPMV_SCALAR, SPMV_VECTOR2, SPMV_VECTOR4, SPMV_VECTOR8, SPMV_VECTOR16, SPMV_VECTOR32, \
-    SPMV_STREAM, SPMV_MERGE, SPMV_ADAPTIVE, SPMV_ADAPTIVE8 = -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
+    SPMV_STREAM, SPMV_MERGE, SPMV_ADAPTIVE, SPMV_ADAPTIVE16 = -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
 SPMV_VARIANTS = {
     "scalar": 0, "vector2": 1, "vector4": 2, "vector8": 3, "vector16": 4, "vector32": 5,
-    "stream": 6, "merge": 7, "adaptive": 8, "adaptive8": 9,
+    "stream": 6, "merge": 7, "adaptive": 8, "adaptive16": 9,
 }
 SPMV_NAMES = {v: k for k, v in SPMV_VARIANTS.items()}
 

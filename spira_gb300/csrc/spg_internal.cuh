@@ -81,9 +81,11 @@ struct DevBuf {
 // Cached SpMV plan (row blocks for the stream / merge variants).
 struct SpmvPlan {
     int kind = -1;           // variant the plan belongs to
-    uint64_t n_items = 0;    // number of work items (blocks / tiles)
+    uint64_t n_items = 0;    // number of work items (blocks / tiles / chunks)
+    uint64_t count1 = 0;     // variant-specific count
     DevBuf items;            // variant-specific item descriptors
     DevBuf aux;              // variant-specific scratch (carry-outs)
+    DevBuf extra0, extra1, extra2;
 };
 
 struct Ctx {
@@ -129,14 +131,12 @@ struct Csr {
     uint64_t max_row = 0;
     int selected_spmv = -1;
     SpmvPlan plan_stream, plan_merge, plan_adaptive;
-    uint64_t adaptive_long_rows = 0;  // second item count of plan_adaptive
     void invalidate_derived() {
         stats_valid = false;
         selected_spmv = -1;
         plan_stream = SpmvPlan{};
         plan_merge = SpmvPlan{};
         plan_adaptive = SpmvPlan{};
-        adaptive_long_rows = 0;
     }
     const uint64_t *d_off() const { return off.as<uint64_t>(); }
     const uint32_t *d_cols() const { return cols.as<uint32_t>(); }

@@ -1,8 +1,10 @@
-"""Host model of SPG_SPMV_ADAPTIVE's plan and thread ownership
-(spira_gb300/csrc/spg_spmv_adaptive.cu), run on the CPU: every shared-memory
-index and every aligned chunk load stays inside its buffer, and every row is
-written exactly once with the right sum. Mirrors the kernel's integer logic
-step by step."""
+"""Host model of SPG_SPMV_ADAPTIVE (spira_gb300/csrc/spg_spmv_adaptive.cu),
+run on the CPU before the kernel ever runs: it follows the kernel's integer
+logic lane by lane (bitmap words, row-start prefix counts, vector-load
+windows, direct writes, chunk records and the record fix-up) and checks that
+every load window stays inside the padded CSR allocation, that only real
+columns are gathered, and that every row's y is written exactly once with
+the right sum."""
 from __future__ import annotations
 
 import numpy as np
@@ -10,96 +12,126 @@ import pytest
 
 from spira_gb300 import gen
 
-AD_BLOCK, AD_LONG, AD_ROWCAP = 256, 128, 1024
+NONE = 0xFFFFFFFF
 
 
-def plan(off, items):
+def model(off, cols, vals, x, items):
     n = len(off) - 1
-    BIN = AD_BLOCK * items - 16 - AD_LONG
+    nnz = int(off[-1])
+    alloc = ((nnz + 15) & ~15) + 16          # csr_alloc_elems(nnz)
     lens = np.diff(off)
-    lng = lens > AD_LONG
-    brk = np.zeros(n, bool)
-    for r in range(n):
-        b = lng[r] or r == 0 or r % AD_ROWCAP == 0
-        if not b:
-            b = lens[r - 1] > AD_LONG or (off[r - 1] // BIN) != (off[r] // BIN)
-        brk[r] = b
-    B = list(np.nonzero(brk)[0]) + [n]
-    tiles = [(B[j], B[j + 1]) for j in range(len(B) - 1) if not lng[B[j]]]
-    return tiles, list(np.nonzero(lng)[0])
+    nonempty = np.nonzero(lens > 0)[0]
+    nzrow = nonempty if len(nonempty) < n else None
+    bitmap = np.zeros((nnz + 31) // 32 + 1, np.uint64)
+    for r in nonempty:
+        b = int(off[r])
+        bitmap[b >> 5] |= np.uint64(1 << (b & 31))
+    chunk = 32 * items
+    n_chunks = (nnz + chunk - 1) // chunk
+    pc = np.array([bin(int(w)).count("1") for w in bitmap], np.int64)
+    pcs = np.concatenate([[0], np.cumsum(pc)])
+    chunk_base = [int(pcs[c * items]) for c in range(n_chunks)]
+    y = np.full(n, np.nan)
+    writes = np.zeros(n, np.int64)
 
+    def ywrite(i):
+        return int(nzrow[i]) if nzrow is not None else i
 
-def run_tile(off, cols, vals, x, r0, r1, items, alloc, y, writes):
-    nr = r1 - r0
-    assert 1 <= nr <= AD_ROWCAP
-    k0, k1 = int(off[r0]), int(off[r1])
-    s_end = [int(off[r0 + i + 1] - k0) for i in range(nr)]
-    a0 = k0 & ~15
-    span = ((k1 + 15) & ~15) - a0
-    assert span <= AD_BLOCK * items, "bulk-copy window larger than a stage"
-    assert a0 + span <= alloc, "bulk-copy window leaves the cols/vals allocation"
-    ro = r0 & ~1
-    nro = ((r1 + 1 - ro) + 1) & ~1
-    assert nro <= AD_ROWCAP + 2 and ro + nro <= (len(off) - 1) + 3, "offsets window leaves its allocation"
-    if k1 == k0:
-        for i in range(nr):
-            y[r0 + i] = 0.0
-            writes[r0 + i] += 1
-        return
-    tails, heads = {}, {}
-    for t in range(AD_BLOCK):
-        ca = a0 + items * t
-        lo, hi = max(ca, k0), min(ca + items, k1)
-        if lo >= hi:
-            continue
-        assert ca % items == 0 and ca + items <= alloc  # aligned chunk inside the allocation
-        plo, phi = lo - k0, hi - k0
-        row, head = 0, False
-        if plo > 0:
-            l, h = 0, nr - 1
-            while l < h:
-                m = (l + h) >> 1
-                if s_end[m] > plo:
-                    h = m
-                else:
-                    l = m + 1
-            row = l
-            head = (0 if row == 0 else s_end[row - 1]) < plo
-        rfirst, acc, head_row = row, 0.0, None
-        for u in range(items):
-            it = ca + u
-            if it < lo or it >= hi:
+    recs = [None] * (2 * n_chunks)
+    for w in range(n_chunks):
+        lanes = []
+        for lane in range(32):
+            p0 = w * chunk + lane * items
+            word = 0
+            if p0 < nnz:
+                word = (int(bitmap[p0 >> 5]) >> (p0 & 31))
+                if items < 32:
+                    word &= (1 << items) - 1
+                if nnz - p0 < items:
+                    word &= (1 << (nnz - p0)) - 1
+            lanes.append((p0, word))
+        pcs_l = [bin(wd).count("1") for _, wd in lanes]
+        excl = np.concatenate([[0], np.cumsum(pcs_l)])[:32]
+        state = []
+        for lane, (p0, word) in enumerate(lanes):
+            sb = chunk_base[w] + int(excl[lane])
+            cur = sb - 1
+            acc, head, seen = 0.0, 0.0, False
+            for h in range(items // 16):
+                base = p0 + 16 * h
+                nv = min(nnz - base, 16) if base < nnz else 0
+                if nv:
+                    assert base % 16 == 0 and base + 16 <= alloc, "vector load window leaves allocation"
+                for u in range(16):
+                    i = 16 * h + u
+                    if (word >> i) & 1:
+                        if not seen:
+                            head, seen = acc, True
+                        else:
+                            assert 0 <= cur
+                            r = ywrite(cur)
+                            y[r] = acc
+                            writes[r] += 1
+                        acc = 0.0
+                        cur += 1
+                    if u < nv:
+                        k = base + u
+                        acc += x[cols[k]] * vals[k]
+            state.append((sb, cur, acc, head, word != 0, word))
+        has = [s[4] for s in state]
+        carry = [0.0] * 32
+        run = 0.0
+        for lane in range(32):  # exclusive segmented scan of tails
+            carry[lane] = run
+            tail = state[lane][2]
+            run = tail if has[lane] else run + tail
+        for lane in range(32):
+            sb, cur, tail, head, hs, word = state[lane]
+            if not hs:
                 continue
-            p = it - k0
-            while s_end[row] <= p:
-                assert row < nr
-                if head and row == rfirst:
-                    heads[t] = (row, acc)
-                    head_row = row
-                else:
-                    y[r0 + row] = acc
-                    writes[r0 + row] += 1
-                acc = 0.0
-                row += 1
-            acc += x[cols[it]] * vals[it]
-        while row < nr and s_end[row] <= phi:
-            if head and row == rfirst:
-                heads[t] = (row, acc)
-                head_row = row
+            total = carry[lane] + head
+            if any(has[:lane]):
+                r = ywrite(sb - 1)
+                y[r] = total
+                writes[r] += 1
             else:
-                y[r0 + row] = acc
-                writes[r0 + row] += 1
-            acc = 0.0
-            row += 1
-        if row < nr:
-            tails[t] = (row, acc)
-    for t, (hr, hv) in heads.items():
-        j = t - 1
-        while j >= 0 and j in tails and tails[j][0] == hr:
-            j -= 1
-        s = sum(tails[q][1] for q in range(j + 1, t))
-        y[r0 + hr] = s + hv
-        writes[r0 + hr] += 1
+                recs[2 * w] = (NONE if (lane == 0 and (word & 1)) else sb - 1, total)
+        sb, cur, tail, head, hs, word = state[31]
+        out = tail if hs else carry[31] + tail
+        if not any(has):
+            recs[2 * w] = (cur, out)
+            recs[2 * w + 1] = (NONE, 0.0)
+        else:
+            recs[2 * w + 1] = (cur, out)
+    assert all(r is not None for r in recs), "a chunk record was left unwritten"
+    for q in range(len(recs)):  # seg_fixup
+        row = recs[q][0]
+        if row == NONE:
+            continue
+        if q > 0:
+            p = q - 1
+            if recs[p][0] == NONE and p > 0:
+                p -= 1
+            if recs[p][0] == row:
+                continue
+        s = recs[q][1]
+        k = q + 1
+        while k < len(recs):
+            r = recs[k][0]
+            if r == NONE and k + 1 < len(recs):
+                k += 1
+                r = recs[k][0]
+            if r != row:
+                break
+            s += recs[k][1]
+            k += 1
+        rr = ywrite(row)
+        y[rr] = s
+        writes[rr] += 1
+    for r in np.nonzero(lens == 0)[0]:
+        y[r] = 0.0
+        writes[r] += 1
+    return y, writes
 
 
 def check(lengths, items, seed=0):
@@ -107,40 +139,29 @@ def check(lengths, items, seed=0):
     off = np.zeros(len(lengths) + 1, np.int64)
     off[1:] = np.cumsum(lengths)
     nnz = int(off[-1])
-    alloc = ((nnz + 15) & ~15) + 16
-    n_cols = 1000
     ctr = np.arange(nnz, dtype=np.uint64)
-    cols = gen.below(gen.hash3(seed, 1, ctr), n_cols)
+    cols = gen.below(gen.hash3(seed, 1, ctr), 1000)
     vals = gen.sym_unit(gen.hash3(seed, 2, ctr))
-    x = gen.dense_x(n_cols, seed + 1)
-    tiles, longs = plan(off, items)
-    y = np.full(len(lengths), np.nan)
-    writes = np.zeros(len(lengths), np.int64)
-    for r0, r1 in tiles:
-        run_tile(off, cols, vals, x, r0, r1, items, alloc, y, writes)
-    for r in longs:
-        b, e = int(off[r]), int(off[r + 1])
-        a0 = b & ~(items - 1)
-        assert ((e - a0 + items - 1) // items) * items + a0 <= alloc
-        y[r] = float(np.dot(x[cols[b:e]], vals[b:e]))
-        writes[r] += 1
-    assert np.all(writes == 1), np.nonzero(writes != 1)[0][:10]
+    x = gen.dense_x(1000, seed + 1)
+    y, writes = model(off, cols, vals, x, items)
+    assert np.all(writes == 1), (np.nonzero(writes != 1)[0][:10], writes[writes != 1][:10])
     ref = np.array([np.dot(x[cols[off[r]:off[r + 1]]], vals[off[r]:off[r + 1]]) for r in range(len(lengths))])
     np.testing.assert_allclose(y, ref, rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.parametrize("items", [8, 16])
+@pytest.mark.parametrize("items", [16, 32])
 @pytest.mark.parametrize("lengths", [
-    [0], [1], [0, 0, 0], [5] * 3000, [0] * 2500 + [3] + [0] * 10,
+    [0], [1], [0, 0, 0], [5] * 700, [0] * 50 + [3] + [0] * 10,
     [128, 129, 127, 0, 1, 2000, 128, 3, 4095, 1],
-    [1, 0, 2, 0, 0, 3] * 700,
-    [16] * 1000, [15, 17] * 600,
+    [1, 0, 2, 0, 0, 3] * 300,
+    [16] * 300, [15, 17] * 200, [32] * 100, [1024] * 3, [1023, 1025, 1],
+    [5000], [0, 5000, 0],
 ])
 def test_adaptive_model(items, lengths):
     check(lengths, items)
 
 
-@pytest.mark.parametrize("items", [8, 16])
+@pytest.mark.parametrize("items", [16, 32])
 def test_adaptive_model_zipf(items):
-    L = gen.zipf_lengths(20_000, 1.8, 10_000, 16.0, seed=3)
+    L = gen.zipf_lengths(3000, 1.8, 10_000, 16.0, seed=3)
     check(L, items, seed=4)
