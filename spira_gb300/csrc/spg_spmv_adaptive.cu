@@ -74,8 +74,10 @@ __global__ void seg_row_maps(const uint64_t *__restrict__ ne_scan, uint64_t n, u
 }
 
 // ---------------------------------------------------------------- SpMV
-template <int ITEMS>
-__global__ void __launch_bounds__(256)
+// ITEMS nonzeros per lane, handled in sub-batches of SUB (loads, gathers, FMAs)
+// to keep registers low enough for 4 CTAs of 256 threads per SM.
+template <int ITEMS, int SUB>
+__global__ void __launch_bounds__(256, 4)
 spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, const double *__restrict__ x,
          double *__restrict__ y, uint64_t nnz, const unsigned *__restrict__ bitmap,
          const uint32_t *__restrict__ chunk_base, const uint32_t *__restrict__ nzrow, Rec *__restrict__ recs,
@@ -103,20 +105,20 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
     double acc = 0.0, head = 0.0;
     bool seen = false;
 #pragma unroll
-    for (int h = 0; h < ITEMS / 16; ++h) {
-        const uint64_t base = p0 + 16ull * h;
-        const uint32_t nv = base < nnz ? (uint32_t)min(nnz - base, (uint64_t)16) : 0u;
-        double v[16], g[16];
-        uint32_t c[16];
+    for (int h = 0; h < ITEMS / SUB; ++h) {
+        const uint64_t base = p0 + (uint64_t)SUB * h;
+        const uint32_t nv = base < nnz ? (uint32_t)min(nnz - base, (uint64_t)SUB) : 0u;
+        double v[SUB], g[SUB];
+        uint32_t c[SUB];
         if (nv) {
 #pragma unroll
-            for (int u = 0; u < 16; u += 2) {
+            for (int u = 0; u < SUB; u += 2) {
                 const double2 t = *reinterpret_cast<const double2 *>(vals + base + u);
                 v[u] = t.x;
                 v[u + 1] = t.y;
             }
 #pragma unroll
-            for (int u = 0; u < 16; u += 4) {
+            for (int u = 0; u < SUB; u += 4) {
                 const uint4 t = *reinterpret_cast<const uint4 *>(cols + base + u);
                 c[u] = t.x;
                 c[u + 1] = t.y;
@@ -125,14 +127,14 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
             }
         }
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
+        for (int u = 0; u < SUB; ++u) {
             g[u] = 0.0;
             if ((uint32_t)u < nv) g[u] = ldx(x, c[u]);  // only real columns are read
             else v[u] = 0.0;
         }
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-            if ((word >> (16 * h + u)) & 1u) {  // a row starts at this nonzero: close the previous one
+        for (int u = 0; u < SUB; ++u) {
+            if ((word >> (SUB * h + u)) & 1u) {  // a row starts at this nonzero: close the previous one
                 if (!seen) {
                     head = acc;
                     seen = true;
@@ -294,10 +296,10 @@ int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int items, cudaStr
     if (nch) {
         const unsigned grid = grid_for(nch * 32, 256);
         if (items == 16)
-            spmv_seg<16><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
+            spmv_seg<16, 8><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
                                               P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), nch);
         else
-            spmv_seg<32><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
+            spmv_seg<32, 8><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
                                               P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), nch);
         SPG_LAUNCH_CHECK();
         seg_fixup<<<grid_for(2 * nch, 256), 256, 0, s>>>(P.aux.as<Rec>(), 2 * nch, nzrow, y);
