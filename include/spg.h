@@ -142,6 +142,46 @@ int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
 /* The variant SPG_SPMV_AUTO resolves to for A. */
 int spg_spmv_selected(spg_ctx *ctx, const spg_csr *A, int *variant);
 
+/* ---- SpMV variant choice ----------------------------------------------------
+ * No Spira counterpart: Spira has a single SpMV code path per type
+ * combination (serial/spmv.hpp:141-186). These choose which of this engine's
+ * kernels computes it; the arithmetic is the same whichever is chosen.
+ * SPG_SPMV_AUTO follows the context's policy (per matrix, cached until the
+ * next lock): SPG_POLICY_SELECTOR uses the learned selector when one is
+ * loaded and the exhaustive autotuner otherwise; SPG_POLICY_AUTOTUNE always
+ * autotunes; SPG_POLICY_FIXED takes SPG_SPMV_ADAPTIVE16 without measuring. */
+#define SPG_SELECT_FEATURES 40 /* 32-bin log2 row-length histogram + 8 shape stats */
+#define SPG_SELECT_HIDDEN 64   /* MLP 40 -> 64 -> 64 -> K, FP32, ReLU */
+enum spg_spmv_policy { SPG_POLICY_SELECTOR = 0, SPG_POLICY_AUTOTUNE = 1, SPG_POLICY_FIXED = 2 };
+
+int spg_set_spmv_policy(spg_ctx *ctx, int policy);
+/* The 40 selector features of A (host array). */
+int spg_spmv_features(spg_ctx *ctx, const spg_csr *A, float *features);
+/* Times every variant (median of `reps` warm runs, CUDA events): times_ms
+ * [SPG_SPMV_N_VARIANTS] (may be NULL) and the fastest in *best (may be NULL). */
+int spg_spmv_autotune(spg_ctx *ctx, const spg_csr *A, int reps, float *times_ms, int *best);
+/* Installs a trained selector (NULL blob removes it). Blob layout, FP32:
+ * mean[40] scale[40] W1[64][40] b1[64] W2[64][64] b2[64] W3[K][64] b3[K];
+ * output k predicts log(time of variant k / fastest time). */
+int spg_selector_load(spg_ctx *ctx, const float *blob, uint64_t n_floats, int n_outputs);
+/* Number of MLP parameters (W1..b3) for K outputs. */
+uint64_t spg_mlp_param_count(int n_outputs);
+/* Batched inference of the loaded selector on device features [B][40]. */
+int spg_selector_predict(spg_ctx *ctx, const float *d_features, uint32_t B, float *d_out, void *stream);
+/* Training kernels on device buffers (FP32). d_act holds [B][2*64]
+ * activations from forward for backward; d_grad has the parameter layout. */
+int spg_mlp_forward(spg_ctx *ctx, const float *d_params, int n_outputs, const float *d_x, uint32_t B,
+                    float *d_act, float *d_out, void *stream);
+int spg_mlp_backward(spg_ctx *ctx, const float *d_params, int n_outputs, const float *d_x, uint32_t B,
+                     const float *d_act, const float *d_dout, float *d_grad, void *stream);
+/* Mean squared error over n outputs: d_dpred = 2 (pred - target) / n; the
+ * loss is added to *d_loss when d_loss is not NULL. */
+int spg_mlp_mse(spg_ctx *ctx, const float *d_pred, const float *d_target, uint64_t n, float *d_dpred,
+                float *d_loss, void *stream);
+int spg_mlp_adam(spg_ctx *ctx, float *d_params, const float *d_grad, float *d_m, float *d_v, uint64_t n,
+                 float lr, float beta1, float beta2, float eps, uint32_t step, void *stream);
+int spg_mlp_argmin(spg_ctx *ctx, const float *d_pred, uint32_t B, int n_outputs, int *d_best, void *stream);
+
 /* ---- transpose / SpGEMM ----------------------------------------------------
  * spg_transpose: AT <- A^T (AT is reshaped to n_cols x n_rows, capacity ==
  * nnz); each output row lists its source rows in ascending order

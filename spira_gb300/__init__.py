@@ -101,12 +101,28 @@ _SIGS = [
     ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
     ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
     ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
+    ("spg_set_spmv_policy", _I, [_P, _I]),
+    ("spg_spmv_features", _I, [_P, _P, _P]),
+    ("spg_spmv_autotune", _I, [_P, _P, _I, _P, C.POINTER(_I)]),
+    ("spg_selector_load", _I, [_P, _P, _U64, _I]),
+    ("spg_mlp_param_count", _U64, [_I]),
+    ("spg_selector_predict", _I, [_P, _P, _U32, _P, _P]),
+    ("spg_mlp_forward", _I, [_P, _P, _I, _P, _U32, _P, _P, _P]),
+    ("spg_mlp_backward", _I, [_P, _P, _I, _P, _U32, _P, _P, _P, _P]),
+    ("spg_mlp_mse", _I, [_P, _P, _P, _U64, _P, _P, _P]),
+    ("spg_mlp_adam", _I, [_P, _P, _P, _P, _P, _U64, C.c_float, C.c_float, C.c_float, C.c_float, _U32, _P]),
+    ("spg_mlp_argmin", _I, [_P, _P, _U32, _I, _P, _P]),
     ("spg_transpose", _I, [_P, _P, _P]),
     ("spg_spgemm", _I, [_P, _P, _P, _P]),
     # spg_gen.h
     ("spg_gen_draw", _I, [_P, _U64, _U64, _U64, _U64, _I, _U64, _P]),
     ("spg_gen_expand_rows", _I, [_P, _P, _U64, _P, C.POINTER(_U64)]),
+    ("spg_gen_family", _I, [_P, _I, _U64, _U64, C.c_double, _P, _U64, _P, _P, _P, C.POINTER(_U64)]),
 ]
+
+N_FEATURES, N_HIDDEN = 40, 64
+POLICY_SELECTOR, POLICY_AUTOTUNE, POLICY_FIXED = 0, 1, 2
+FAM_BANDED, FAM_BLOCKDIAG, FAM_POWERLAW, FAM_UNIFORM, FAM_STENCIL2D, FAM_STENCIL3D, FAM_POISSON = range(7)
 
 
 def exported_symbols() -> list[str]:
@@ -172,6 +188,17 @@ class Context:
 
     def sync(self):
         _check(lib().spg_ctx_sync(self.h))
+
+    def set_spmv_policy(self, policy: int):
+        _check(lib().spg_set_spmv_policy(self.h, policy))
+
+    def load_selector(self, blob, n_outputs: int):
+        """Install a selector blob (numpy float32) for SPMV_AUTO; None removes it."""
+        if blob is None:
+            _check(lib().spg_selector_load(self.h, None, 0, 0))
+            return
+        blob = np.ascontiguousarray(blob, dtype=np.float32)
+        _check(lib().spg_selector_load(self.h, _ptr(blob), len(blob), n_outputs))
 
 
 class Csr:
@@ -272,6 +299,18 @@ class Csr:
         _check(lib().spg_spmv_selected(self.ctx.h, self.h, C.byref(v)))
         return v.value
 
+    def features(self) -> np.ndarray:
+        f = np.empty(N_FEATURES, np.float32)
+        _check(lib().spg_spmv_features(self.ctx.h, self.h, _ptr(f)))
+        return f
+
+    def autotune(self, reps: int = 5):
+        """(times_ms per variant, fastest variant)."""
+        t = np.empty(len(SPMV_VARIANTS), np.float32)
+        b = C.c_int()
+        _check(lib().spg_spmv_autotune(self.ctx.h, self.h, reps, _ptr(t), C.byref(b)))
+        return t, b.value
+
     def transpose(self) -> "Csr":
         """A new device matrix holding A^T."""
         T = Csr(self.ctx, 0, 0)
@@ -298,3 +337,37 @@ def gen_expand_rows(ctx: Context, d_lengths, n_rows: int, d_rows=None) -> int:
     tot = C.c_uint64()
     _check(lib().spg_gen_expand_rows(ctx.h, _ptr(d_lengths), n_rows, _ptr(d_rows), C.byref(tot)))
     return tot.value
+
+
+def gen_family(ctx: Context, family: int, n_rows: int, p: int, ls: float = 0.0, d_cdf=None, seed: int = 0,
+               d_rows=None, d_cols=None, d_vals=None) -> int:
+    m = C.c_uint64()
+    _check(lib().spg_gen_family(ctx.h, family, n_rows, p, ls, _ptr(d_cdf), seed, _ptr(d_rows), _ptr(d_cols),
+                                _ptr(d_vals), C.byref(m)))
+    return m.value
+
+
+class Mlp:
+    """Device-side FP32 MLP 40 -> 64 -> 64 -> K through libspg's kernels
+    (buffers are torch CUDA tensors)."""
+
+    def __init__(self, ctx: Context, n_outputs: int):
+        self.ctx, self.K = ctx, n_outputs
+        self.n_params = int(lib().spg_mlp_param_count(n_outputs))
+
+    def forward(self, params, X, act, out, B: int):
+        _check(lib().spg_mlp_forward(self.ctx.h, _ptr(params), self.K, _ptr(X), B, _ptr(act), _ptr(out), None))
+
+    def backward(self, params, X, act, dout, grad, B: int):
+        _check(lib().spg_mlp_backward(self.ctx.h, _ptr(params), self.K, _ptr(X), B, _ptr(act), _ptr(dout),
+                                      _ptr(grad), None))
+
+    def mse(self, pred, target, n: int, dpred, loss=None):
+        _check(lib().spg_mlp_mse(self.ctx.h, _ptr(pred), _ptr(target), n, _ptr(dpred), _ptr(loss), None))
+
+    def adam(self, params, grad, m, v, lr, step, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(lib().spg_mlp_adam(self.ctx.h, _ptr(params), _ptr(grad), _ptr(m), _ptr(v), self.n_params, lr, beta1,
+                                  beta2, eps, step, None))
+
+    def argmin(self, pred, B: int, best):
+        _check(lib().spg_mlp_argmin(self.ctx.h, _ptr(pred), B, self.K, _ptr(best), None))

@@ -121,6 +121,7 @@ int spg_ctx_create(int device, spg_ctx **out) {
         delete c;
         return set_error(SPG_ERR_CUDA, "spg_ctx_create: %s", cudaGetErrorString(e));
     }
+    selector_load_default(c);
     *out = c;
     return SPG_OK;
 }

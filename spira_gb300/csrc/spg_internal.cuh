@@ -112,6 +112,10 @@ struct Ctx {
     int ensure_pinned(size_t bytes);
     // Device vectors reused by spg_spmv_host.
     DevBuf xbuf, ybuf;
+    // SpMV variant choice: policy and the loaded selector (spg_tune.cu).
+    int spmv_policy = SPG_POLICY_SELECTOR;
+    DevBuf model;  // FP32 selector blob
+    int model_k = 0;
 };
 
 struct Csr {
@@ -194,6 +198,8 @@ int csr_row_stats(Ctx *c, Csr *A, cudaStream_t s);
 int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant,
                 cudaStream_t s);
 int spmv_resolve_auto(Ctx *c, Csr *A, int *variant);
+// Loads spg_selector.bin from beside libspg.so (or $SPG_SELECTOR_MODEL) if any.
+int selector_load_default(Ctx *c);
 // SPG_SPMV_ADAPTIVE with `items` (8 or 16) nonzeros per thread chunk
 // (spg_spmv_adaptive.cu); builds and caches its plan on first use.
 int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int items, cudaStream_t s);

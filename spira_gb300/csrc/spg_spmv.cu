@@ -494,17 +494,4 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStr
     return SPG_OK;
 }
 
-int spmv_resolve_auto(Ctx *c, Csr *A, int *variant) {
-    // Placeholder policy until the selector lands: long-row-heavy matrices go
-    // to STREAM, short regular rows to VECTOR4.
-    (void)c;
-    if (A->selected_spmv >= 0) {
-        *variant = A->selected_spmv;
-        return SPG_OK;
-    }
-    *variant = SPG_SPMV_STREAM;
-    A->selected_spmv = *variant;
-    return SPG_OK;
-}
-
 }  // namespace spg

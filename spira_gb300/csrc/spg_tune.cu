@@ -1,0 +1,489 @@
+// spg_tune.cu — variant choice for SpMV: the exhaustive autotuner, the
+// matrix features, and the learned selector (a 40 -> 64 -> 64 -> K FP32 MLP
+// with hand-written forward, backward and Adam kernels).
+//
+// Spira has a single SpMV code path per type combination (serial/spmv.hpp,
+// parallel/algorithms/spmv.hpp), so none of this has a Spira counterpart; it
+// decides which of this engine's kernels computes Spira's SpMV. The
+// arithmetic of the SpMV kernels is the same whichever is chosen.
+//
+// Policy for SPG_SPMV_AUTO (per matrix, cached until the next lock):
+//   a selector model is installed -> features + MLP inference on the device,
+//                                    argmin of the predicted log-times;
+//   otherwise                      -> exhaustive autotune (every variant timed
+//                                    with CUDA events), fastest wins.
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "spg_internal.cuh"
+
+namespace spg {
+namespace {
+
+// ---------------------------------------------------------------- features
+// acc layout (doubles): [0..31] histogram, 32 sum L, 33 sum L^2, 34 max L,
+// 35 empty rows, 36 sum of |col/n_cols - row/n_rows| over sampled nonzeros,
+// 37 sampled nonzeros.
+__global__ void feat_rows(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols, uint64_t n_rows,
+                          uint64_t n_cols, double *__restrict__ acc) {
+    __shared__ double s[38];
+    for (int i = threadIdx.x; i < 38; i += blockDim.x) s[i] = 0.0;
+    __syncthreads();
+    double sl = 0, sl2 = 0, mx = 0, emp = 0, spread = 0, cnt = 0;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n_rows;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = off[r], e = off[r + 1];
+        const uint64_t L = e - b;
+        int bin = 0;
+        if (L) {
+            bin = 1 + (63 - __clzll((long long)L));
+            if (bin > 31) bin = 31;
+        } else {
+            emp += 1;
+        }
+        atomicAdd(&s[bin], 1.0);
+        sl += (double)L;
+        sl2 += (double)L * (double)L;
+        mx = fmax(mx, (double)L);
+        if ((r & 15) == 0 && L) {  // spread proxy on every 16th row, first and last entry
+            const double rr = (double)r / (double)n_rows;
+            spread += fabs((double)cols[b] / (double)n_cols - rr) + fabs((double)cols[e - 1] / (double)n_cols - rr);
+            cnt += 2;
+        }
+    }
+    atomicAdd(&s[32], sl);
+    atomicAdd(&s[33], sl2);
+    atomicAdd(&s[35], emp);
+    atomicAdd(&s[36], spread);
+    atomicAdd(&s[37], cnt);
+    // max via integer atomic on the bit pattern (non-negative doubles order as integers)
+    atomicMax(reinterpret_cast<unsigned long long *>(&s[34]), __double_as_longlong(mx));
+    __syncthreads();
+    for (int i = threadIdx.x; i < 38; i += blockDim.x) {
+        if (i == 34) atomicMax(reinterpret_cast<unsigned long long *>(&acc[34]), __double_as_longlong(s[34]));
+        else atomicAdd(&acc[i], s[i]);
+    }
+}
+
+// ---------------------------------------------------------------- MLP
+// Parameter layout (floats): W1[H][F] b1[H] W2[H][H] b2[H] W3[K][H] b3[K];
+// a selector blob is [mean[F] scale[F] params...]: x_norm = (x - mean) * scale.
+constexpr int F = SPG_SELECT_FEATURES;
+constexpr int H = SPG_SELECT_HIDDEN;
+
+__host__ __device__ constexpr uint64_t n_params(int K) {
+    return (uint64_t)H * F + H + (uint64_t)H * H + H + (uint64_t)K * H + K;
+}
+
+// layer: out[b][j] = act(sum_i W[j][i] in[b][i] + bias[j]); one thread per (b, j)
+__global__ void mlp_dense(const float *__restrict__ W, const float *__restrict__ bias, const float *__restrict__ in,
+                          int n_in, int n_out, uint32_t B, int relu, float *__restrict__ out) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)B * n_out) return;
+    const uint32_t b = (uint32_t)(t / n_out);
+    const int j = (int)(t % n_out);
+    const float *w = W + (uint64_t)j * n_in;
+    const float *x = in + (uint64_t)b * n_in;
+    float s = bias[j];
+    for (int i = 0; i < n_in; ++i) s = fmaf(w[i], x[i], s);
+    out[t] = relu ? fmaxf(s, 0.0f) : s;
+}
+
+__global__ void mlp_normalize(const float *__restrict__ X, const float *__restrict__ mean,
+                              const float *__restrict__ scale, uint32_t B, float *__restrict__ out) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)B * F) return;
+    const int i = (int)(t % F);
+    out[t] = (X[t] - mean[i]) * scale[i];
+}
+
+// dIn[b][i] = sum_j dOut[b][j] * W[j][i], masked by the ReLU of `act_in` when given
+__global__ void mlp_back_input(const float *__restrict__ W, const float *__restrict__ dout, int n_in, int n_out,
+                               uint32_t B, const float *__restrict__ act_in, float *__restrict__ din) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)B * n_in) return;
+    const uint32_t b = (uint32_t)(t / n_in);
+    const int i = (int)(t % n_in);
+    float s = 0.0f;
+    for (int j = 0; j < n_out; ++j) s = fmaf(dout[(uint64_t)b * n_out + j], W[(uint64_t)j * n_in + i], s);
+    if (act_in && act_in[t] <= 0.0f) s = 0.0f;
+    din[t] = s;
+}
+
+// dW[j][i] = sum_b dOut[b][j] in[b][i]; dbias[j] = sum_b dOut[b][j]; one thread per weight
+__global__ void mlp_back_weights(const float *__restrict__ dout, const float *__restrict__ in, int n_in, int n_out,
+                                 uint32_t B, float *__restrict__ dW, float *__restrict__ db) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nw = (uint64_t)n_out * n_in;
+    if (t < nw) {
+        const int j = (int)(t / n_in), i = (int)(t % n_in);
+        float s = 0.0f;
+        for (uint32_t b = 0; b < B; ++b) s = fmaf(dout[(uint64_t)b * n_out + j], in[(uint64_t)b * n_in + i], s);
+        dW[t] = s;
+    } else if (t < nw + n_out) {
+        const int j = (int)(t - nw);
+        float s = 0.0f;
+        for (uint32_t b = 0; b < B; ++b) s += dout[(uint64_t)b * n_out + j];
+        db[j] = s;
+    }
+}
+
+// loss = mean over (b, k) of (pred - target)^2; dpred = 2 (pred - target) / (B K)
+__global__ void mlp_mse_grad(const float *__restrict__ pred, const float *__restrict__ target, uint64_t n,
+                             float *__restrict__ dpred, float *__restrict__ loss_acc) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (t < n) {
+        const float d = pred[t] - target[t];
+        dpred[t] = 2.0f * d / (float)n;
+        l = d * d / (float)n;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0 && loss_acc) atomicAdd(loss_acc, l);
+}
+
+__global__ void mlp_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                         float *__restrict__ v, uint64_t n, float lr, float b1, float b2, float eps, float c1,
+                         float c2) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float gt = g[t];
+    const float mt = b1 * m[t] + (1.0f - b1) * gt;
+    const float vt = b2 * v[t] + (1.0f - b2) * gt * gt;
+    m[t] = mt;
+    v[t] = vt;
+    w[t] -= lr * (mt / c1) / (sqrtf(vt / c2) + eps);
+}
+
+__global__ void mlp_argmin(const float *__restrict__ pred, uint32_t B, int K, int *__restrict__ best) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    int bi = 0;
+    float bv = pred[(uint64_t)b * K];
+    for (int k = 1; k < K; ++k) {
+        const float v = pred[(uint64_t)b * K + k];
+        if (v < bv) {
+            bv = v;
+            bi = k;
+        }
+    }
+    best[b] = bi;
+}
+
+struct Layers {
+    const float *W1, *b1, *W2, *b2, *W3, *b3;
+};
+
+Layers layers(const float *P, int K) {
+    Layers L;
+    L.W1 = P;
+    L.b1 = L.W1 + (uint64_t)H * F;
+    L.W2 = L.b1 + H;
+    L.b2 = L.W2 + (uint64_t)H * H;
+    L.W3 = L.b2 + H;
+    L.b3 = L.W3 + (uint64_t)K * H;
+    return L;
+}
+
+// act workspace per sample: h1[H], h2[H]
+int forward(const float *P, int K, const float *Xn, uint32_t B, float *act, float *out, cudaStream_t s) {
+    const Layers L = layers(P, K);
+    float *h1 = act, *h2 = act + (uint64_t)B * H;
+    mlp_dense<<<grid_for((uint64_t)B * H, 256), 256, 0, s>>>(L.W1, L.b1, Xn, F, H, B, 1, h1);
+    mlp_dense<<<grid_for((uint64_t)B * H, 256), 256, 0, s>>>(L.W2, L.b2, h1, H, H, B, 1, h2);
+    mlp_dense<<<grid_for((uint64_t)B * K, 256), 256, 0, s>>>(L.W3, L.b3, h2, H, K, B, 0, out);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+int spmv_features(Ctx *c, Csr *A, float *f) {
+    cudaStream_t s = c->stream;
+    DevBuf acc;
+    SPG_TRY(acc.alloc(38 * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(acc.ptr, 0, 38 * sizeof(double), s));
+    if (A->n_rows) {
+        feat_rows<<<grid_for(A->n_rows, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(A->d_off(), A->d_cols(), A->n_rows,
+                                                                                    A->n_cols ? A->n_cols : 1,
+                                                                                    acc.as<double>());
+        SPG_LAUNCH_CHECK();
+    }
+    double h[38];
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, acc.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    const double n = (double)(A->n_rows ? A->n_rows : 1);
+    for (int i = 0; i < 32; ++i) f[i] = (float)(h[i] / n);
+    const double mean = h[32] / n;
+    const double var = std::max(0.0, h[33] / n - mean * mean);
+    f[32] = (float)(std::log2((double)A->n_rows + 1.0) / 32.0);
+    f[33] = (float)(std::log2((double)A->n_cols + 1.0) / 32.0);
+    f[34] = (float)(std::log2((double)A->nnz + 1.0) / 40.0);
+    f[35] = (float)(std::log2(mean + 1.0) / 16.0);
+    f[36] = (float)(std::log2(std::sqrt(var) + 1.0) / 16.0);
+    f[37] = (float)(std::log2(h[34] + 1.0) / 32.0);
+    f[38] = (float)(h[35] / n);
+    f[39] = (float)(h[37] > 0 ? h[36] / h[37] : 0.0);
+    return SPG_OK;
+}
+
+int spmv_autotune(Ctx *c, Csr *A, int reps, float *times_ms, int *best) {
+    cudaStream_t s = c->stream;
+    if (reps < 1) reps = 1;
+    if (c->xbuf.bytes < A->n_cols * sizeof(double)) SPG_TRY(c->xbuf.alloc(A->n_cols * sizeof(double), s));
+    if (c->ybuf.bytes < A->n_rows * sizeof(double)) SPG_TRY(c->ybuf.alloc(A->n_rows * sizeof(double), s));
+    // x = 1.0 everywhere (timing does not depend on the values)
+    if (A->n_cols) {
+        std::vector<double> ones(std::min<uint64_t>(A->n_cols, 1u << 20), 1.0);
+        for (uint64_t o = 0; o < A->n_cols; o += ones.size()) {
+            const uint64_t m = std::min<uint64_t>(ones.size(), A->n_cols - o);
+            SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.as<double>() + o, ones.data(), m * sizeof(double),
+                                         cudaMemcpyHostToDevice, s));
+            SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        }
+    }
+    cudaEvent_t e0, e1;
+    SPG_CUDA_TRY(cudaEventCreate(&e0));
+    SPG_CUDA_TRY(cudaEventCreate(&e1));
+    int bi = 0;
+    float bt = 0.0f;
+    int rc = SPG_OK;
+    for (int v = 0; v < SPG_SPMV_N_VARIANTS && rc == SPG_OK; ++v) {
+        rc = spmv_launch(c, A, c->xbuf.as<double>(), c->ybuf.as<double>(), v, s);  // builds plans, warms up
+        if (rc != SPG_OK) break;
+        std::vector<float> ts(reps);
+        for (int r = 0; r < reps && rc == SPG_OK; ++r) {
+            cudaEventRecord(e0, s);
+            rc = spmv_launch(c, A, c->xbuf.as<double>(), c->ybuf.as<double>(), v, s);
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) rc = set_error(SPG_ERR_CUDA, "autotune: event sync failed");
+            cudaEventElapsedTime(&ts[r], e0, e1);
+        }
+        std::sort(ts.begin(), ts.end());
+        const float t = ts[ts.size() / 2];
+        if (times_ms) times_ms[v] = t;
+        if (v == 0 || t < bt) {
+            bt = t;
+            bi = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SPG_TRY(rc);
+    SPG_TRY(c->take_status());
+    if (best) *best = bi;
+    return SPG_OK;
+}
+
+int selector_predict_dev(Ctx *c, const float *d_x, uint32_t B, float *d_out, cudaStream_t s) {
+    const int K = c->model_k;
+    const float *mean = c->model.as<float>();
+    const float *scale = mean + F;
+    const float *P = scale + F;
+    DevBuf xn, act;
+    SPG_TRY(xn.alloc((uint64_t)B * F * sizeof(float), s));
+    SPG_TRY(act.alloc((uint64_t)B * 2 * H * sizeof(float), s));
+    mlp_normalize<<<grid_for((uint64_t)B * F, 256), 256, 0, s>>>(d_x, mean, scale, B, xn.as<float>());
+    SPG_LAUNCH_CHECK();
+    return forward(P, K, xn.as<float>(), B, act.as<float>(), d_out, s);
+}
+
+int spmv_resolve_auto(Ctx *c, Csr *A, int *variant) {
+    if (A->selected_spmv >= 0) {
+        *variant = A->selected_spmv;
+        return SPG_OK;
+    }
+    int v = SPG_SPMV_ADAPTIVE;
+    if (c->spmv_policy == SPG_POLICY_FIXED) {
+        v = SPG_SPMV_ADAPTIVE16;
+    } else if (c->spmv_policy == SPG_POLICY_SELECTOR && c->model_k > 0) {
+        float f[F];
+        SPG_TRY(spmv_features(c, A, f));
+        cudaStream_t s = c->stream;
+        DevBuf df, dout, db;
+        SPG_TRY(df.alloc(F * sizeof(float), s));
+        SPG_TRY(dout.alloc(c->model_k * sizeof(float), s));
+        SPG_TRY(db.alloc(sizeof(int), s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(df.ptr, f, sizeof(f), cudaMemcpyHostToDevice, s));
+        SPG_TRY(selector_predict_dev(c, df.as<float>(), 1, dout.as<float>(), s));
+        mlp_argmin<<<1, 32, 0, s>>>(dout.as<float>(), 1, c->model_k, db.as<int>());
+        SPG_LAUNCH_CHECK();
+        SPG_CUDA_TRY(cudaMemcpyAsync(&v, db.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (v < 0 || v >= SPG_SPMV_N_VARIANTS) v = SPG_SPMV_ADAPTIVE;
+    } else {
+        SPG_TRY(spmv_autotune(c, A, 5, nullptr, &v));
+    }
+    A->selected_spmv = v;
+    *variant = v;
+    return SPG_OK;
+}
+
+// The trained selector shipped beside the library (spg_selector.bin in the
+// directory of libspg.so) or named by SPG_SELECTOR_MODEL; absent or malformed
+// files leave the context on the autotuner.
+int selector_load_default(Ctx *c) {
+    std::string path;
+    if (const char *env = getenv("SPG_SELECTOR_MODEL")) {
+        path = env;
+    } else {
+        Dl_info info;
+        if (dladdr(reinterpret_cast<void *>(&selector_load_default), &info) && info.dli_fname) {
+            path = info.dli_fname;
+            const size_t slash = path.rfind('/');
+            path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/spg_selector.bin";
+        }
+    }
+    if (path.empty()) return SPG_OK;
+    FILE *fp = fopen(path.c_str(), "rb");
+    if (!fp) return SPG_OK;
+    std::vector<float> blob;
+    float buf[4096];
+    size_t got;
+    while ((got = fread(buf, sizeof(float), 4096, fp)) > 0) blob.insert(blob.end(), buf, buf + got);
+    fclose(fp);
+    const long long base = 2LL * F + (long long)n_params(0);
+    const long long per_k = H + 1;
+    const long long rest = (long long)blob.size() - base;
+    if (rest <= 0 || rest % per_k) return SPG_OK;
+    const int K = (int)(rest / per_k);
+    if (K < 1 || K > SPG_SPMV_N_VARIANTS) return SPG_OK;
+    if (c->model.alloc(blob.size() * sizeof(float), c->stream) != SPG_OK) return SPG_OK;
+    if (cudaMemcpyAsync(c->model.ptr, blob.data(), blob.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        c->model.release();
+        return SPG_OK;
+    }
+    c->model_k = K;
+    return SPG_OK;
+}
+
+}  // namespace spg
+
+using namespace spg;
+
+extern "C" {
+
+int spg_spmv_features(spg_ctx *c, const spg_csr *A, float *features) {
+    if (!c || !A || !features) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_features: null argument");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return spmv_features(c, const_cast<spg_csr *>(A), features);
+}
+
+int spg_spmv_autotune(spg_ctx *c, const spg_csr *A, int reps, float *times_ms, int *best) {
+    if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_autotune: null argument");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return spmv_autotune(c, const_cast<spg_csr *>(A), reps, times_ms, best);
+}
+
+int spg_set_spmv_policy(spg_ctx *c, int policy) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_set_spmv_policy: null context");
+    if (policy < SPG_POLICY_SELECTOR || policy > SPG_POLICY_FIXED)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_set_spmv_policy: unknown policy %d", policy);
+    c->spmv_policy = policy;
+    return SPG_OK;
+}
+
+int spg_selector_load(spg_ctx *c, const float *blob, uint64_t n_floats, int n_outputs) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_selector_load: null context");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!blob) {
+        c->model.release();
+        c->model_k = 0;
+        return SPG_OK;
+    }
+    if (n_outputs < 1 || n_outputs > SPG_SPMV_N_VARIANTS || n_floats != 2 * F + n_params(n_outputs))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_selector_load: blob of %llu floats does not fit K=%d",
+                         (unsigned long long)n_floats, n_outputs);
+    SPG_TRY(c->model.alloc(n_floats * sizeof(float), c->stream));
+    SPG_CUDA_TRY(cudaMemcpyAsync(c->model.ptr, blob, n_floats * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    SPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->model_k = n_outputs;
+    return SPG_OK;
+}
+
+uint64_t spg_mlp_param_count(int n_outputs) { return n_params(n_outputs); }
+
+int spg_selector_predict(spg_ctx *c, const float *d_features, uint32_t B, float *d_out, void *stream) {
+    if (!c || (B && (!d_features || !d_out))) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_selector_predict: null");
+    if (c->model_k <= 0) return set_error(SPG_ERR_LOGIC, "spg_selector_predict: no selector loaded");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!B) return SPG_OK;
+    return selector_predict_dev(c, d_features, B, d_out, pick_stream(c, stream));
+}
+
+int spg_mlp_forward(spg_ctx *c, const float *d_params, int n_outputs, const float *d_x, uint32_t B, float *d_act,
+                    float *d_out, void *stream) {
+    if (!c || !d_params || (B && (!d_x || !d_act || !d_out)))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_mlp_forward: null argument");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!B) return SPG_OK;
+    return forward(d_params, n_outputs, d_x, B, d_act, d_out, pick_stream(c, stream));
+}
+
+int spg_mlp_backward(spg_ctx *c, const float *d_params, int n_outputs, const float *d_x, uint32_t B,
+                     const float *d_act, const float *d_dout, float *d_grad, void *stream) {
+    if (!c || !d_params || !d_grad || (B && (!d_x || !d_act || !d_dout)))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_mlp_backward: null argument");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = pick_stream(c, stream);
+    const int K = n_outputs;
+    const Layers L = layers(d_params, K);
+    float *gW1 = d_grad, *gb1 = gW1 + (uint64_t)H * F, *gW2 = gb1 + H, *gb2 = gW2 + (uint64_t)H * H,
+          *gW3 = gb2 + H, *gb3 = gW3 + (uint64_t)K * H;
+    const float *h1 = d_act, *h2 = d_act + (uint64_t)B * H;
+    DevBuf d2, d1;
+    SPG_TRY(d2.alloc((uint64_t)(B ? B : 1) * H * sizeof(float), s));
+    SPG_TRY(d1.alloc((uint64_t)(B ? B : 1) * H * sizeof(float), s));
+    mlp_back_weights<<<grid_for((uint64_t)K * H + K, 256), 256, 0, s>>>(d_dout, h2, H, K, B, gW3, gb3);
+    mlp_back_input<<<grid_for((uint64_t)B * H, 256), 256, 0, s>>>(L.W3, d_dout, H, K, B, h2, d2.as<float>());
+    mlp_back_weights<<<grid_for((uint64_t)H * H + H, 256), 256, 0, s>>>(d2.as<float>(), h1, H, H, B, gW2, gb2);
+    mlp_back_input<<<grid_for((uint64_t)B * H, 256), 256, 0, s>>>(L.W2, d2.as<float>(), H, H, B, h1, d1.as<float>());
+    mlp_back_weights<<<grid_for((uint64_t)H * F + H, 256), 256, 0, s>>>(d1.as<float>(), d_x, F, H, B, gW1, gb1);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int spg_mlp_mse(spg_ctx *c, const float *d_pred, const float *d_target, uint64_t n, float *d_dpred, float *d_loss,
+                void *stream) {
+    if (!c || (n && (!d_pred || !d_target || !d_dpred)))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_mlp_mse: null argument");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!n) return SPG_OK;
+    mlp_mse_grad<<<grid_for(n, 256), 256, 0, pick_stream(c, stream)>>>(d_pred, d_target, n, d_dpred, d_loss);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int spg_mlp_adam(spg_ctx *c, float *d_params, const float *d_grad, float *d_m, float *d_v, uint64_t n, float lr,
+                 float beta1, float beta2, float eps, uint32_t step, void *stream) {
+    if (!c || !d_params || !d_grad || !d_m || !d_v || step == 0)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_mlp_adam: bad argument");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    const float c1 = 1.0f - std::pow(beta1, (float)step), c2 = 1.0f - std::pow(beta2, (float)step);
+    mlp_adam<<<grid_for(n, 256), 256, 0, pick_stream(c, stream)>>>(d_params, d_grad, d_m, d_v, n, lr, beta1, beta2,
+                                                                    eps, c1, c2);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int spg_mlp_argmin(spg_ctx *c, const float *d_pred, uint32_t B, int n_outputs, int *d_best, void *stream) {
+    if (!c || (B && (!d_pred || !d_best))) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_mlp_argmin: null");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!B) return SPG_OK;
+    mlp_argmin<<<grid_for(B, 256), 256, 0, pick_stream(c, stream)>>>(d_pred, B, n_outputs, d_best);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+}  // extern "C"
