@@ -193,8 +193,7 @@ def run_ours(args):
     dom = int(np.argmax(per_sel))
     dm = mats[dom]
     achieved = dm["bytes"] / (per_sel[dom] * 1e-3) / 1e9
-    launches_per = {sg.SPMV_MERGE: 2}
-    gpu_launches = args.steps * sum(launches_per.get(m["selected"], 1) for m in mats)
+    gpu_launches = args.steps * sum(m["A"].spmv_launches(m["selected"]) for m in mats)
 
     cpu = cpu_baseline(host, [m["x"] for m in mats], total_bytes)
     line = {

@@ -141,6 +141,9 @@ int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
                   uint64_t x_len, double *y, uint64_t y_len, int variant);
 /* The variant SPG_SPMV_AUTO resolves to for A. */
 int spg_spmv_selected(spg_ctx *ctx, const spg_csr *A, int *variant);
+/* Number of kernel launches one spg_spmv of A with `variant` issues (plans
+ * are built beforehand and not counted). */
+int spg_spmv_launches(spg_ctx *ctx, const spg_csr *A, int variant, int *n_launches);
 
 /* ---- SpMV variant choice ----------------------------------------------------
  * No Spira counterpart: Spira has a single SpMV code path per type
@@ -181,6 +184,25 @@ int spg_mlp_mse(spg_ctx *ctx, const float *d_pred, const float *d_target, uint64
 int spg_mlp_adam(spg_ctx *ctx, float *d_params, const float *d_grad, float *d_m, float *d_v, uint64_t n,
                  float lr, float beta1, float beta2, float eps, uint32_t step, void *stream);
 int spg_mlp_argmin(spg_ctx *ctx, const float *d_pred, uint32_t B, int n_outputs, int *d_best, void *stream);
+
+/* ---- batched multi-RHS SpMV ------------------------------------------------
+ * No Spira counterpart as a call: each item is Spira's SpMV
+ * (serial/spmv.hpp:141-186) applied to the k columns of a row-major X
+ * (n_cols x k, X[c * k + j]) into Y (n_rows x k). spg_batch_create builds the
+ * work list of (matrix, row tile) items and captures one persistent launch in
+ * a CUDA graph; config < 0 autotunes the tile size and CTAs per SM on the
+ * batch (runs it a few times), config 0..7 picks one directly. k must be a
+ * power of two <= 32. Matrices and vectors must outlive the batch and keep
+ * their device arrays (no lock in between). */
+typedef struct spg_batch spg_batch;
+int spg_batch_create(spg_ctx *ctx, uint32_t n, const spg_csr *const *mats, const double *const *d_X,
+                     double *const *d_Y, const uint32_t *k, int config, spg_batch **out);
+int spg_batch_config(const spg_batch *batch, int *config, uint32_t *n_items);
+/* Replays the graph (one persistent kernel) on `stream`. */
+int spg_batch_run(spg_ctx *ctx, spg_batch *batch, void *stream);
+/* The comparison path: one plain SpMV launch per matrix per right-hand side. */
+int spg_batch_run_plain(spg_ctx *ctx, spg_batch *batch, void *stream);
+int spg_batch_destroy(spg_batch *batch);
 
 /* ---- transpose / SpGEMM ----------------------------------------------------
  * spg_transpose: AT <- A^T (AT is reshaped to n_cols x n_rows, capacity ==

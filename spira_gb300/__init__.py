@@ -101,6 +101,7 @@ _SIGS = [
     ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
     ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
     ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
+    ("spg_spmv_launches", _I, [_P, _P, _I, C.POINTER(_I)]),
     ("spg_set_spmv_policy", _I, [_P, _I]),
     ("spg_spmv_features", _I, [_P, _P, _P]),
     ("spg_spmv_autotune", _I, [_P, _P, _I, _P, C.POINTER(_I)]),
@@ -112,6 +113,11 @@ _SIGS = [
     ("spg_mlp_mse", _I, [_P, _P, _P, _U64, _P, _P, _P]),
     ("spg_mlp_adam", _I, [_P, _P, _P, _P, _P, _U64, C.c_float, C.c_float, C.c_float, C.c_float, _U32, _P]),
     ("spg_mlp_argmin", _I, [_P, _P, _U32, _I, _P, _P]),
+    ("spg_batch_create", _I, [_P, _U32, _P, _P, _P, _P, _I, C.POINTER(_P)]),
+    ("spg_batch_config", _I, [_P, C.POINTER(_I), C.POINTER(_U32)]),
+    ("spg_batch_run", _I, [_P, _P, _P]),
+    ("spg_batch_run_plain", _I, [_P, _P, _P]),
+    ("spg_batch_destroy", _I, [_P]),
     ("spg_transpose", _I, [_P, _P, _P]),
     ("spg_spgemm", _I, [_P, _P, _P, _P]),
     # spg_gen.h
@@ -299,6 +305,11 @@ class Csr:
         _check(lib().spg_spmv_selected(self.ctx.h, self.h, C.byref(v)))
         return v.value
 
+    def spmv_launches(self, variant: int = SPMV_AUTO) -> int:
+        n = C.c_int()
+        _check(lib().spg_spmv_launches(self.ctx.h, self.h, variant, C.byref(n)))
+        return n.value
+
     def features(self) -> np.ndarray:
         f = np.empty(N_FEATURES, np.float32)
         _check(lib().spg_spmv_features(self.ctx.h, self.h, _ptr(f)))
@@ -345,6 +356,44 @@ def gen_family(ctx: Context, family: int, n_rows: int, p: int, ls: float = 0.0, 
     _check(lib().spg_gen_family(ctx.h, family, n_rows, p, ls, _ptr(d_cdf), seed, _ptr(d_rows), _ptr(d_cols),
                                 _ptr(d_vals), C.byref(m)))
     return m.value
+
+
+class Batch:
+    """Persistent multi-RHS batch (spg_batch). mats: Csr list; X, Y: device
+    buffers (torch tensors / pointers), row-major n x k; k: powers of two."""
+
+    def __init__(self, ctx: Context, mats, Xs, Ys, ks, config: int = -1):
+        n = len(mats)
+        self.ctx, self._keep = ctx, (mats, Xs, Ys)
+        ph = (C.c_void_p * n)(*[m.h.value for m in mats])
+        px = (C.c_void_p * n)(*[_ptr(x) for x in Xs])
+        py = (C.c_void_p * n)(*[_ptr(y) for y in Ys])
+        kk = (C.c_uint32 * n)(*ks)
+        h = _P()
+        _check(lib().spg_batch_create(ctx.h, n, ph, px, py, kk, config, C.byref(h)))
+        self.h = h
+
+    def config(self):
+        c, n = C.c_int(), C.c_uint32()
+        _check(lib().spg_batch_config(self.h, C.byref(c), C.byref(n)))
+        return c.value, n.value
+
+    def run(self, stream=None):
+        _check(lib().spg_batch_run(self.ctx.h, self.h, stream))
+
+    def run_plain(self, stream=None):
+        _check(lib().spg_batch_run_plain(self.ctx.h, self.h, stream))
+
+    def close(self):
+        if self.h:
+            lib().spg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Mlp:

@@ -381,6 +381,36 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
     return c->take_status();
 }
 
+int spg_spmv_launches(spg_ctx *c, const spg_csr *Ac, int variant, int *n) {
+    if (!c || !Ac || !n) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_launches: null argument");
+    if (!Ac->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    spg_csr *A = const_cast<spg_csr *>(Ac);
+    if (variant == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &variant));
+    if (variant < 0 || variant >= SPG_SPMV_N_VARIANTS)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_launches: unknown variant %d", variant);
+    if (A->n_rows == 0) {
+        *n = 0;
+        return SPG_OK;
+    }
+    switch (variant) {
+        case SPG_SPMV_MERGE:
+            *n = 2;
+            break;
+        case SPG_SPMV_ADAPTIVE:
+        case SPG_SPMV_ADAPTIVE16:
+            SPG_TRY(build_adaptive_plan(c, A, variant == SPG_SPMV_ADAPTIVE ? 32 : 16, c->stream));
+            *n = (A->plan_adaptive.n_items ? 2 : 0) + (A->plan_adaptive.count1 ? 1 : 0);
+            break;
+        case SPG_SPMV_STREAM:
+            *n = 1;
+            break;
+        default:
+            *n = 1;
+    }
+    return SPG_OK;
+}
+
 int spg_spmv_selected(spg_ctx *c, const spg_csr *Ac, int *variant) {
     if (!c || !Ac || !variant) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_selected: null argument");
     if (!Ac->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");

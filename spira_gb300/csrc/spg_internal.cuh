@@ -203,6 +203,7 @@ int selector_load_default(Ctx *c);
 // SPG_SPMV_ADAPTIVE with `items` (8 or 16) nonzeros per thread chunk
 // (spg_spmv_adaptive.cu); builds and caches its plan on first use.
 int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int items, cudaStream_t s);
+int build_adaptive_plan(Ctx *c, Csr *A, int items, cudaStream_t s);
 
 }  // namespace spg
 
