@@ -101,11 +101,22 @@ struct Batch {
     int ctas_per_sm = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    ~Batch() {
+    void release() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        d_mats.release();
+        d_items.release();
+        d_counter.release();
     }
+    ~Batch() { release(); }
 };
+
+void batch_orphan(Batch *b) {
+    b->release();
+    b->ctx = nullptr;
+}
 
 static int batch_build_items(Batch *B, int tile_nnzk, cudaStream_t s) {
     std::vector<BatchItem> items;
@@ -257,6 +268,7 @@ int spg_batch_create(spg_ctx *c, uint32_t n, const spg_csr *const *mats, const d
         delete B;
         return rc;
     }
+    c->live_batches.push_back(B);
     *out = B;
     return SPG_OK;
 }
@@ -273,6 +285,7 @@ int spg_batch_config(const spg_batch *B, int *config, uint32_t *n_items) {
 
 int spg_batch_run(spg_ctx *c, spg_batch *B, void *stream) {
     if (!c || !B) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_batch_run: null argument");
+    if (!B->ctx) return set_error(SPG_ERR_LOGIC, "the batch's context was destroyed");
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     SPG_CUDA_TRY(cudaGraphLaunch(B->exec, pick_stream(c, stream)));
     return SPG_OK;
@@ -280,6 +293,7 @@ int spg_batch_run(spg_ctx *c, spg_batch *B, void *stream) {
 
 int spg_batch_run_plain(spg_ctx *c, spg_batch *B, void *stream) {
     if (!c || !B) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_batch_run_plain: null argument");
+    if (!B->ctx) return set_error(SPG_ERR_LOGIC, "the batch's context was destroyed");
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = pick_stream(c, stream);
     for (const BatchMat &M : B->host_mats) {
@@ -294,7 +308,11 @@ int spg_batch_run_plain(spg_ctx *c, spg_batch *B, void *stream) {
 
 int spg_batch_destroy(spg_batch *B) {
     if (!B) return SPG_OK;
-    cudaSetDevice(B->ctx->device);
+    if (Ctx *c = B->ctx) {
+        cudaSetDevice(c->device);
+        auto &v = c->live_batches;
+        v.erase(std::remove(v.begin(), v.end(), static_cast<Batch *>(B)), v.end());
+    }
     delete B;
     return SPG_OK;
 }

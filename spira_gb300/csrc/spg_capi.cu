@@ -1,6 +1,7 @@
 // spg_capi.cu — the extern "C" surface of libspg.so: contexts, CSR handles,
 // host<->device transfer, load_csr validation, point lookup and SpMV entry
 // points. Lock lives in spg_lock.cu; kernels in spg_spmv.cu.
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -130,6 +131,11 @@ int spg_ctx_destroy(spg_ctx *c) {
     if (!c) return SPG_OK;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    for (Batch *b : c->live_batches) batch_orphan(b);
+    c->live_batches.clear();
+    for (Csr *A : c->live_csrs) A->orphan();
+    c->live_csrs.clear();
+    c->model.release();
     c->xbuf.release();
     c->ybuf.release();
     cudaStreamSynchronize(c->stream);
@@ -163,14 +169,19 @@ int spg_csr_create(spg_ctx *c, uint64_t n_rows, uint64_t n_cols, spg_csr **out) 
     A->ctx = c;
     A->n_rows = n_rows;
     A->n_cols = n_cols;
+    c->live_csrs.push_back(A);
     *out = A;
     return SPG_OK;
 }
 
 int spg_csr_destroy(spg_csr *A) {
     if (!A) return SPG_OK;
-    cudaSetDevice(A->ctx->device);
-    delete A;  // DevBufs free stream-ordered
+    if (Ctx *c = A->ctx) {  // still owned: unregister, free on the context's stream
+        cudaSetDevice(c->device);
+        auto &v = c->live_csrs;
+        v.erase(std::remove(v.begin(), v.end(), static_cast<Csr *>(A)), v.end());
+    }
+    delete A;
     return SPG_OK;
 }
 
@@ -212,6 +223,7 @@ int spg_csr_download(spg_ctx *c, const spg_csr *A, uint64_t *offsets, uint32_t *
 int spg_csr_load(spg_ctx *c, spg_csr *A, const uint64_t *offsets, const uint32_t *cols,
                  const double *vals, uint64_t nnz) {
     if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_load: null handle");
+    SPG_CHECK_LIVE(A);
     // Validation in the order of matrix::load_csr (matrix.hpp:524-575).
     if (!offsets) return set_error(SPG_ERR_INVALID_ARGUMENT, "spira::matrix::load_csr: CSR offsets array is null");
     if (offsets[0] != 0)
@@ -265,6 +277,8 @@ int spg_csr_load(spg_ctx *c, spg_csr *A, const uint64_t *offsets, const uint32_t
 
 int spg_csr_copy(spg_ctx *c, const spg_csr *src, spg_csr *dst) {
     if (!c || !src || !dst) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_csr_copy: null handle");
+    SPG_CHECK_LIVE(src);
+    SPG_CHECK_LIVE(dst);
     if (src == dst) return SPG_OK;
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
@@ -341,6 +355,7 @@ int spg_csr_row_range(spg_ctx *c, const spg_csr *A, uint64_t row, uint64_t *begi
 
 int spg_spmv(spg_ctx *c, const spg_csr *Ac, const double *d_x, double *d_y, int variant, void *stream) {
     if (!c || !Ac) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv: null handle");
+    SPG_CHECK_LIVE(Ac);
     spg_csr *A = const_cast<spg_csr *>(Ac);  // plans are cached on the handle
     if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
     if ((A->n_cols && !d_x) || (A->n_rows && !d_y))
@@ -355,6 +370,7 @@ int spg_spmv(spg_ctx *c, const spg_csr *Ac, const double *d_x, double *d_y, int 
 int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,
                   int variant) {
     if (!c || !Ac) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: null handle");
+    SPG_CHECK_LIVE(Ac);
     // Checks in the order of serial/spmv.hpp:150-158.
     if (x_len != Ac->n_cols)
         return set_error(SPG_ERR_INVALID_ARGUMENT,

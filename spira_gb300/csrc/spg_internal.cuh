@@ -88,10 +88,19 @@ struct SpmvPlan {
     DevBuf extra0, extra1, extra2;
 };
 
+struct Csr;
+struct Batch;
+void batch_orphan(Batch *b);  // spg_batch.cu
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaMemPool_t pool = nullptr;
+    // Live handles created on this context. Destroying the context releases
+    // their device memory and orphans them; an orphaned handle can still be
+    // destroyed, every other call on it returns SPG_ERR_LOGIC.
+    std::vector<Csr *> live_csrs;
+    std::vector<Batch *> live_batches;
     int n_sms = 0;
     size_t l2_bytes = 0;
     // Status word written by kernels whose bounded waits ran out; 0 = ok.
@@ -145,7 +154,24 @@ struct Csr {
     const uint64_t *d_off() const { return off.as<uint64_t>(); }
     const uint32_t *d_cols() const { return cols.as<uint32_t>(); }
     const double *d_vals() const { return vals.as<double>(); }
+    // Frees the device arrays while the owning context's stream still exists.
+    void orphan() {
+        invalidate_derived();
+        off.release();
+        cols.release();
+        vals.release();
+        built = false;
+        nnz = capacity = 0;
+        ctx = nullptr;
+    }
 };
+
+// Checks that a handle still belongs to a live context.
+#define SPG_CHECK_LIVE(A)                                                                              \
+    do {                                                                                               \
+        if ((A)->ctx == nullptr)                                                                       \
+            return ::spg::set_error(SPG_ERR_LOGIC, "the matrix's context was destroyed");             \
+    } while (0)
 
 inline cudaStream_t pick_stream(Ctx *c, void *s) {
     return s ? static_cast<cudaStream_t>(s) : c->stream;

@@ -396,6 +396,7 @@ extern "C" {
 int spg_lock_device(spg_ctx *c, spg_csr *A, const uint32_t *d_rows, const uint32_t *d_cols, const double *d_vals,
                     uint64_t n_staged) {
     if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock_device: null handle");
+    SPG_CHECK_LIVE(A);
     if (n_staged && (!d_rows || !d_cols || !d_vals))
         return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock_device: null staging array");
     SPG_CUDA_TRY(cudaSetDevice(c->device));
@@ -405,6 +406,7 @@ int spg_lock_device(spg_ctx *c, spg_csr *A, const uint32_t *d_rows, const uint32
 int spg_lock(spg_ctx *c, spg_csr *A, const uint32_t *rows, const uint32_t *cols, const double *vals,
              uint64_t n_staged) {
     if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock: null handle");
+    SPG_CHECK_LIVE(A);
     if (n_staged && (!rows || !cols || !vals))
         return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_lock: null staging array");
     SPG_CUDA_TRY(cudaSetDevice(c->device));

@@ -205,6 +205,9 @@ using namespace spg;
 
 extern "C" int spg_spgemm(spg_ctx *c, const spg_csr *A, const spg_csr *B, spg_csr *Cm) {
     if (!c || !A || !B || !Cm) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm: null handle");
+    SPG_CHECK_LIVE(A);
+    SPG_CHECK_LIVE(B);
+    SPG_CHECK_LIVE(Cm);
     // Checks in the order of serial/spgemm.hpp:14-21.
     if (A->n_cols != B->n_rows) return set_error(SPG_ERR_INVALID_ARGUMENT, "A.cols must equal B.rows");
     if (!A->built) return set_error(SPG_ERR_LOGIC, "spgemm: A must be locked");

@@ -105,6 +105,8 @@ using namespace spg;
 
 extern "C" int spg_transpose(spg_ctx *c, const spg_csr *A, spg_csr *T) {
     if (!c || !A || !T) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_transpose: null handle");
+    SPG_CHECK_LIVE(A);
+    SPG_CHECK_LIVE(T);
     if (!A->built) return set_error(SPG_ERR_LOGIC, "transpose: matrix must be locked");
     if (A == T) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_transpose: output aliases input");
     SPG_CUDA_TRY(cudaSetDevice(c->device));

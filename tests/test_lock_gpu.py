@@ -139,6 +139,22 @@ def test_relock_after_load_with_explicit_zeros(ctx):
     np.testing.assert_array_equal(got.vals, [7.0, 8.0, 0.0, 5.0])
 
 
+def test_context_destroyed_before_its_matrices():
+    """Destroying a context frees its matrices' device memory; the handles
+    stay safe to use (LogicError) and to destroy."""
+    c2 = sg.Context(0)
+    A = sg.Csr(c2, 10, 10)
+    A.lock(np.array([1], np.uint32), np.array([2], np.uint32), np.array([3.0]))
+    c2.close()
+    c3 = sg.Context(0)
+    r = np.array([1], np.uint32)
+    v = np.array([3.0])
+    st = sg.lib().spg_lock(c3.h, A.h, r.ctypes.data, r.ctypes.data, v.ctypes.data, 1)
+    assert st == sg.LogicError.code  # the orphaned matrix refuses work
+    A.close()
+    c3.close()
+
+
 def test_spmv_before_lock_is_logic_error(ctx):
     A = sg.Csr(ctx, 3, 3)
     with pytest.raises(sg.LogicError):
