@@ -139,6 +139,24 @@ int spg_spmv(spg_ctx *ctx, const spg_csr *A, const double *d_x, double *d_y,
  * SPG_ERR_INVALID_ARGUMENT (serial/spmv.hpp:150-155). */
 int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
                   uint64_t x_len, double *y, uint64_t y_len, int variant);
+/* SpMV that allocates no device memory at all. No counterpart in Spira.
+ * For callers that cannot call cudaMalloc (or let this library call it):
+ * code whose device memory is all owned by another allocator or a fixed
+ * arena sized at start-up, and latency-critical loops where an allocation
+ * could stall other work on the device. It runs the MERGE variant with its
+ * scratch (tile starts and carry-outs) in a fixed array of about 2 MiB
+ * compiled into libspg.so, which every device that loads the library keeps
+ * until the process exits. Limit: rows + nonzeros <= spg_spmv_noalloc_max()
+ * (117 440 512); larger matrices get SPG_ERR_INVALID_ARGUMENT. The first call
+ * on a device looks up the array's device address (this may also load the
+ * library's GPU code), so make that first call before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (different
+ * streams, or several host threads) race, and the caller must serialize
+ * them. Each call rewrites all the scratch it reads. Device x, y; asynchronous
+ * on `stream`. */
+int spg_spmv_noalloc(spg_ctx *ctx, const spg_csr *A, const double *d_x, double *d_y, void *stream);
+uint64_t spg_spmv_noalloc_max(void);
+
 /* The variant SPG_SPMV_AUTO resolves to for A. */
 int spg_spmv_selected(spg_ctx *ctx, const spg_csr *A, int *variant);
 /* Number of kernel launches one spg_spmv of A with `variant` issues (plans

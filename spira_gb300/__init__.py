@@ -100,6 +100,8 @@ _SIGS = [
     ("spg_lock_device", _I, [_P, _P, _P, _P, _P, _U64]),
     ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
     ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
+    ("spg_spmv_noalloc", _I, [_P, _P, _P, _P, _P]),
+    ("spg_spmv_noalloc_max", _U64, []),
     ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
     ("spg_spmv_launches", _I, [_P, _P, _I, C.POINTER(_I)]),
     ("spg_set_spmv_policy", _I, [_P, _I]),

@@ -495,3 +495,76 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStr
 }
 
 }  // namespace spg
+
+// ---------------------------------------------------------------------------
+// SpMV without any device allocation: the MERGE variant with its scratch (the
+// tiles' merge-path starts and carry-outs) in a fixed array compiled into the
+// library, for callers that must not allocate device memory.
+// ---------------------------------------------------------------------------
+namespace spg {
+namespace {
+
+constexpr uint64_t NOALLOC_MAX_TILES = 65536;  // rows + nonzeros <= 65536 * MG_TILE
+constexpr size_t NOALLOC_STARTS_BYTES = 2 * (NOALLOC_MAX_TILES + 1) * sizeof(uint64_t);
+constexpr size_t NOALLOC_BYTES = NOALLOC_STARTS_BYTES + NOALLOC_MAX_TILES * sizeof(Carry);
+
+// Every device that loads libspg.so holds these ~2 MiB until the process exits.
+static __device__ __align__(256) unsigned char g_spmv_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array for the current device; looked up once
+// per device. The host-side symbol is only a stand-in and must never be
+// handed to a kernel.
+int noalloc_scratch(int device, void **out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return set_error(SPG_ERR_UNSUPPORTED, "spg_spmv_noalloc: device %d beyond %d", device, NOALLOC_MAX_DEVICES);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_error(SPG_ERR_CUDA, "spg_spmv_noalloc: cudaGetSymbolAddress failed: %s",
+                             cudaGetErrorString(e));
+        g_noalloc_addr[device] = p;
+    }
+    *out = g_noalloc_addr[device];
+    return SPG_OK;
+}
+
+}  // namespace
+}  // namespace spg
+
+extern "C" uint64_t spg_spmv_noalloc_max(void) { return spg::NOALLOC_MAX_TILES * (uint64_t)spg::MG_TILE; }
+
+extern "C" int spg_spmv_noalloc(spg_ctx *c, const spg_csr *A, const double *d_x, double *d_y, void *stream) {
+    using namespace spg;
+    if (!c || !A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_noalloc: null handle");
+    SPG_CHECK_LIVE(A);
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+    if ((A->n_cols && !d_x) || (A->n_rows && !d_y))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_noalloc: null vector");
+    const uint64_t total = A->n_rows + A->nnz;
+    if (total > spg_spmv_noalloc_max())
+        return set_error(SPG_ERR_INVALID_ARGUMENT,
+                         "spg_spmv_noalloc: rows + nonzeros = %llu exceeds the fixed scratch limit of %llu "
+                         "(use spg_spmv)",
+                         (unsigned long long)total, (unsigned long long)spg_spmv_noalloc_max());
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (A->n_rows == 0) return SPG_OK;
+    void *scratch = nullptr;
+    SPG_TRY(noalloc_scratch(c->device, &scratch));
+    uint64_t *starts = static_cast<uint64_t *>(scratch);
+    Carry *carry = reinterpret_cast<Carry *>(static_cast<unsigned char *>(scratch) + NOALLOC_STARTS_BYTES);
+    const uint64_t nt = (total + MG_TILE - 1) / MG_TILE;
+    cudaStream_t s = pick_stream(c, stream);
+    // Every call rewrites all tile starts and carries it reads, so nothing
+    // left from an earlier call is used.
+    merge_tile_starts<<<grid_for(nt + 1, 256), 256, 0, s>>>(A->d_off(), A->n_rows, A->nnz, nt, starts);
+    SPG_LAUNCH_CHECK();
+    spmv_merge<<<(unsigned)nt, BLOCK, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), d_x, d_y, A->n_rows, starts, carry);
+    SPG_LAUNCH_CHECK();
+    merge_fixup<<<grid_for(nt, 256), 256, 0, s>>>(carry, nt, A->n_rows, d_y);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
