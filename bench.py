@@ -36,6 +36,12 @@ GRID = 1414
 ZIPF_N = 4_000_000
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel from one ncu
+# capture (profiles/spmv_interleaved_zipf4m.md): (bytes, nonzeros of the
+# captured matrix); scaled to the bench matrix by its nonzero count.
+NCU_TRAFFIC = {("zipf4m", "interleaved"): (811.0e6, 63_247_590)}
+
+
 def spmv_bytes(n_rows, n_cols, nnz):
     return 12 * nnz + 8 * (n_rows + 1) + 8 * n_cols + 8 * n_rows
 
@@ -163,11 +169,26 @@ def run_ours(args):
         total_ms = float(ev[0][0].elapsed_time(ev[-1][-1]))
         return total_ms / steps, per.mean(axis=0)
 
+    def b2b(m, reps=100):
+        """ms per SpMV over `reps` back-to-back SpMVs of one matrix (each one
+        streams more than the L2 holds), events only at the ends."""
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                m["A"].spmv(m["xd"], m["yd"], m["selected"], stream=ctx.stream)
+            e0.record(stream)
+            for _ in range(reps):
+                m["A"].spmv(m["xd"], m["yd"], m["selected"], stream=ctx.stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
     clk = ClockSampler(dev)
     clk.start()
     ms_sel, per_sel = timed(lambda m: m["selected"], args.steps, args.warmup)
     ms_plain, per_plain = timed(lambda m: sg.SPMV_SCALAR, args.steps, args.warmup)
     ms_auto, per_auto = timed(lambda m: m["autotuned"], max(args.steps // 4, 10), args.warmup)
+    ms_b2b = [b2b(m) for m in mats]
     clocks = clk.stop()
     batched = None if args.no_batched else run_batched(ctx, stream)
 
@@ -195,10 +216,16 @@ def run_ours(args):
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
 
     peak, peak_kind = peaks()
+    ops = None if args.no_ops else run_ops(ctx, peak)
     dom = int(np.argmax(per_sel))
     dm = mats[dom]
     achieved = dm["bytes"] / (per_sel[dom] * 1e-3) / 1e9
     gpu_launches = args.steps * sum(m["A"].spmv_launches(m["selected"]) for m in mats)
+    # the second ceiling of a random-column matrix: one L2 sector read per nonzero
+    gather_rate = ctx.probe_gather_rate(1 << 22, 1 << 26)
+    floor_ms = dm["nnz"] / gather_rate * 1e3
+    cap = NCU_TRAFFIC.get((dm["name"], sg.SPMV_NAMES[dm["selected"]]))
+    traffic = round(cap[0] * dm["nnz"] / cap[1]) if cap else None
 
     cpu = cpu_baseline(host, [m["x"] for m in mats], total_bytes)
     line = {
@@ -219,7 +246,10 @@ def run_ours(args):
              "bytes_per_spmv": m["bytes"], "variant": sg.SPMV_NAMES[m["selected"]],
              "ms_selected": round(float(per_sel[i]), 5), "ms_plain": round(float(per_plain[i]), 5),
              "gbs_selected": round(m["bytes"] / (per_sel[i] * 1e-3) / 1e9, 1),
-             "gbs_plain": round(m["bytes"] / (per_plain[i] * 1e-3) / 1e9, 1)}
+             "gbs_plain": round(m["bytes"] / (per_plain[i] * 1e-3) / 1e9, 1),
+             "ms_100_back_to_back": round(ms_b2b[i], 5),
+             "gbs_100_back_to_back": round(m["bytes"] / (ms_b2b[i] * 1e-3) / 1e9, 1),
+             "frac_100_back_to_back": round(m["bytes"] / (ms_b2b[i] * 1e-3) / 1e9 / peak, 4)}
             for i, m in enumerate(mats)],
             "bytes_per_step": total_bytes,
             "l2": "no flush: each step streams 1.03 GB (> 129 MB L2)"},
@@ -232,9 +262,15 @@ def run_ours(args):
                                                              for v, t in enumerate(m["autotune_ms"])}
                                                   for m in mats}},
         "batched": batched,
+        "ops": ops,
         "roofline": {"bound": "hbm", "kernel": f"spmv[{dm['name']}:{sg.SPMV_NAMES[dm['selected']]}]",
                      "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None},
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "algorithmic_bytes": dm["bytes"],
+                     "gather_ceiling": {"random_8B_gathers_per_s": round(gather_rate, -6),
+                                        "probe": "spg_probe_gather_rate(2^22 doubles, 2^26 reads)",
+                                        "floor_ms": round(floor_ms, 5),
+                                        "frac_of_ceiling": round(floor_ms / per_sel[dom], 4)}},
         "parity": {"max_err_vs_compensated_oracle": max_err, "tolerance": 1e-12,
                    "bound": "|y-y_ref| <= tol * sum|a x| per row"},
         "e2e": {"value": round(total_bytes / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
@@ -311,6 +347,147 @@ def run_batched(ctx, stream, n_mats=4096, seed=2024):
     return out
 
 
+def lock_bytes(n_rows, staged, nnz_old, nnz_new):
+    """Algorithmic bytes of one lock(): read the staged triples (u32 row, u32
+    column, f64 value) and the old CSR, write the new CSR."""
+    old = 12 * nnz_old + 8 * (n_rows + 1) if nnz_old else 0
+    return 16 * staged + old + 12 * nnz_new + 8 * (n_rows + 1)
+
+
+def csr_bytes(n_rows, nnz):
+    return 12 * nnz + 8 * (n_rows + 1)
+
+
+def run_ops(ctx, peak):
+    """lock() (first build and 1 % re-lock merge), transpose and SpGEMM on the
+    GPU at their full configuration sizes, against the oracle's C port of the
+    same steps on one host core. GPU times are wall-clock around the C-ABI
+    call with the stream synchronised on both sides (the calls synchronise
+    internally: their output sizes are data-dependent), median of 3."""
+    import torch
+
+    import oracle
+    import spira_gb300 as sg
+    from spira_gb300 import gen, gen_device
+
+    def wall(fn, reps=3, setup=None):
+        ts = []
+        for _ in range(reps):
+            if setup:
+                setup()
+            ctx.sync()
+            t0 = time.perf_counter()
+            fn()
+            ctx.sync()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3
+
+    def cpu(fn):
+        t0 = time.perf_counter()
+        out = fn()
+        return (time.perf_counter() - t0) * 1e3, out
+
+    def rec(name, gpu_ms, by, cpu_ms, **kw):
+        d = {"case": name, "gpu_ms": round(gpu_ms, 3), "bytes": int(by),
+             "gbs": round(by / (gpu_ms * 1e-3) / 1e9, 1), "frac_of_hbm": round(by / (gpu_ms * 1e-3) / 1e9 / peak, 4)}
+        if cpu_ms is not None:
+            d.update({"cpu_ms": round(cpu_ms, 1), "cpu_kind": "port", "cpu_cores": 1,
+                      "speedup_vs_cpu": round(cpu_ms / gpu_ms, 1)})
+        d.update(kw)
+        return d
+
+    out = {"lock": [], "transpose": [], "spgemm": []}
+    dev = "cuda:0"
+
+    def to_dev(r, c, v):
+        return (torch.from_numpy(r.view(np.int32)).to(dev), torch.from_numpy(c.view(np.int32)).to(dev),
+                torch.from_numpy(v).to(dev))
+
+    # ---- lock: 2D Laplacian (2a) and Zipf 4M (2b), first lock + 1 % re-lock
+    g2 = GRID * GRID
+    r, c, v = gen.laplacian_2d(GRID)
+    b = gen.relock_batch(g2, g2, len(r), seed=21)
+    cases = [("laplacian2d", g2, (r, c, v), b, True)]
+    zr, zc, zv, zm = gen_device.zipf_rows(ctx, ZIPF_N, seed=31)
+    cases.append(("zipf4m", ZIPF_N, (zr, zc, zv, zm), gen.relock_batch(ZIPF_N, ZIPF_N, zm, seed=32), False))
+    for name, n, first, delta, host_first in cases:
+        d_first = to_dev(*first) + (len(first[0]),) if host_first else first
+        m = d_first[3]
+        holder = []
+
+        def do_first():
+            A = sg.Csr(ctx, n, n)
+            A.lock_device(*d_first)
+            holder.append(A)
+
+        t_first = wall(do_first)
+        A = holder[-1]
+        nnz0 = A.nnz
+        for h in holder[:-1]:
+            h.close()
+        pristine = sg.Csr(ctx, n, n)
+        pristine.copy_from(A)
+        t_relock = wall(lambda: A.lock(*delta), setup=lambda: A.copy_from(pristine))
+        nnz1 = A.nnz
+        t_e2e = None
+        cpu_first = cpu_relock = None
+        if host_first:
+            def do_host():
+                B = sg.Csr(ctx, n, n)
+                B.lock(*first)
+                B.close()
+            t_e2e = wall(do_host)
+            cpu_first, _ = cpu(lambda: oracle.lock_epochs(n, n, [first]))
+            cpu_both, _ = cpu(lambda: oracle.lock_epochs(n, n, [first, delta]))
+            cpu_relock = max(cpu_both - cpu_first, 0.0)
+        out["lock"].append(rec(f"{name}_first", t_first, lock_bytes(n, m, 0, nnz0), cpu_first, staged=int(m),
+                               nnz=int(nnz0), staging="device",
+                               **({"e2e_ms_host_staging": round(t_e2e, 3)} if t_e2e else {})))
+        out["lock"].append(rec(f"{name}_relock", t_relock, lock_bytes(n, len(delta[0]), nnz0, nnz1), cpu_relock,
+                               staged=int(len(delta[0])), nnz=int(nnz1), staging="host",
+                               **({"cpu_note": "port: lock of both epochs minus the first"} if cpu_relock else {})))
+        A.close()
+        pristine.close()
+        del d_first
+    del zr, zc, zv
+    torch.cuda.empty_cache()
+
+    # ---- transpose and SpGEMM: 3D Laplacian 100^3 (3a), uniform 200k x 8 (3b)
+    for name, n, (r, c, v) in [("laplacian3d_100", 100 ** 3, gen.laplacian_3d(100)),
+                               ("uniform200k_8", 200_000, gen.uniform_rows(200_000, 200_000, 8, seed=77))]:
+        A = sg.Csr(ctx, n, n)
+        A.lock(r, c, v)
+        H = A.download()
+        res = {}
+
+        def do_t():
+            res["T"] = A.transpose()
+
+        t_t = wall(do_t)
+        cpu_t, T_ref = cpu(lambda: oracle.transpose(H))
+        T = res["T"]
+        same_t = oracle.csr_digest(T.download()) == oracle.csr_digest(T_ref)
+        out["transpose"].append(rec(name, t_t, 2 * csr_bytes(n, A.nnz), cpu_t, nnz=int(A.nnz), bit_exact=same_t))
+        T.close()
+
+        def do_g():
+            if "C" in res:
+                res["C"].close()
+            res["C"] = A.spgemm(A)
+
+        t_g = wall(do_g)
+        cpu_g, C_ref = cpu(lambda: oracle.spgemm(H, H))
+        Cm = res["C"]
+        prods = int(oracle.spgemm_products(H, H))
+        same_g = oracle.csr_digest(Cm.download()) == oracle.csr_digest(C_ref)
+        by = 2 * csr_bytes(n, A.nnz) + csr_bytes(n, Cm.nnz)
+        out["spgemm"].append(rec(name, t_g, by, cpu_g, nnz_a=int(A.nnz), nnz_c=int(Cm.nnz), products=prods,
+                                 gproducts_per_s=round(prods / (t_g * 1e-3) / 1e9, 2), bit_exact=same_g))
+        Cm.close()
+        A.close()
+    return out
+
+
 def _cpu_spmv_seconds(host, xs, nthr, kind, budget_s):
     """Mean seconds of one SpMV per matrix on the host cores."""
     import oracle
@@ -374,14 +551,69 @@ def run_reference(args):
     }))
 
 
+PROFILE_CASES = {
+    # name: (rows, kind); zipf1m is a quarter-size Zipf matrix (~16M nonzeros,
+    # ~220 MB: larger than L2, small enough for multi-pass ncu captures)
+    "laplacian2d": (GRID * GRID, "laplacian"),
+    "zipf1m": (1_000_000, "zipf"),
+    "zipf4m": (ZIPF_N, "zipf"),
+}
+
+
+def run_profile_case(args):
+    """One matrix, a few SpMVs per listed variant: the program ncu captures.
+    Prints the per-SpMV CUDA-event times (not a bench value)."""
+    import torch
+
+    import spira_gb300 as sg
+    from spira_gb300 import gen, gen_device
+    ctx = sg.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    n, kind = PROFILE_CASES[args.profile_case]
+    if kind == "zipf":
+        r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
+        A = sg.Csr(ctx, n, n)
+        A.lock_device(r, c, v, m)
+        del r, c, v
+    else:
+        r, c, v = gen.laplacian_2d(GRID)
+        A = sg.Csr(ctx, n, n)
+        A.lock(r, c, v)
+    x = torch.from_numpy(gen.dense_x(n, 3)).to("cuda:0")
+    y = torch.empty(n, dtype=torch.float64, device="cuda:0")
+    ctx.sync()
+    out = {}
+    with torch.cuda.stream(stream):
+        for name in args.variants.split(","):
+            vid = sg.SPMV_VARIANTS[name]
+            A.spmv(x, y, vid, stream=ctx.stream)  # builds the variant's plan
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.reps + 1)]
+            ev[0].record(stream)
+            for i in range(args.reps):
+                A.spmv(x, y, vid, stream=ctx.stream)
+                ev[i + 1].record(stream)
+            torch.cuda.synchronize()
+            out[name] = [round(ev[i].elapsed_time(ev[i + 1]), 5) for i in range(args.reps)]
+    print(json.dumps({"profile_case": args.profile_case, "n_rows": n, "nnz": A.nnz,
+                      "bytes_per_spmv": spmv_bytes(n, n, A.nnz), "ms_per_spmv": out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
+                    help="run a few SpMVs of one matrix (for ncu captures) instead of the bench")
+    ap.add_argument("--variants", default="adaptive16", help="with --profile-case: comma-separated variant names")
+    ap.add_argument("--reps", type=int, default=2, help="with --profile-case: SpMVs per variant after one warm-up")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-RHS section")
+    ap.add_argument("--no-ops", action="store_true", help="skip the lock / transpose / SpGEMM section")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:

@@ -57,7 +57,11 @@ enum spg_spmv_variant {
                                FMA chain, rows closed at a row-start bitmap, segmented
                                combine across lanes and chunks */
     SPG_SPMV_ADAPTIVE16 = 9, /* the same with 16 nonzeros per lane */
-    SPG_SPMV_N_VARIANTS = 10
+    SPG_SPMV_INTERLEAVED = 10, /* ADAPTIVE16's arithmetic over a copy of cols/vals stored
+                                  lane-interleaved per 512-nonzero chunk, so every load is
+                                  one contiguous 512-byte warp access; the copy costs
+                                  12 B per nonzero of device memory while cached */
+    SPG_SPMV_N_VARIANTS = 11
 };
 
 typedef struct spg_ctx spg_ctx; /* one device + one stream + memory pool */
@@ -181,6 +185,13 @@ int spg_spmv_features(spg_ctx *ctx, const spg_csr *A, float *features);
 /* Times every variant (median of `reps` warm runs, CUDA events): times_ms
  * [SPG_SPMV_N_VARIANTS] (may be NULL) and the fastest in *best (may be NULL). */
 int spg_spmv_autotune(spg_ctx *ctx, const spg_csr *A, int reps, float *times_ms, int *best);
+/* Device probe, no Spira counterpart: the rate (gathers per second, median of
+ * 5 timed runs after 2 warm-up runs) of random 8-byte reads from an n_x-entry
+ * double vector (n_x a power of two; 2^22 = 32 MB stays in L2), n_gathers
+ * reads per run, 16 per thread at hashed positions. It is the ceiling of SpMV
+ * on matrices with randomly spread columns, where every nonzero's x read hits
+ * its own L2 sector. */
+int spg_probe_gather_rate(spg_ctx *ctx, uint64_t n_x, uint64_t n_gathers, double *gathers_per_s);
 /* Installs a trained selector (NULL blob removes it). Blob layout, FP32:
  * mean[40] scale[40] W1[64][40] b1[64] W2[64][64] b2[64] W3[K][64] b3[K];
  * output k predicts log(time of variant k / fastest time). */

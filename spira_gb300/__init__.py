@@ -20,10 +20,10 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libspg.so"
 
 SPMV_AUTO, SPMV_SCALAR, SPMV_VECTOR2, SPMV_VECTOR4, SPMV_VECTOR8, SPMV_VECTOR16, SPMV_VECTOR32, \
-    SPMV_STREAM, SPMV_MERGE, SPMV_ADAPTIVE, SPMV_ADAPTIVE16 = -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
+    SPMV_STREAM, SPMV_MERGE, SPMV_ADAPTIVE, SPMV_ADAPTIVE16, SPMV_INTERLEAVED = -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
 SPMV_VARIANTS = {
     "scalar": 0, "vector2": 1, "vector4": 2, "vector8": 3, "vector16": 4, "vector32": 5,
-    "stream": 6, "merge": 7, "adaptive": 8, "adaptive16": 9,
+    "stream": 6, "merge": 7, "adaptive": 8, "adaptive16": 9, "interleaved": 10,
 }
 SPMV_NAMES = {v: k for k, v in SPMV_VARIANTS.items()}
 
@@ -107,6 +107,7 @@ _SIGS = [
     ("spg_set_spmv_policy", _I, [_P, _I]),
     ("spg_spmv_features", _I, [_P, _P, _P]),
     ("spg_spmv_autotune", _I, [_P, _P, _I, _P, C.POINTER(_I)]),
+    ("spg_probe_gather_rate", _I, [_P, _U64, _U64, C.POINTER(C.c_double)]),
     ("spg_selector_load", _I, [_P, _P, _U64, _I]),
     ("spg_mlp_param_count", _U64, [_I]),
     ("spg_selector_predict", _I, [_P, _P, _U32, _P, _P]),
@@ -207,6 +208,13 @@ class Context:
             return
         blob = np.ascontiguousarray(blob, dtype=np.float32)
         _check(lib().spg_selector_load(self.h, _ptr(blob), len(blob), n_outputs))
+
+    def probe_gather_rate(self, n_x: int = 1 << 22, n_gathers: int = 1 << 26) -> float:
+        """Random 8-byte gathers per second from an n_x-entry vector: the
+        ceiling of SpMV on matrices with randomly spread columns."""
+        r = C.c_double()
+        _check(lib().spg_probe_gather_rate(self.h, n_x, n_gathers, C.byref(r)))
+        return r.value
 
 
 class Csr:

@@ -415,9 +415,12 @@ int spg_spmv_launches(spg_ctx *c, const spg_csr *Ac, int variant, int *n) {
             break;
         case SPG_SPMV_ADAPTIVE:
         case SPG_SPMV_ADAPTIVE16:
-            SPG_TRY(build_adaptive_plan(c, A, variant == SPG_SPMV_ADAPTIVE ? 32 : 16, c->stream));
-            *n = (A->plan_adaptive.n_items ? 2 : 0) + (A->plan_adaptive.count1 ? 1 : 0);
+        case SPG_SPMV_INTERLEAVED: {
+            SPG_TRY(build_adaptive_plan(c, A, variant, c->stream));
+            const SpmvPlan &P = adaptive_plan_of(A, variant);
+            *n = (P.n_items ? 2 : 0) + (P.count1 ? 1 : 0);
             break;
+        }
         case SPG_SPMV_STREAM:
             *n = 1;
             break;

@@ -86,6 +86,7 @@ struct SpmvPlan {
     DevBuf items;            // variant-specific item descriptors
     DevBuf aux;              // variant-specific scratch (carry-outs)
     DevBuf extra0, extra1, extra2;
+    DevBuf extra3, extra4;
 };
 
 struct Csr;
@@ -143,13 +144,14 @@ struct Csr {
     bool stats_valid = false;
     uint64_t max_row = 0;
     int selected_spmv = -1;
-    SpmvPlan plan_stream, plan_merge, plan_adaptive;
+    SpmvPlan plan_stream, plan_merge, plan_adaptive, plan_inter;
     void invalidate_derived() {
         stats_valid = false;
         selected_spmv = -1;
         plan_stream = SpmvPlan{};
         plan_merge = SpmvPlan{};
         plan_adaptive = SpmvPlan{};
+        plan_inter = SpmvPlan{};
     }
     const uint64_t *d_off() const { return off.as<uint64_t>(); }
     const uint32_t *d_cols() const { return cols.as<uint32_t>(); }
@@ -226,10 +228,14 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant,
 int spmv_resolve_auto(Ctx *c, Csr *A, int *variant);
 // Loads spg_selector.bin from beside libspg.so (or $SPG_SELECTOR_MODEL) if any.
 int selector_load_default(Ctx *c);
-// SPG_SPMV_ADAPTIVE with `items` (8 or 16) nonzeros per thread chunk
-// (spg_spmv_adaptive.cu); builds and caches its plan on first use.
-int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int items, cudaStream_t s);
-int build_adaptive_plan(Ctx *c, Csr *A, int items, cudaStream_t s);
+// SPG_SPMV_ADAPTIVE, SPG_SPMV_ADAPTIVE16 and SPG_SPMV_INTERLEAVED
+// (spg_spmv_adaptive.cu); each builds and caches its plan on first use.
+int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s);
+int build_adaptive_plan(Ctx *c, Csr *A, int variant, cudaStream_t s);
+// The cached plan slot of one of those variants.
+inline SpmvPlan &adaptive_plan_of(Csr *A, int variant) {
+    return variant == SPG_SPMV_INTERLEAVED ? A->plan_inter : A->plan_adaptive;
+}
 
 }  // namespace spg
 

@@ -484,9 +484,9 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStr
             break;
         }
         case SPG_SPMV_ADAPTIVE:
-            return spmv_adaptive(c, A, x, y, 32, s);
         case SPG_SPMV_ADAPTIVE16:
-            return spmv_adaptive(c, A, x, y, 16, s);
+        case SPG_SPMV_INTERLEAVED:
+            return spmv_adaptive(c, A, x, y, variant, s);
         default:
             return set_error(SPG_ERR_INVALID_ARGUMENT, "spmv: unknown variant %d", variant);
     }

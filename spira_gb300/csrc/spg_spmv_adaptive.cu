@@ -22,6 +22,16 @@
 // starts a row, the common case for short rows); rows crossing a chunk
 // boundary leave a (row, partial) record per chunk, summed in chunk order by
 // a second small kernel. Deterministic for a given matrix and variant.
+//
+// SPG_SPMV_INTERLEAVED runs the same kernel over a copy of cols and vals
+// stored lane-interleaved within each 512-nonzero chunk (vals in pairs, cols
+// in quads: the k-th 16-byte piece of every lane lies side by side). A lane
+// still owns 16 consecutive nonzeros and sums them in the same order, so y is
+// bit-identical to SPG_SPMV_ADAPTIVE16, but each warp load is one contiguous
+// 512-byte access instead of 32 strided 16-byte pieces. On random-column
+// matrices the x gathers saturate the L1 data pipe; the strided loads of the
+// in-place layout cost about as many L1 wavefronts again, the interleaved ones
+// an eighth of that.
 #include "spg_internal.cuh"
 
 namespace spg {
@@ -75,8 +85,9 @@ __global__ void seg_row_maps(const uint64_t *__restrict__ ne_scan, uint64_t n, u
 
 // ---------------------------------------------------------------- SpMV
 // ITEMS nonzeros per lane, handled in sub-batches of SUB (loads, gathers, FMAs)
-// to keep registers low enough for 4 CTAs of 256 threads per SM.
-template <int ITEMS, int SUB>
+// to keep registers low enough for 4 CTAs of 256 threads per SM. INTER: cols
+// and vals are the lane-interleaved copies (ITEMS == 16).
+template <int ITEMS, int SUB, bool INTER>
 __global__ void __launch_bounds__(256, 4)
 spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, const double *__restrict__ x,
          double *__restrict__ y, uint64_t nnz, const unsigned *__restrict__ bitmap,
@@ -111,19 +122,40 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
         double v[SUB], g[SUB];
         uint32_t c[SUB];
         if (nv) {
+            if constexpr (INTER) {
+                // piece k of lane l sits at chunk + 64 k + 2 l (vals), chunk + 128 k + 4 l (cols)
+                const uint64_t cb = w * (32ull * ITEMS);
 #pragma unroll
-            for (int u = 0; u < SUB; u += 2) {
-                const double2 t = *reinterpret_cast<const double2 *>(vals + base + u);
-                v[u] = t.x;
-                v[u + 1] = t.y;
-            }
+                for (int u = 0; u < SUB; u += 2) {
+                    const double2 t = __ldcs(reinterpret_cast<const double2 *>(
+                        vals + cb + 64u * (unsigned)((SUB * h + u) >> 1) + 2u * (unsigned)lane));
+                    v[u] = t.x;
+                    v[u + 1] = t.y;
+                }
 #pragma unroll
-            for (int u = 0; u < SUB; u += 4) {
-                const uint4 t = *reinterpret_cast<const uint4 *>(cols + base + u);
-                c[u] = t.x;
-                c[u + 1] = t.y;
-                c[u + 2] = t.z;
-                c[u + 3] = t.w;
+                for (int u = 0; u < SUB; u += 4) {
+                    const uint4 t = __ldcs(reinterpret_cast<const uint4 *>(
+                        cols + cb + 128u * (unsigned)((SUB * h + u) >> 2) + 4u * (unsigned)lane));
+                    c[u] = t.x;
+                    c[u + 1] = t.y;
+                    c[u + 2] = t.z;
+                    c[u + 3] = t.w;
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < SUB; u += 2) {
+                    const double2 t = *reinterpret_cast<const double2 *>(vals + base + u);
+                    v[u] = t.x;
+                    v[u + 1] = t.y;
+                }
+#pragma unroll
+                for (int u = 0; u < SUB; u += 4) {
+                    const uint4 t = *reinterpret_cast<const uint4 *>(cols + base + u);
+                    c[u] = t.x;
+                    c[u + 1] = t.y;
+                    c[u + 2] = t.z;
+                    c[u + 3] = t.w;
+                }
             }
         }
 #pragma unroll
@@ -200,6 +232,21 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
     }
 }
 
+// Lane-interleaved copy for SPG_SPMV_INTERLEAVED: nonzero p = 512 w + 16 l + u
+// (chunk w, lane l, item u) goes to 512 w + 64 (u / 2) + 2 l + u % 2 in vals and
+// 512 w + 128 (u / 4) + 4 l + u % 4 in cols; the tail of the last chunk is zero.
+__global__ void seg_interleave(const uint32_t *__restrict__ cols, const double *__restrict__ vals, uint64_t nnz,
+                               uint64_t n_slots, uint32_t *__restrict__ icols, double *__restrict__ ivals) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_slots;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t w = p >> 9;
+        const unsigned q = (unsigned)(p & 511), l = q >> 4, u = q & 15;
+        const bool real = p < nnz;
+        ivals[(w << 9) + 64u * (u >> 1) + 2u * l + (u & 1u)] = real ? vals[p] : 0.0;
+        icols[(w << 9) + 128u * (u >> 2) + 4u * l + (u & 3u)] = real ? cols[p] : 0u;
+    }
+}
+
 // Rows crossing chunk boundaries: each run of records with the same row
 // (at most one NONE record between two of them) is summed in chunk order by
 // the thread holding its first record.
@@ -236,10 +283,15 @@ __global__ void seg_empty_rows(const uint32_t *__restrict__ empty, uint64_t n_em
 
 }  // namespace
 
-// Plan layout in Csr::plan_adaptive: items = bitmap, extra0 = chunk_base,
-// aux = chunk records, extra1 = nzrow, extra2 = empty rows, count1 = #empty.
-int build_adaptive_plan(Ctx *c, Csr *A, int items, cudaStream_t s) {
-    if (A->plan_adaptive.kind == SPG_SPMV_ADAPTIVE * 100 + items) return SPG_OK;
+// Plan layout (Csr::plan_adaptive, or Csr::plan_inter for the interleaved
+// variant): items = bitmap, extra0 = chunk_base, aux = chunk records,
+// extra1 = nzrow, extra2 = empty rows, count1 = #empty; interleaved only:
+// extra3 = cols, extra4 = vals in lane-interleaved order.
+int build_adaptive_plan(Ctx *c, Csr *A, int variant, cudaStream_t s) {
+    const int items = variant == SPG_SPMV_ADAPTIVE ? 32 : 16;
+    const bool inter = variant == SPG_SPMV_INTERLEAVED;
+    SpmvPlan &slot = adaptive_plan_of(A, variant);
+    if (slot.kind == variant * 100 + items) return SPG_OK;
     const uint64_t n = A->n_rows, nnz = A->nnz;
     const uint64_t chunk = 32ull * items;
     const uint64_t n_chunks = (nnz + chunk - 1) / chunk;
@@ -276,7 +328,15 @@ int build_adaptive_plan(Ctx *c, Csr *A, int items, cudaStream_t s) {
         SPG_LAUNCH_CHECK();
     }
     SPG_TRY(recs.alloc((2 * n_chunks + 1) * sizeof(Rec), s));
-    P.kind = SPG_SPMV_ADAPTIVE * 100 + items;
+    if (inter && n_chunks) {
+        const uint64_t n_slots = n_chunks * chunk;
+        SPG_TRY(P.extra3.alloc(n_slots * sizeof(uint32_t), s));
+        SPG_TRY(P.extra4.alloc(n_slots * sizeof(double), s));
+        seg_interleave<<<grid_for(n_slots, 256, (unsigned)c->n_sms * 16), 256, 0, s>>>(
+            A->d_cols(), A->d_vals(), nnz, n_slots, P.extra3.as<uint32_t>(), P.extra4.as<double>());
+        SPG_LAUNCH_CHECK();
+    }
+    P.kind = variant * 100 + items;
     P.n_items = n_chunks;
     P.items = std::move(bm);
     P.aux = std::move(recs);
@@ -284,23 +344,29 @@ int build_adaptive_plan(Ctx *c, Csr *A, int items, cudaStream_t s) {
     P.extra1 = std::move(nzrow);
     P.extra2 = std::move(empty);
     P.count1 = n_empty;
-    A->plan_adaptive = std::move(P);
+    slot = std::move(P);
     return SPG_OK;
 }
 
-int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int items, cudaStream_t s) {
-    SPG_TRY(build_adaptive_plan(c, A, items, s));
-    const SpmvPlan &P = A->plan_adaptive;
+int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s) {
+    SPG_TRY(build_adaptive_plan(c, A, variant, s));
+    const SpmvPlan &P = adaptive_plan_of(A, variant);
     const uint64_t nch = P.n_items;
     const uint32_t *nzrow = P.count1 ? P.extra1.as<uint32_t>() : nullptr;
     if (nch) {
         const unsigned grid = grid_for(nch * 32, 256);
-        if (items == 16)
-            spmv_seg<16, 8><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
-                                              P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), nch);
+        if (variant == SPG_SPMV_INTERLEAVED)
+            spmv_seg<16, 8, true><<<grid, 256, 0, s>>>(P.extra3.as<uint32_t>(), P.extra4.as<double>(), x, y, A->nnz,
+                                                    P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
+                                                    P.aux.as<Rec>(), nch);
+        else if (variant == SPG_SPMV_ADAPTIVE16)
+            spmv_seg<16, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz,
+                                                     P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
+                                                     P.aux.as<Rec>(), nch);
         else
-            spmv_seg<32, 8><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
-                                              P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), nch);
+            spmv_seg<32, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz,
+                                                     P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
+                                                     P.aux.as<Rec>(), nch);
         SPG_LAUNCH_CHECK();
         seg_fixup<<<grid_for(2 * nch, 256), 256, 0, s>>>(P.aux.as<Rec>(), 2 * nch, nzrow, y);
         SPG_LAUNCH_CHECK();

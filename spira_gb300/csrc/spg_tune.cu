@@ -25,6 +25,32 @@
 namespace spg {
 namespace {
 
+// ---------------------------------------------------------------- gather probe
+// The ceiling of SpMV on matrices whose columns are spread at random: random
+// 8-byte reads of an L2-resident x. Each thread makes 16 independent reads at
+// hashed positions (32-bit "lowbias32" finaliser), so every warp request
+// touches ~32 different sectors, as the x gathers of such a matrix do.
+constexpr uint64_t GATHER_PER_THREAD = 16;
+
+__device__ __forceinline__ uint32_t mix32(uint32_t a) {
+    a ^= a >> 16;
+    a *= 0x7feb352dU;
+    a ^= a >> 15;
+    a *= 0x846ca68bU;
+    a ^= a >> 16;
+    return a;
+}
+
+__global__ void gather_probe(const double *__restrict__ x, uint32_t mask, double *__restrict__ out, uint64_t n_thr) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (t >= n_thr) return;
+    double a = 0.0;
+#pragma unroll
+    for (uint32_t j = 0; j < GATHER_PER_THREAD; ++j)
+        a += __ldg(x + (mix32((uint32_t)t * (uint32_t)GATHER_PER_THREAD + j) & mask));
+    out[t] = a;
+}
+
 // ---------------------------------------------------------------- features
 // acc layout (doubles): [0..31] histogram, 32 sum L, 33 sum L^2, 34 max L,
 // 35 empty rows, 36 sum of |col/n_cols - row/n_rows| over sampled nonzeros,
@@ -483,6 +509,43 @@ int spg_mlp_argmin(spg_ctx *c, const float *d_pred, uint32_t B, int n_outputs, i
     if (!B) return SPG_OK;
     mlp_argmin<<<grid_for(B, 256), 256, 0, pick_stream(c, stream)>>>(d_pred, B, n_outputs, d_best);
     SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int spg_probe_gather_rate(spg_ctx *c, uint64_t n_x, uint64_t n_gathers, double *gathers_per_s) {
+    if (!c || !gathers_per_s) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate: null argument");
+    if (n_x == 0 || (n_x & (n_x - 1)) || n_x > (1ull << 32))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate: n_x must be a power of two <= 2^32");
+    const uint64_t n_thr = n_gathers / GATHER_PER_THREAD;
+    if (n_thr == 0 || n_thr > (1ull << 32))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate: n_gathers out of range");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    DevBuf x, out;
+    SPG_TRY(x.alloc(n_x * sizeof(double), s));
+    SPG_TRY(out.alloc(n_thr * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(x.ptr, 0, n_x * sizeof(double), s));
+    cudaEvent_t e0, e1;
+    SPG_CUDA_TRY(cudaEventCreate(&e0));
+    SPG_CUDA_TRY(cudaEventCreate(&e1));
+    std::vector<float> ts;
+    int rc = SPG_OK;
+    for (int r = 0; r < 7 && rc == SPG_OK; ++r) {
+        cudaEventRecord(e0, s);
+        gather_probe<<<grid_for(n_thr, 256), 256, 0, s>>>(x.as<double>(), (uint32_t)(n_x - 1), out.as<double>(),
+                                                          n_thr);
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) rc = set_error(SPG_ERR_CUDA, "gather probe: event sync failed");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r >= 2) ts.push_back(ms);  // two warm-up runs
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SPG_TRY(rc);
+    SPG_LAUNCH_CHECK();
+    std::sort(ts.begin(), ts.end());
+    *gathers_per_s = (double)(n_thr * GATHER_PER_THREAD) / (ts[ts.size() / 2] * 1e-3);
     return SPG_OK;
 }
 

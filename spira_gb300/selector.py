@@ -27,7 +27,7 @@ from . import (FAM_BANDED, FAM_BLOCKDIAG, FAM_POWERLAW, FAM_STENCIL2D, FAM_STENC
 from . import gen
 
 K = len(SPMV_VARIANTS)
-NNZ_CAP = 8_000_000
+NNZ_CAP = 16_000_000
 FAMILY_NAMES = ["banded", "blockdiag", "powerlaw", "uniform", "stencil"]
 
 

@@ -99,6 +99,37 @@ def test_spmv_scalar_is_bit_exact_with_fused_scalar_order(ctx):
     np.testing.assert_array_equal(y, oracle.spmv_scalar(A.download(), x, fused=True))
 
 
+@pytest.mark.parametrize("lengths", [[5000], [1, 3, 0, 17] * 3000, list(range(0, 3000, 7)), [16] * 4096])
+def test_interleaved_is_bit_identical_to_adaptive16(ctx, lengths):
+    """The interleaved variant runs ADAPTIVE16's per-lane FMA chains over a
+    permuted copy of cols/vals: the same bits, whatever the row lengths."""
+    r, c, v = _csr_from_rows(lengths, 30_000, seed=sum(lengths) % 1000)
+    A = build(ctx, len(lengths), 30_000, [(r, c, v)])
+    x = gen.dense_x(30_000, 6)
+    np.testing.assert_array_equal(A.spmv_host(x, variant=sg.SPMV_INTERLEAVED),
+                                  A.spmv_host(x, variant=sg.SPMV_ADAPTIVE16))
+
+
+def test_plans_follow_relock(ctx):
+    """Cached plans (and the interleaved copy) are rebuilt after a re-lock."""
+    r, c, v = gen.zipf_rows(30_000, seed=13)
+    A = build(ctx, 30_000, 30_000, [(r, c, v)])
+    x = gen.dense_x(30_000, 14)
+    for _, var in VARIANTS:
+        A.spmv_host(x, variant=var)
+    A.lock(*gen.relock_batch(30_000, 30_000, len(r), seed=15, zero_frac=0.1))
+    check_all_variants(A, x)
+
+
+def test_gather_probe(ctx):
+    r = ctx.probe_gather_rate(1 << 20, 1 << 22)
+    assert 1e9 < r < 1e13
+    with pytest.raises(sg.InvalidArgument):
+        ctx.probe_gather_rate(3, 1 << 20)
+    with pytest.raises(sg.InvalidArgument):
+        ctx.probe_gather_rate(1 << 20, 8)
+
+
 def test_spmv_laplacian_2a_full(ctx):
     """Config 2a at full size: 5-point Laplacian on 1414^2, re-lock, SpMV."""
     r, c, v = gen.laplacian_2d(1414)
