@@ -557,7 +557,51 @@ PROFILE_CASES = {
     "laplacian2d": (GRID * GRID, "laplacian"),
     "zipf1m": (1_000_000, "zipf"),
     "zipf4m": (ZIPF_N, "zipf"),
+    # lock / transpose / SpGEMM: `--reps` calls of the operation
+    "lock_zipf1m": (1_000_000, "lock"),
+    "lock_laplacian2d": (GRID * GRID, "lock"),
+    "transpose_laplacian3d": (100 ** 3, "transpose"),
+    "spgemm_laplacian3d": (100 ** 3, "spgemm"),
+    "spgemm_uniform200k": (200_000, "spgemm"),
 }
+
+
+def run_profile_op(ctx, case, n, kind, reps):
+    """lock / transpose / SpGEMM cases of run_profile_case."""
+    import spira_gb300 as sg
+    from spira_gb300 import gen, gen_device
+    ms = []
+    if kind == "lock":
+        if case == "lock_laplacian2d":
+            import torch
+            hr, hc, hv = gen.laplacian_2d(GRID)
+            r, c, v = (torch.from_numpy(hr.view(np.int32)).cuda(), torch.from_numpy(hc.view(np.int32)).cuda(),
+                       torch.from_numpy(hv).cuda())
+            m = len(hr)
+        else:
+            r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
+        for _ in range(reps + 1):
+            A = sg.Csr(ctx, n, n)
+            ctx.sync()
+            t0 = time.perf_counter()
+            A.lock_device(r, c, v, m)
+            ctx.sync()
+            ms.append((time.perf_counter() - t0) * 1e3)
+            nnz = A.nnz
+            A.close()
+    else:
+        r, c, v = gen.laplacian_3d(100) if n == 100 ** 3 else gen.uniform_rows(n, n, 8, seed=77)
+        A = sg.Csr(ctx, n, n)
+        A.lock(r, c, v)
+        nnz = A.nnz
+        for _ in range(reps + 1):
+            ctx.sync()
+            t0 = time.perf_counter()
+            B = A.transpose() if kind == "transpose" else A.spgemm(A)
+            ctx.sync()
+            ms.append((time.perf_counter() - t0) * 1e3)
+            B.close()
+    print(json.dumps({"profile_case": case, "n_rows": n, "nnz": nnz, "ms_per_call": [round(t, 3) for t in ms]}))
 
 
 def run_profile_case(args):
@@ -570,6 +614,9 @@ def run_profile_case(args):
     ctx = sg.Context(0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     n, kind = PROFILE_CASES[args.profile_case]
+    if kind in ("lock", "transpose", "spgemm"):
+        run_profile_op(ctx, args.profile_case, n, kind, args.reps)
+        return
     if kind == "zipf":
         r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
         A = sg.Csr(ctx, n, n)

@@ -44,6 +44,15 @@ __global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t
     }
 }
 
+// *unsorted = 1 if some key is greater than its successor.
+__global__ void keys_descent(const uint64_t *__restrict__ keys, uint64_t m, unsigned *__restrict__ unsorted) {
+    bool d = false;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < m;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        d |= keys[i] > keys[i + 1];
+    if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) *unsorted = 1u;
+}
+
 // flag[i] = 1 iff sorted key i is the last of its run (the last write).
 __global__ void lock_last_flags(const uint64_t *__restrict__ keys, uint64_t m, uint64_t *__restrict__ flag) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
@@ -139,6 +148,10 @@ __device__ __forceinline__ uint64_t row_of(const uint64_t *__restrict__ off, uin
     return lo;
 }
 
+// Rows of a chunk whose offsets fit in shared memory; chunks spanning more
+// rows (long runs of empty rows) search the global arrays instead.
+constexpr int MO_WIN = 1536;
+
 __global__ void __launch_bounds__(LB)
 merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
                 const double *__restrict__ vals, uint64_t n_rows, uint64_t nnz_old,
@@ -146,6 +159,7 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
                 const int64_t *__restrict__ P, const uint64_t *__restrict__ new_off,
                 uint32_t *__restrict__ out_cols, double *__restrict__ out_vals) {
     __shared__ uint64_t win[2];
+    __shared__ uint64_t s_off[MO_WIN + 1], s_new[MO_WIN + 1], s_doff[MO_WIN + 1];
     const uint64_t k0 = (uint64_t)blockIdx.x * MO_CHUNK;
     const uint64_t k1 = min(k0 + (uint64_t)MO_CHUNK, nnz_old);
     if (threadIdx.x == 0) {
@@ -154,12 +168,37 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
     }
     __syncthreads();
     const uint64_t rlo = win[0], rhi = win[1];
+    const bool local = rhi - rlo < (uint64_t)MO_WIN;
+    if (local) {
+        for (uint64_t t = threadIdx.x; t <= rhi - rlo + 1; t += LB) {
+            s_off[t] = off[rlo + t];
+            s_new[t] = new_off[rlo + t];
+            s_doff[t] = doff[rlo + t];
+        }
+    }
+    __syncthreads();
     for (uint64_t k = k0 + threadIdx.x; k < k1; k += LB) {
-        const uint64_t r = row_of(off, rlo, rhi, k);
-        const uint64_t p = k - off[r];
+        uint64_t p, ds, de, nb;
+        if (local) {
+            int lo = 0, hi = (int)(rhi - rlo);  // last t with s_off[t] <= k
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_off[mid] <= k) lo = mid;
+                else hi = mid - 1;
+            }
+            p = k - s_off[lo];
+            ds = s_doff[lo];
+            de = s_doff[lo + 1];
+            nb = s_new[lo];
+        } else {
+            const uint64_t r = row_of(off, rlo, rhi, k);
+            p = k - off[r];
+            ds = doff[r];
+            de = doff[r + 1];
+            nb = new_off[r];
+        }
         const uint32_t c = cols[k];
-        const uint64_t ds = doff[r], de = doff[r + 1];
-        uint64_t dst = new_off[r] + p;
+        uint64_t dst = nb + p;
         if (ds != de) {
             uint64_t lo = ds, hi = de;
             while (lo < hi) {
@@ -228,16 +267,61 @@ struct Delta {
     DevBuf row, col, val;
 };
 
-int sort_dedup(Ctx *c, const uint32_t *rows, const uint32_t *cols, const double *vals, uint64_t m,
-               uint64_t n_rows, uint64_t n_cols, Delta &D, cudaStream_t s) {
+// First lock (build_csr, csr_build.hpp:32-98): the CSR is the last write of
+// every key with zeros dropped. flag[i] = 1 iff sorted entry i is kept.
+__global__ void first_keep_flags(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx,
+                                 const double *__restrict__ vals, uint64_t m, uint64_t *__restrict__ flag) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        flag[i] = ((i + 1 == m || keys[i] != keys[i + 1]) && !is_zero(vals[idx[i]])) ? 1 : 0;
+}
+
+__global__ void first_gather(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx,
+                             const uint64_t *__restrict__ pos, uint64_t m, int cbits, const double *__restrict__ vals,
+                             uint32_t *__restrict__ orow, uint32_t *__restrict__ ocol, double *__restrict__ oval) {
+    const uint64_t cmask = cbits ? ((1ull << cbits) - 1) : 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t j = pos[i];
+        if (pos[i + 1] == j) continue;
+        const uint64_t k = keys[i];
+        orow[j] = (uint32_t)(k >> cbits);
+        ocol[j] = (uint32_t)(k & cmask);
+        oval[j] = vals[idx[i]];
+    }
+}
+
+// Keys (row << cbits | col) of the staged inserts sorted stably, with their
+// staging indices.
+int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, uint64_t n_rows, uint64_t n_cols,
+              DevBuf &keys, DevBuf &idx, cudaStream_t s) {
     const int cbits = bits_for(n_cols), rbits = bits_for(n_rows);
     const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
-    DevBuf keys, idx, pos;
     SPG_TRY(keys.alloc(m * sizeof(uint64_t), s));
     SPG_TRY(idx.alloc(m * sizeof(uint32_t), s));
     lock_make_keys<<<g, LB, 0, s>>>(rows, cols, m, cbits, keys.as<uint64_t>(), idx.as<uint32_t>());
     SPG_LAUNCH_CHECK();
-    SPG_TRY(radix_sort_pairs_u64(c, keys.as<uint64_t>(), idx.as<uint32_t>(), m, rbits + cbits, s));
+    // Inserts staged already in (row, col) order (row by row, ascending
+    // columns: how stencils and most assemblies insert) need no sort: the
+    // stable sort of a non-decreasing sequence is the identity.
+    DevBuf flag;
+    SPG_TRY(flag.alloc(sizeof(unsigned), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), s));
+    keys_descent<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, flag.as<unsigned>());
+    SPG_LAUNCH_CHECK();
+    unsigned unsorted = 1;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&unsorted, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (unsorted) SPG_TRY(radix_sort_pairs_u64(c, keys.as<uint64_t>(), idx.as<uint32_t>(), m, rbits + cbits, s));
+    return SPG_OK;
+}
+
+int sort_dedup(Ctx *c, const uint32_t *rows, const uint32_t *cols, const double *vals, uint64_t m,
+               uint64_t n_rows, uint64_t n_cols, Delta &D, cudaStream_t s) {
+    const int cbits = bits_for(n_cols);
+    const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
+    DevBuf keys, idx, pos;
+    SPG_TRY(sort_keys(c, rows, cols, m, n_rows, n_cols, keys, idx, s));
     SPG_TRY(pos.alloc((m + 1) * sizeof(uint64_t), s));
     lock_last_flags<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, pos.as<uint64_t>());
     SPG_LAUNCH_CHECK();
@@ -260,6 +344,49 @@ int row_offsets(Ctx *c, const uint32_t *srows, uint64_t u, uint64_t n_rows, DevB
     offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
         srows, u, n_rows, doff.as<uint64_t>());
     SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+// First lock: sort, keep the last write of every key unless it is zero, and
+// take the offsets from the kept rows.
+int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const double *vals, uint64_t m,
+               cudaStream_t s) {
+    const uint64_t n = A->n_rows;
+    const int cbits = bits_for(A->n_cols);
+    DevBuf keys, idx, pos, orow, out_cols, out_vals, new_off;
+    uint64_t nnz = 0;
+    if (m) {
+        const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
+        SPG_TRY(sort_keys(c, rows, cols, m, n, A->n_cols, keys, idx, s));
+        SPG_TRY(pos.alloc((m + 1) * sizeof(uint64_t), s));
+        first_keep_flags<<<g, LB, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), vals, m, pos.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+        SPG_TRY(exclusive_scan_u64(c, pos.as<uint64_t>(), m, pos.as<uint64_t>() + m, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(&nnz, pos.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
+        SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
+        SPG_TRY(orow.alloc((nnz ? nnz : 1) * sizeof(uint32_t), s));
+        first_gather<<<g, LB, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), pos.as<uint64_t>(), m, cbits, vals,
+                                      orow.as<uint32_t>(), out_cols.as<uint32_t>(), out_vals.as<double>());
+        SPG_LAUNCH_CHECK();
+    } else {
+        SPG_TRY(out_cols.alloc(csr_alloc_elems(0) * sizeof(uint32_t), s));
+        SPG_TRY(out_vals.alloc(csr_alloc_elems(0) * sizeof(double), s));
+    }
+    SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
+    offsets_from_sorted_rows<<<grid_for(n + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+        orow.as<uint32_t>(), nnz, n, new_off.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    A->invalidate_derived();
+    A->off = std::move(new_off);
+    A->cols = std::move(out_cols);
+    A->vals = std::move(out_vals);
+    A->nnz = nnz;
+    A->capacity = nnz;  // build_csr: exact
+    A->built = true;
+    A->may_have_zeros = false;
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
     return SPG_OK;
 }
 
@@ -286,6 +413,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     const uint64_t n = A->n_rows;
     const bool has_old = A->built;
     if (has_old && m == 0) return SPG_OK;  // no dirty row: Spira's merge leaves the CSR as it is
+    if (!has_old) return first_lock(c, A, rows, cols, vals, m, s);
 
     Delta D;
     if (m) SPG_TRY(sort_dedup(c, rows, cols, vals, m, n, A->n_cols, D, s));

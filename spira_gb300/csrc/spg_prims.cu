@@ -171,6 +171,10 @@ int exclusive_scan_i64(Ctx *c, int64_t *d, uint64_t n, cudaStream_t s) {
 // [w*512, w*512+512) of the tile and walks them in order (iteration-major,
 // lane-minor), so the within-tile rank of every key is its order among equal
 // digits: stability follows, and with it the insertion-order tie-break.
+// The upsweep counts digits with shared-memory atomics; the scatter ranks
+// equal digits within a warp with match.any. The scatter first places the tile in shared memory in digit order, then
+// writes each digit's run to its global position with consecutive threads
+// on consecutive addresses, so the writes coalesce.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -194,12 +198,23 @@ radix_upsweep(const uint64_t *__restrict__ keys, uint64_t n, int shift, unsigned
     for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&cnt[0][0])[i] = 0;
     __syncthreads();
     const uint64_t base = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)warp * (RS_ITERS * 32);
-#pragma unroll 4
+    unsigned dig[RS_ITERS];
+#pragma unroll
     for (int j = 0; j < RS_ITERS; ++j) {
-        uint64_t k = base + j * 32 + lane;
-        unsigned d = (k < n) ? (unsigned)((keys[k] >> shift) & 0xFF) : RS_RADIX;
-        unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (d < RS_RADIX && (peers & lanemask_lt()) == 0) cnt[warp][d] += __popc(peers);
+        const uint64_t k = base + j * 32 + lane;
+        dig[j] = (k < n) ? (unsigned)((keys[k] >> shift) & 0xFF) : RS_RADIX;
+    }
+    // counts only: shared-memory atomics, with one add for a warp whose 32
+    // digits agree (sorted or skewed inputs would otherwise serialise)
+#pragma unroll
+    for (int j = 0; j < RS_ITERS; ++j) {
+        const unsigned d = dig[j];
+        const unsigned d0 = __shfl_sync(0xffffffffu, d, 0);
+        if (__all_sync(0xffffffffu, d == d0)) {
+            if (lane == 0 && d0 < RS_RADIX) cnt[warp][d0] += 32;
+        } else if (d < RS_RADIX) {
+            atomicAdd(&cnt[warp][d], 1u);
+        }
         __syncwarp();
     }
     __syncthreads();
@@ -211,61 +226,99 @@ radix_upsweep(const uint64_t *__restrict__ keys, uint64_t n, int shift, unsigned
     }
 }
 
+// Shared memory of radix_scatter (dynamic: above the 48 KB static limit).
+struct ScatterSmem {
+    uint64_t key[RS_TILE];
+    uint32_t val[RS_TILE];
+    unsigned long long gbase[RS_RADIX];  // global start of each digit's run of this tile
+    unsigned cnt[RS_WARPS][RS_RADIX];    // per-warp digit counts, then per-warp offsets
+    unsigned loc[RS_RADIX];              // tile-local start of each digit's run
+    unsigned wsum[RS_WARPS];
+};
+
+static_assert(RS_BLOCK == RS_RADIX, "one thread per digit in the tile-local scan");
+
 __global__ void __launch_bounds__(RS_BLOCK)
 radix_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
               uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, uint64_t n,
               int shift, unsigned n_tiles, const unsigned long long *__restrict__ offs /* scanned */) {
-    __shared__ unsigned cnt[RS_WARPS][RS_RADIX];
-    __shared__ unsigned long long gbase[RS_RADIX];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&cnt[0][0])[i] = 0;
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK)
-        gbase[d] = offs[(uint64_t)d * n_tiles + blockIdx.x];
+    const int t = threadIdx.x;
+    for (int i = t; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&S.cnt[0][0])[i] = 0;
+    S.gbase[t] = offs[(uint64_t)t * n_tiles + blockIdx.x];
     __syncthreads();
 
-    const uint64_t base = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)warp * (RS_ITERS * 32);
+    const uint64_t tile0 = (uint64_t)blockIdx.x * RS_TILE;
+    const uint64_t base = tile0 + (uint64_t)warp * (RS_ITERS * 32);
     uint64_t key[RS_ITERS];
-    uint32_t val[RS_ITERS];
     unsigned rank[RS_ITERS];
 #pragma unroll
     for (int j = 0; j < RS_ITERS; ++j) {
-        uint64_t k = base + j * 32 + lane;
+        const uint64_t k = base + j * 32 + lane;
         key[j] = (k < n) ? keys_in[k] : 0;
-        val[j] = (k < n) ? vals_in[k] : 0;
     }
+    // rank of each key among the equal digits before it in the warp's order
 #pragma unroll
     for (int j = 0; j < RS_ITERS; ++j) {
-        uint64_t k = base + j * 32 + lane;
-        unsigned d = (k < n) ? (unsigned)((key[j] >> shift) & 0xFF) : RS_RADIX;
-        unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint64_t k = base + j * 32 + lane;
+        const bool ok = k < n;
+        const unsigned valid = __ballot_sync(0xffffffffu, ok);
+        rank[j] = 0;
+        if (!valid) continue;
+        const unsigned d = ok ? (unsigned)((key[j] >> shift) & 0xFF) : RS_RADIX;
+        const unsigned peers = __match_any_sync(0xffffffffu, d) & valid;
         unsigned before = 0;
-        if (d < RS_RADIX) before = cnt[warp][d];
+        if (ok) before = S.cnt[warp][d];
         __syncwarp();
         rank[j] = before + __popc(peers & lanemask_lt());
-        if (d < RS_RADIX && (peers & lanemask_lt()) == 0) cnt[warp][d] = before + __popc(peers);
+        if (ok && (peers & lanemask_lt()) == 0) S.cnt[warp][d] = before + __popc(peers);
         __syncwarp();
     }
     __syncthreads();
-    // Exclusive prefix over warps for every digit (warp order = key order).
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) {
-        unsigned s = 0;
+    // digit t: exclusive prefix over warps (warp order = key order), then an
+    // exclusive scan of the tile's digit totals
+    unsigned tot = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) {
-            unsigned t = cnt[w][d];
-            cnt[w][d] = s;
-            s += t;
+    for (int w = 0; w < RS_WARPS; ++w) {
+        const unsigned c = S.cnt[w][t];
+        S.cnt[w][t] = tot;
+        tot += c;
+    }
+    unsigned inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) S.wsum[warp] = inc;
+    __syncthreads();
+    unsigned wpre = 0;
+    for (int w = 0; w < warp; ++w) wpre += S.wsum[w];
+    S.loc[t] = wpre + inc - tot;
+    __syncthreads();
+    // place the tile in digit order in shared memory
+#pragma unroll
+    for (int j = 0; j < RS_ITERS; ++j) {
+        const uint64_t k = base + j * 32 + lane;
+        if (k < n) {
+            const unsigned d = (unsigned)((key[j] >> shift) & 0xFF);
+            const unsigned p = S.loc[d] + S.cnt[warp][d] + rank[j];
+            S.key[p] = key[j];
+            S.val[p] = vals_in[k];
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int j = 0; j < RS_ITERS; ++j) {
-        uint64_t k = base + j * 32 + lane;
-        if (k < n) {
-            unsigned d = (unsigned)((key[j] >> shift) & 0xFF);
-            unsigned long long pos = gbase[d] + cnt[warp][d] + rank[j];
-            keys_out[pos] = key[j];
-            vals_out[pos] = val[j];
-        }
+    // write each digit's run to its global position: consecutive threads,
+    // consecutive addresses
+    const unsigned tile_n = (unsigned)min((uint64_t)RS_TILE, n - tile0);
+    for (unsigned i = t; i < tile_n; i += RS_BLOCK) {
+        const uint64_t kk = S.key[i];
+        const unsigned d = (unsigned)((kk >> shift) & 0xFF);
+        const unsigned long long pos = S.gbase[d] + (i - S.loc[d]);
+        keys_out[pos] = kk;
+        vals_out[pos] = S.val[i];
     }
 }
 
@@ -293,6 +346,8 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
     uint64_t *kin = d_keys, *kout = kalt.as<uint64_t>();
     uint32_t *vin = d_vals, *vout = valt.as<uint32_t>();
     const int passes = (key_bits + 7) / 8;
+    SPG_CUDA_TRY(cudaFuncSetAttribute(radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(ScatterSmem)));
     for (int p = 0; p < passes; ++p) {
         const int shift = p * 8;
         radix_upsweep<<<n_tiles, RS_BLOCK, 0, s>>>(kin, n, shift, n_tiles, hist.as<unsigned>());
@@ -301,8 +356,8 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
             hist.as<unsigned>(), offs.as<unsigned long long>(), hist_n);
         SPG_LAUNCH_CHECK();
         SPG_TRY(exclusive_scan_u64(c, offs.as<uint64_t>(), hist_n, nullptr, s));
-        radix_scatter<<<n_tiles, RS_BLOCK, 0, s>>>(kin, vin, kout, vout, n, shift, n_tiles,
-                                                   offs.as<unsigned long long>());
+        radix_scatter<<<n_tiles, RS_BLOCK, sizeof(ScatterSmem), s>>>(kin, vin, kout, vout, n, shift, n_tiles,
+                                                                     offs.as<unsigned long long>());
         SPG_LAUNCH_CHECK();
         std::swap(kin, kout);
         std::swap(vin, vout);

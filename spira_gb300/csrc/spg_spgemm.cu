@@ -7,16 +7,23 @@
 // the left-to-right sum over ascending k of the rounded products, starting
 // from 0.0, and exact-zero sums are dropped.
 //
-// GPU formulation (expand - sort - compress):
-//   1. products per row of A, scanned into per-row product offsets;
-//   2. expand every product (key = i << cbits | j, value = a_ik * b_kj
-//      rounded) in (row, A-entry, B-entry) order;
-//   3. stable radix sort of the keys with the product index as payload:
-//      equal (i, j) keep ascending k;
-//   4. sum each run left to right with separate round-to-nearest multiply and
-//      add (__dmul_rn / __dadd_rn, never contracted), drop zero sums, compact.
-// Values match Spira built without FMA contraction (its x86-64 build) bit for
-// bit; structure is exact.
+// GPU formulation. Products per row of A are counted and scanned; every row
+// owns a scratch region of its product count. Two paths fill the regions:
+//
+//   light rows (at most MG_RMAX entries in A's row and MG_PMAX products):
+//   one thread merges the row's B rows (each sorted by column) as a k-way
+//   merge on the column, taking equal columns in ascending A-entry order, so
+//   every C(i, j) is summed in Spira's order; no global sort at all.
+//
+//   heavy rows (expand - sort - compress): expand the row's products (key =
+//   i << cbits | j) in (row, A-entry, B-entry) order, stable radix sort with
+//   the product index as payload (equal (i, j) keep ascending k), sum each
+//   run left to right.
+//
+// Both use separate round-to-nearest multiply and add (__dmul_rn /
+// __dadd_rn, never contracted) from 0.0 and drop exact-zero sums; a final
+// pass compacts the regions into C. Values match Spira built without FMA
+// contraction (its x86-64 build) bit for bit; structure is exact.
 #include "spg_internal.cuh"
 
 namespace spg {
@@ -24,23 +31,162 @@ namespace {
 
 constexpr int GB = 256;
 
+// Products per row of A (thread per row); entry m is 0.
 __global__ void sg_row_products(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols,
                                 const uint64_t *__restrict__ boff, uint64_t m, uint64_t *__restrict__ cnt) {
-    const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w > m) return;
-    if (w == m) {
-        if (lane == 0) cnt[m] = 0;
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i > m) return;
+    uint64_t s = 0;
+    if (i < m)
+        for (uint64_t ka = aoff[i]; ka < aoff[i + 1]; ++ka) {
+            const uint32_t k = acols[ka];
+            s += boff[k + 1] - boff[k];
+        }
+    cnt[i] = s;
+}
+
+constexpr int MG_RSMALL = 8;      // light rows: <= 8 A entries (cursors in registers) ...
+constexpr int MG_RMAX = 32;       // ... or <= 32 (cursors in local memory)
+constexpr uint64_t MG_PMAX = 4096;  // and at most this many products
+
+__device__ __forceinline__ bool mg_light(uint64_t r, uint64_t p) { return r <= MG_RMAX && p <= MG_PMAX; }
+
+// Product counts of the heavy rows only (0 for light rows); entry m is 0.
+__global__ void sg_heavy_products(const uint64_t *__restrict__ aoff, const uint64_t *__restrict__ pofs, uint64_t m,
+                                  uint64_t *__restrict__ hp) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= m; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i == m) {
+            hp[m] = 0;
+            continue;
+        }
+        const uint64_t p = pofs[i + 1] - pofs[i];
+        hp[i] = mg_light(aoff[i + 1] - aoff[i], p) ? 0 : p;
+    }
+}
+
+// Light rows, one thread per row: k-way merge of the B rows named by the
+// row's A entries. Each B row is strictly increasing in column, so every list
+// holds at most one product of a given column; taking the smallest head
+// column and then the lists whose head equals it in ascending list (= A
+// entry = k) order sums C(i, j) exactly as Spira's acc[j] += a_ik * b_kj.
+// Kept entries go to the row's scratch region at pofs[i]; rowcnt[i] = count.
+// R = MG_RSMALL handles rows with r <= R and sets rowcnt = 0 for every other
+// row; R = MG_RMAX handles MG_RSMALL < r <= MG_RMAX.
+template <int R>
+__global__ void __launch_bounds__(128)
+sg_merge_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols, const double *__restrict__ avals,
+              const uint64_t *__restrict__ boff, const uint32_t *__restrict__ bcols, const double *__restrict__ bvals,
+              uint64_t m, const uint64_t *__restrict__ pofs, uint32_t *__restrict__ tcols,
+              double *__restrict__ tvals, uint64_t *__restrict__ rowcnt) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const uint64_t ab = aoff[i], r = aoff[i + 1] - ab;
+    const uint64_t base = pofs[i], P = pofs[i + 1] - base;
+    const bool mine = mg_light(r, P) && (R == MG_RSMALL ? r <= (uint64_t)R : r > (uint64_t)MG_RSMALL);
+    if (!mine) {
+        if (R == MG_RSMALL) rowcnt[i] = 0;
         return;
     }
-    uint64_t s = 0;
-    for (uint64_t ka = aoff[w] + lane; ka < aoff[w + 1]; ka += 32) {
-        const uint32_t k = acols[ka];
-        s += boff[k + 1] - boff[k];
-    }
+    uint64_t cur[R];
+    uint32_t left[R], head[R];
+    double a[R];
 #pragma unroll
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) cnt[w] = s;
+    for (int t = 0; t < R; ++t) {
+        cur[t] = 0;
+        left[t] = 0;
+        head[t] = 0;
+        a[t] = 0.0;
+        if ((uint64_t)t < r) {
+            const uint32_t k = acols[ab + t];
+            const uint64_t b0 = boff[k];
+            cur[t] = b0;
+            left[t] = (uint32_t)(boff[k + 1] - b0);
+            a[t] = avals[ab + t];
+            if (left[t]) head[t] = bcols[b0];
+        }
+    }
+    constexpr uint64_t NONE = 1ull << 32;
+    uint64_t cnt = 0;
+    while (true) {
+        uint64_t j = NONE;
+#pragma unroll
+        for (int t = 0; t < R; ++t)
+            if (left[t] && head[t] < j) j = head[t];
+        if (j == NONE) break;
+        double acc = 0.0;  // ValueTraits zero; acc[j] default-constructs to V{}
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+            if (left[t] && head[t] == j) {
+                acc = __dadd_rn(acc, __dmul_rn(a[t], bvals[cur[t]]));
+                ++cur[t];
+                if (--left[t]) head[t] = bcols[cur[t]];
+            }
+        }
+        if (acc != 0.0) {  // spgemm.hpp:44: v != V{}
+            tcols[base + cnt] = (uint32_t)j;
+            tvals[base + cnt] = acc;
+            ++cnt;
+        }
+    }
+    rowcnt[i] = cnt;
+}
+
+// Heavy rows' results (compacted, sorted by (row, col)) into their rows'
+// scratch regions; the first entry of each row sets its count.
+__global__ void sg_place_heavy(const uint32_t *__restrict__ crow, const uint32_t *__restrict__ ccol,
+                               const double *__restrict__ cval, uint64_t nh, const uint64_t *__restrict__ pofs,
+                               uint32_t *__restrict__ tcols, double *__restrict__ tvals,
+                               uint64_t *__restrict__ rowcnt) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nh; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = crow[e];
+        uint64_t lo = 0, hi = e;  // first entry of row i
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (crow[mid] < i) lo = mid + 1;
+            else hi = mid;
+        }
+        const uint64_t rank = e - lo;
+        tcols[pofs[i] + rank] = ccol[e];
+        tvals[pofs[i] + rank] = cval[e];
+        if (rank == 0) {
+            uint64_t l2 = e, h2 = nh;  // one past the last entry of row i
+            while (l2 < h2) {
+                const uint64_t mid = (l2 + h2) >> 1;
+                if (crow[mid] <= i) l2 = mid + 1;
+                else h2 = mid;
+            }
+            rowcnt[i] = l2 - e;
+        }
+    }
+}
+
+// C from the scratch regions. Block b writes C positions [coff[r0], coff[r1])
+// of its rows r0..r1-1 with consecutive threads on consecutive positions; a
+// position's row is found by binary search in the block's copy of coff.
+constexpr int CP_ROWS = 256;
+
+__global__ void __launch_bounds__(CP_ROWS)
+sg_compact(const uint64_t *__restrict__ pofs, const uint64_t *__restrict__ coff, uint64_t m,
+           const uint32_t *__restrict__ tcols, const double *__restrict__ tvals, uint32_t *__restrict__ ccols,
+           double *__restrict__ cvals) {
+    __shared__ uint64_t soff[CP_ROWS + 1], ssrc[CP_ROWS];
+    const uint64_t r0 = (uint64_t)blockIdx.x * CP_ROWS;
+    const int nr = (int)min((uint64_t)CP_ROWS, m - r0);
+    for (int t = threadIdx.x; t <= nr; t += blockDim.x) soff[t] = coff[r0 + t];
+    for (int t = threadIdx.x; t < nr; t += blockDim.x) ssrc[t] = pofs[r0 + t];
+    __syncthreads();
+    const uint64_t q1 = soff[nr];
+    for (uint64_t q = soff[0] + threadIdx.x; q < q1; q += blockDim.x) {
+        int lo = 0, hi = nr;  // last t with soff[t] <= q
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (soff[mid] <= q) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t src = ssrc[lo] + (q - soff[lo]);
+        ccols[q] = tcols[src];
+        cvals[q] = tvals[src];
+    }
 }
 
 __global__ void sg_expand(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols,
@@ -52,6 +198,7 @@ __global__ void sg_expand(const uint64_t *__restrict__ aoff, const uint32_t *__r
     const int lane = threadIdx.x & 31;
     if (w >= m) return;
     uint64_t base = pofs[w];
+    if (pofs[w + 1] == base) return;  // no products here (or a row handled by the merge path)
     const uint64_t rk = w << cbits;
     for (uint64_t ka = aoff[w]; ka < aoff[w + 1]; ++ka) {
         const uint32_t k = acols[ka];
@@ -104,26 +251,69 @@ __global__ void sg_write(const uint64_t *__restrict__ begin, const uint64_t *__r
     }
 }
 
-__global__ void sg_offsets(const uint32_t *__restrict__ srows, uint64_t u, uint64_t n_rows,
-                           uint64_t *__restrict__ off) {
-    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r <= n_rows;
-         r += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t lo = 0, hi = u;
-        while (lo < hi) {
-            const uint64_t mid = (lo + hi) >> 1;
-            if ((uint64_t)srows[mid] < r) lo = mid + 1;
-            else hi = mid;
-        }
-        off[r] = lo;
-    }
-}
-
 uint64_t read_u64(const uint64_t *d, cudaStream_t s, int *rc) {
     uint64_t h = 0;
     cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) *rc = set_error(SPG_ERR_CUDA, "spgemm: %s", cudaGetErrorString(e));
     return h;
+}
+
+// Expand - sort - compress for the rows the merge kernels leave (more than
+// MG_RMAX A entries or more than MG_PMAX products); results go to the rows'
+// scratch regions and counts.
+int spgemm_heavy_rows(Ctx *c, const Csr *A, const Csr *B, const uint64_t *pofs, uint32_t *tcols, double *tvals,
+                      uint64_t *rowcnt, int rbits, int cbits, cudaStream_t s) {
+    const uint64_t m = A->n_rows;
+    const unsigned gmax = (unsigned)c->n_sms * 32;
+    int rc = SPG_OK;
+    DevBuf hp;
+    SPG_TRY(hp.alloc((m + 1) * sizeof(uint64_t), s));
+    sg_heavy_products<<<grid_for(m + 1, GB, gmax), GB, 0, s>>>(A->d_off(), pofs, m, hp.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_u64(c, hp.as<uint64_t>(), m + 1, nullptr, s));
+    const uint64_t P = read_u64(hp.as<uint64_t>() + m, s, &rc);
+    SPG_TRY(rc);
+    if (P == 0) return SPG_OK;
+    DevBuf key, idx, pval, flag, begin, sum, keep, crow, ccol, cval;
+    SPG_TRY(key.alloc(P * sizeof(uint64_t), s));
+    SPG_TRY(idx.alloc(P * sizeof(uint32_t), s));
+    SPG_TRY(pval.alloc(P * sizeof(double), s));
+    sg_expand<<<grid_for(m * 32, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), B->d_off(), B->d_cols(),
+                                                 B->d_vals(), m, cbits, hp.as<uint64_t>(), key.as<uint64_t>(),
+                                                 idx.as<uint32_t>(), pval.as<double>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(radix_sort_pairs_u64(c, key.as<uint64_t>(), idx.as<uint32_t>(), P, rbits + cbits, s));
+    SPG_TRY(flag.alloc((P + 1) * sizeof(uint64_t), s));
+    sg_run_flags<<<grid_for(P, GB, gmax), GB, 0, s>>>(key.as<uint64_t>(), P, flag.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_u64(c, flag.as<uint64_t>(), P, flag.as<uint64_t>() + P, s));
+    const uint64_t U = read_u64(flag.as<uint64_t>() + P, s, &rc);
+    SPG_TRY(rc);
+    SPG_TRY(begin.alloc((U + 1) * sizeof(uint64_t), s));
+    sg_run_begins<<<grid_for(P, GB, gmax), GB, 0, s>>>(key.as<uint64_t>(), flag.as<uint64_t>(), P, U,
+                                                      begin.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(sum.alloc(U * sizeof(double), s));
+    SPG_TRY(keep.alloc((U + 1) * sizeof(uint64_t), s));
+    sg_run_sums<<<grid_for(U, GB, gmax), GB, 0, s>>>(begin.as<uint64_t>(), idx.as<uint32_t>(), pval.as<double>(), U,
+                                                    sum.as<double>(), keep.as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_u64(c, keep.as<uint64_t>(), U, keep.as<uint64_t>() + U, s));
+    const uint64_t nh = read_u64(keep.as<uint64_t>() + U, s, &rc);
+    SPG_TRY(rc);
+    if (nh == 0) return SPG_OK;
+    SPG_TRY(crow.alloc(nh * sizeof(uint32_t), s));
+    SPG_TRY(ccol.alloc(nh * sizeof(uint32_t), s));
+    SPG_TRY(cval.alloc(nh * sizeof(double), s));
+    sg_write<<<grid_for(U, GB, gmax), GB, 0, s>>>(begin.as<uint64_t>(), key.as<uint64_t>(), sum.as<double>(),
+                                                 keep.as<uint64_t>(), U, cbits, ccol.as<uint32_t>(), cval.as<double>(),
+                                                 crow.as<uint32_t>());
+    SPG_LAUNCH_CHECK();
+    sg_place_heavy<<<grid_for(nh, GB, gmax), GB, 0, s>>>(crow.as<uint32_t>(), ccol.as<uint32_t>(),
+                                                        cval.as<double>(), nh, pofs, tcols, tvals, rowcnt);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
 }
 
 }  // namespace
@@ -135,7 +325,7 @@ int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
     int rc = SPG_OK;
     DevBuf pofs;
     SPG_TRY(pofs.alloc((m + 1) * sizeof(uint64_t), s));
-    sg_row_products<<<grid_for((m + 1) * 32, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), B->d_off(), m,
+    sg_row_products<<<grid_for(m + 1, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), B->d_off(), m,
                                                              pofs.as<uint64_t>());
     SPG_LAUNCH_CHECK();
     SPG_TRY(exclusive_scan_u64(c, pofs.as<uint64_t>(), m + 1, nullptr, s));
@@ -143,49 +333,37 @@ int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
     SPG_TRY(rc);
     if (P >= (1ull << 32))
         return set_error(SPG_ERR_UNSUPPORTED, "spgemm: %llu products exceed 2^32-1", (unsigned long long)P);
-    DevBuf key, idx, pval, flag, begin, sum, keep, out_off, out_cols, out_vals, crow;
-    uint64_t U = 0, nnz = 0;
-    if (P) {
-        SPG_TRY(key.alloc(P * sizeof(uint64_t), s));
-        SPG_TRY(idx.alloc(P * sizeof(uint32_t), s));
-        SPG_TRY(pval.alloc(P * sizeof(double), s));
-        sg_expand<<<grid_for(m * 32, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), B->d_off(),
-                                                     B->d_cols(), B->d_vals(), m, cbits, pofs.as<uint64_t>(),
-                                                     key.as<uint64_t>(), idx.as<uint32_t>(), pval.as<double>());
-        SPG_LAUNCH_CHECK();
-        SPG_TRY(radix_sort_pairs_u64(c, key.as<uint64_t>(), idx.as<uint32_t>(), P, rbits + cbits, s));
-        SPG_TRY(flag.alloc((P + 1) * sizeof(uint64_t), s));
-        sg_run_flags<<<grid_for(P, GB, gmax), GB, 0, s>>>(key.as<uint64_t>(), P, flag.as<uint64_t>());
-        SPG_LAUNCH_CHECK();
-        SPG_TRY(exclusive_scan_u64(c, flag.as<uint64_t>(), P, flag.as<uint64_t>() + P, s));
-        U = read_u64(flag.as<uint64_t>() + P, s, &rc);
-        SPG_TRY(rc);
-        SPG_TRY(begin.alloc((U + 1) * sizeof(uint64_t), s));
-        sg_run_begins<<<grid_for(P, GB, gmax), GB, 0, s>>>(key.as<uint64_t>(), flag.as<uint64_t>(), P, U,
-                                                          begin.as<uint64_t>());
-        SPG_LAUNCH_CHECK();
-        SPG_TRY(sum.alloc(U * sizeof(double), s));
-        SPG_TRY(keep.alloc((U + 1) * sizeof(uint64_t), s));
-        sg_run_sums<<<grid_for(U, GB, gmax), GB, 0, s>>>(begin.as<uint64_t>(), idx.as<uint32_t>(),
-                                                        pval.as<double>(), U, sum.as<double>(), keep.as<uint64_t>());
-        SPG_LAUNCH_CHECK();
-        SPG_TRY(exclusive_scan_u64(c, keep.as<uint64_t>(), U, keep.as<uint64_t>() + U, s));
-        nnz = read_u64(keep.as<uint64_t>() + U, s, &rc);
-        SPG_TRY(rc);
-    }
+    // out_off holds the per-row kept counts, then (scanned) C's offsets
+    DevBuf tcols, tvals, out_off, out_cols, out_vals;
     SPG_TRY(out_off.alloc(csr_off_elems(m) * sizeof(uint64_t), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(out_off.ptr, 0, csr_off_elems(m) * sizeof(uint64_t), s));
+    if (P) {
+        SPG_TRY(tcols.alloc(P * sizeof(uint32_t), s));
+        SPG_TRY(tvals.alloc(P * sizeof(double), s));
+        sg_merge_rows<MG_RSMALL><<<grid_for(m, 128), 128, 0, s>>>(
+            A->d_off(), A->d_cols(), A->d_vals(), B->d_off(), B->d_cols(), B->d_vals(), m, pofs.as<uint64_t>(),
+            tcols.as<uint32_t>(), tvals.as<double>(), out_off.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+        sg_merge_rows<MG_RMAX><<<grid_for(m, 128), 128, 0, s>>>(
+            A->d_off(), A->d_cols(), A->d_vals(), B->d_off(), B->d_cols(), B->d_vals(), m, pofs.as<uint64_t>(),
+            tcols.as<uint32_t>(), tvals.as<double>(), out_off.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+        SPG_TRY(spgemm_heavy_rows(c, A, B, pofs.as<uint64_t>(), tcols.as<uint32_t>(), tvals.as<double>(),
+                                  out_off.as<uint64_t>(), rbits, cbits, s));
+    }
+    SPG_TRY(exclusive_scan_u64(c, out_off.as<uint64_t>(), m + 1, nullptr, s));
+    const uint64_t nnz = read_u64(out_off.as<uint64_t>() + m, s, &rc);
+    SPG_TRY(rc);
     SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
-    SPG_TRY(crow.alloc((nnz ? nnz : 1) * sizeof(uint32_t), s));
-    if (U) {
-        sg_write<<<grid_for(U, GB, gmax), GB, 0, s>>>(begin.as<uint64_t>(), key.as<uint64_t>(), sum.as<double>(),
-                                                     keep.as<uint64_t>(), U, cbits, out_cols.as<uint32_t>(),
-                                                     out_vals.as<double>(), crow.as<uint32_t>());
+    if (nnz) {
+        sg_compact<<<grid_for(m, CP_ROWS), CP_ROWS, 0, s>>>(pofs.as<uint64_t>(), out_off.as<uint64_t>(), m,
+                                                           tcols.as<uint32_t>(), tvals.as<double>(),
+                                                           out_cols.as<uint32_t>(), out_vals.as<double>());
         SPG_LAUNCH_CHECK();
     }
-    sg_offsets<<<grid_for(m + 1, GB, gmax), GB, 0, s>>>(crow.as<uint32_t>(), nnz, m, out_off.as<uint64_t>());
-    SPG_LAUNCH_CHECK();
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    (void)gmax;
     Cm->invalidate_derived();
     Cm->n_rows = m;
     Cm->n_cols = n;

@@ -89,6 +89,20 @@ def test_lock_laplacian_relock_matches_oracle(ctx):
     assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(r, c, v), b]))
 
 
+def test_lock_presorted_input_with_duplicates(ctx):
+    """Inserts already in (row, col) order skip the sort; duplicates still
+    resolve to the last write and a last zero still deletes."""
+    rows = np.array([0, 0, 0, 1, 1, 3, 3, 3], np.uint32)
+    cols = np.array([1, 1, 2, 0, 0, 0, 5, 5], np.uint32)
+    vals = np.array([1.0, 2.0, 3.0, 4.0, 0.0, 7.0, -1.0, 9.0])
+    A = gpu_lock(ctx, 4, 6, [(rows, cols, vals)])
+    assert_csr_equal(A.download(), oracle.lock_epochs(4, 6, [(rows, cols, vals)]))
+    # a sorted second epoch merges too
+    b = (np.array([0, 2, 3], np.uint32), np.array([2, 2, 5], np.uint32), np.array([0.0, 5.0, 8.0]))
+    A.lock(*b)
+    assert_csr_equal(A.download(), oracle.lock_epochs(4, 6, [(rows, cols, vals), b]))
+
+
 def test_lock_zipf_long_rows(ctx):
     r, c, v = gen.zipf_rows(100_000, seed=9)
     b = gen.relock_batch(100_000, 100_000, len(r), seed=10, zero_frac=0.05)

@@ -98,6 +98,24 @@ def test_spgemm_cancellation_and_rectangular(ctx):
     assert_csr_equal(Cm.download(), oracle.spgemm(A.download(), B.download()))
 
 
+def test_spgemm_every_row_class(ctx):
+    """Rows for each SpGEMM path: merge with <= 8 A entries, merge with 9..32,
+    expand-sort for > 32 entries and for > 4096 products; exact cancellations
+    (integer values) included. Bit-exact against the oracle."""
+    n = 3000
+    lengths = np.array([0, 1, 3, 8, 9, 20, 32, 33, 60, 5] * (n // 10), np.int64)
+    lengths[7::50] = 2000  # long rows: as B rows they push products past 4096
+    rows = np.repeat(np.arange(n, dtype=np.uint32), lengths)
+    ctr = np.arange(len(rows), dtype=np.uint64)
+    cols = gen.below(gen.hash3(5, 1, ctr), n)
+    vals = (gen.below(gen.hash3(5, 2, ctr), 7).astype(np.int64) - 3).astype(np.float64)
+    vals[::5] = gen.sym_unit(gen.hash3(5, 3, ctr[::5]))
+    A = locked(ctx, n, n, rows, cols, vals)
+    H = A.download()
+    Cm = A.spgemm(A)
+    assert_csr_equal(Cm.download(), oracle.spgemm(H, H))
+
+
 def test_spgemm_errors(ctx):
     A = locked(ctx, 3, 4, np.array([0], np.uint32), np.array([1], np.uint32), np.array([1.0]))
     B = sg.Csr(ctx, 3, 3)
