@@ -44,13 +44,172 @@ __global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t
     }
 }
 
-// *unsorted = 1 if some key is greater than its successor.
-__global__ void keys_descent(const uint64_t *__restrict__ keys, uint64_t m, unsigned *__restrict__ unsorted) {
-    bool d = false;
+// flags[0] = 1 if some key is greater than its successor (not sorted);
+// flags[1] = 1 if some row is greater than its successor (rows not grouped).
+__global__ void keys_descent(const uint64_t *__restrict__ keys, uint64_t m, int cbits, unsigned *__restrict__ flags) {
+    bool d = false, g = false;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < m;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        d |= keys[i] > keys[i + 1];
-    if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) *unsorted = 1u;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = keys[i], b = keys[i + 1];
+        d |= a > b;
+        g |= (a >> cbits) > (b >> cbits);
+    }
+    const bool wd = __any_sync(0xffffffffu, d), wg = __any_sync(0xffffffffu, g);
+    if ((threadIdx.x & 31) == 0) {
+        if (wd) flags[0] = 1u;
+        if (wg) flags[1] = 1u;
+    }
+}
+
+// Row-grouped inserts (rows non-decreasing, columns in any order): sort each
+// row's entries by column in shared memory, tile by tile. Tile t holds the
+// rows whose first entry lies in [t*TS_SPAN, (t+1)*TS_SPAN): its entries
+// [start_t, start_{t+1}) are contiguous and already in row order, so sorting
+// inside the tile by (row, column), stably, puts them in their final global
+// places. The sort is an LSD radix sort (8-bit digits) of a permutation over
+// the composite key (row - first row of the tile, column). Two launches
+// share the tiles: tiles of at most TS_SMALL entries (the common case; three
+// blocks per SM) and tiles of up to TS_MAX (one holding a long row; one block
+// per SM). A tile longer than TS_MAX (a row of more than ~10 000 entries)
+// sets *overflow and the caller sorts globally instead.
+constexpr int TS_SPAN = 2048;
+constexpr int TS_SMALL = 4096;
+constexpr int TS_MAX = 12288;
+constexpr int TS_THREADS_SMALL = 512;
+constexpr int TS_THREADS_LARGE = 1024;
+
+template <int MAXE, int WARPS>
+struct TileSortSmem {
+    uint32_t col[MAXE];
+    uint32_t seg[MAXE];
+    uint16_t perm[2][MAXE];
+    unsigned cnt[WARPS][256];
+    unsigned loc[256];
+    unsigned wsum[8];
+    uint64_t bounds[2];  // first row of this tile and of the next
+};
+
+__device__ __forceinline__ uint64_t first_row_at_or_after(const uint64_t *__restrict__ s_off, uint64_t n,
+                                                          uint64_t pos) {
+    uint64_t lo = 0, hi = n;  // first r in [0, n] with s_off[r] >= pos
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (s_off[mid] < pos) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ unsigned lane_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Handles the tiles with MINE < entries <= MAXE, THREADS threads per tile.
+template <int MINE, int MAXE, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+lock_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
+               uint64_t n_rows, int cbits, uint64_t *__restrict__ keys_out, uint32_t *__restrict__ idx_out,
+               unsigned *__restrict__ overflow) {
+    constexpr int TS_THREADS = THREADS, TS_WARPS = THREADS / 32;
+    extern __shared__ __align__(16) unsigned char ts_raw[];
+    TileSortSmem<MAXE, TS_WARPS> &S = *reinterpret_cast<TileSortSmem<MAXE, TS_WARPS> *>(ts_raw);
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {
+        S.bounds[0] = first_row_at_or_after(s_off, n_rows, (uint64_t)blockIdx.x * TS_SPAN);
+        S.bounds[1] = first_row_at_or_after(s_off, n_rows, (uint64_t)(blockIdx.x + 1) * TS_SPAN);
+    }
+    __syncthreads();
+    const uint64_t r0 = S.bounds[0], r1 = S.bounds[1];
+    const uint64_t start = s_off[r0], end = s_off[r1];
+    const uint64_t E64 = end - start;
+    if (E64 <= (uint64_t)MINE) return;  // empty, or the other launch's tile
+    if (E64 > (uint64_t)MAXE) {
+        if (MAXE == TS_MAX && t == 0) *overflow = 1u;
+        return;
+    }
+    const int E = (int)E64;
+    for (int e = t; e < E; e += TS_THREADS) {
+        S.col[e] = cols[start + e];
+        S.seg[e] = rows[start + e] - (uint32_t)r0;
+        S.perm[0][e] = (uint16_t)e;
+    }
+    const int segbits = 32 - __clz((unsigned)(r1 - r0));  // bits of the largest seg (r1 - r0 - 1), rounded up
+    const int bits = segbits + cbits;
+    const int chunk = (E + TS_WARPS - 1) / TS_WARPS;
+    const int q0 = min(E, warp * chunk), q1 = min(E, q0 + chunk);
+    int cur = 0;
+    __syncthreads();
+    for (int shift = 0; shift < bits; shift += 8) {
+        for (int i = t; i < TS_WARPS * 256; i += TS_THREADS) (&S.cnt[0][0])[i] = 0;
+        __syncthreads();
+        // counts per warp and digit, in the warp's slice of the current order
+        for (int q = q0; q < q1; q += 32) {
+            const int qq = q + lane;
+            const bool ok = qq < q1;
+            unsigned d = 256;
+            if (ok) {
+                const int e = S.perm[cur][qq];
+                d = (unsigned)(((((uint64_t)S.seg[e]) << cbits) | S.col[e]) >> shift) & 0xFFu;
+            }
+            const unsigned peers = warp_match_digit(d);
+            if (ok && (peers & lane_lt()) == 0) S.cnt[warp][d] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (t < 256) {  // digit t: starts per warp, then across digits
+            unsigned tot = 0;
+            for (int w = 0; w < TS_WARPS; ++w) {
+                const unsigned c = S.cnt[w][t];
+                S.cnt[w][t] = tot;
+                tot += c;
+            }
+            unsigned inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if (lane == 31) S.wsum[warp] = inc;
+            S.loc[t] = inc - tot;
+        }
+        __syncthreads();
+        if (t < 256) {
+            unsigned pre = 0;
+            for (int w = 0; w < warp; ++w) pre += S.wsum[w];
+            const unsigned base = S.loc[t] + pre;
+            for (int w = 0; w < TS_WARPS; ++w) S.cnt[w][t] += base;
+        }
+        __syncthreads();
+        // stable scatter of the permutation
+        for (int q = q0; q < q1; q += 32) {
+            const int qq = q + lane;
+            const bool ok = qq < q1;
+            int e = 0;
+            unsigned d = 256;
+            if (ok) {
+                e = S.perm[cur][qq];
+                d = (unsigned)(((((uint64_t)S.seg[e]) << cbits) | S.col[e]) >> shift) & 0xFFu;
+            }
+            const unsigned peers = warp_match_digit(d);
+            unsigned before = 0;
+            if (ok) before = S.cnt[warp][d];
+            __syncwarp();
+            if (ok) {
+                S.perm[cur ^ 1][before + __popc(peers & lane_lt())] = (uint16_t)e;
+                if ((peers & lane_lt()) == 0) S.cnt[warp][d] = before + __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (int q = t; q < E; q += TS_THREADS) {
+        const int e = S.perm[cur][q];
+        keys_out[start + q] = ((uint64_t)(r0 + S.seg[e]) << cbits) | S.col[e];
+        idx_out[start + q] = (uint32_t)(start + e);
+    }
 }
 
 // flag[i] = 1 iff sorted key i is the last of its run (the last write).
@@ -303,16 +462,50 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
     SPG_LAUNCH_CHECK();
     // Inserts staged already in (row, col) order (row by row, ascending
     // columns: how stencils and most assemblies insert) need no sort: the
-    // stable sort of a non-decreasing sequence is the identity.
+    // stable sort of a non-decreasing sequence is the identity. Inserts staged
+    // row by row with columns in any order are sorted row by row on chip.
     DevBuf flag;
-    SPG_TRY(flag.alloc(sizeof(unsigned), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), s));
-    keys_descent<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, flag.as<unsigned>());
+    SPG_TRY(flag.alloc(3 * sizeof(unsigned), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, 3 * sizeof(unsigned), s));
+    keys_descent<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, cbits, flag.as<unsigned>());
     SPG_LAUNCH_CHECK();
-    unsigned unsorted = 1;
-    SPG_CUDA_TRY(cudaMemcpyAsync(&unsorted, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    unsigned f[2] = {1u, 1u};
+    SPG_CUDA_TRY(cudaMemcpyAsync(f, flag.ptr, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
-    if (unsorted) SPG_TRY(radix_sort_pairs_u64(c, keys.as<uint64_t>(), idx.as<uint32_t>(), m, rbits + cbits, s));
+    if (!f[0]) return SPG_OK;
+    if (!f[1]) {
+        DevBuf s_off, keys2, idx2;
+        SPG_TRY(s_off.alloc((n_rows + 1) * sizeof(uint64_t), s));
+        offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+            rows, m, n_rows, s_off.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+        SPG_TRY(keys2.alloc(m * sizeof(uint64_t), s));
+        SPG_TRY(idx2.alloc(m * sizeof(uint32_t), s));
+        constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL, TS_THREADS_SMALL / 32>);
+        constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX, TS_THREADS_LARGE / 32>);
+        auto small_k = lock_tile_sort<0, TS_SMALL, TS_THREADS_SMALL>;
+        auto large_k = lock_tile_sort<TS_SMALL, TS_MAX, TS_THREADS_LARGE>;
+        SPG_CUDA_TRY(cudaFuncSetAttribute(small_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+        SPG_CUDA_TRY(cudaFuncSetAttribute(large_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)large_smem));
+        const uint64_t n_tiles = (m + TS_SPAN - 1) / TS_SPAN;
+        small_k<<<(unsigned)n_tiles, TS_THREADS_SMALL, small_smem, s>>>(
+            rows, cols, s_off.as<uint64_t>(), n_rows, cbits, keys2.as<uint64_t>(), idx2.as<uint32_t>(),
+            flag.as<unsigned>() + 2);
+        SPG_LAUNCH_CHECK();
+        large_k<<<(unsigned)n_tiles, TS_THREADS_LARGE, large_smem, s>>>(
+            rows, cols, s_off.as<uint64_t>(), n_rows, cbits, keys2.as<uint64_t>(), idx2.as<uint32_t>(),
+            flag.as<unsigned>() + 2);
+        SPG_LAUNCH_CHECK();
+        unsigned overflow = 1;
+        SPG_CUDA_TRY(cudaMemcpyAsync(&overflow, flag.as<unsigned>() + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!overflow) {
+            keys = std::move(keys2);
+            idx = std::move(idx2);
+            return SPG_OK;
+        }
+    }
+    SPG_TRY(radix_sort_pairs_u64(c, keys.as<uint64_t>(), idx.as<uint32_t>(), m, rbits + cbits, s));
     return SPG_OK;
 }
 

@@ -172,7 +172,7 @@ int exclusive_scan_i64(Ctx *c, int64_t *d, uint64_t n, cudaStream_t s) {
 // lane-minor), so the within-tile rank of every key is its order among equal
 // digits: stability follows, and with it the insertion-order tie-break.
 // The upsweep counts digits with shared-memory atomics; the scatter ranks
-// equal digits within a warp with match.any. The scatter first places the tile in shared memory in digit order, then
+// equal digits within a warp with ballots. The scatter first places the tile in shared memory in digit order, then
 // writes each digit's run to its global position with consecutive threads
 // on consecutive addresses, so the writes coalesce.
 // ---------------------------------------------------------------------------
@@ -268,7 +268,7 @@ radix_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__
         rank[j] = 0;
         if (!valid) continue;
         const unsigned d = ok ? (unsigned)((key[j] >> shift) & 0xFF) : RS_RADIX;
-        const unsigned peers = __match_any_sync(0xffffffffu, d) & valid;
+        const unsigned peers = warp_match_digit(d) & valid;
         unsigned before = 0;
         if (ok) before = S.cnt[warp][d];
         __syncwarp();

@@ -103,6 +103,37 @@ def test_lock_presorted_input_with_duplicates(ctx):
     assert_csr_equal(A.download(), oracle.lock_epochs(4, 6, [(rows, cols, vals), b]))
 
 
+@pytest.mark.parametrize("lengths,n_rows,n_cols", [
+    ([13_000, 5, 0, 7], 4, 50_000),                    # a row longer than one on-chip tile: global sort
+    ([3, 0, 0, 1, 2] * 4000, 20_000, 300),              # short rows, heavy duplicates
+    ([9000, 1, 1, 2000, 4000, 1], 6, 1 << 22),          # long rows within a tile, 22-bit columns
+])
+def test_lock_row_grouped_inserts(ctx, lengths, n_rows, n_cols):
+    """Inserts staged row by row with columns in any order (the on-chip
+    per-row sort), duplicates and zeros included; also rows far apart."""
+    lengths = np.asarray(lengths, np.int64)
+    rows = np.repeat(np.arange(len(lengths), dtype=np.uint32), lengths)
+    if n_rows > len(lengths):
+        rows = (rows.astype(np.uint64) * (n_rows // len(lengths))).astype(np.uint32)
+    ctr = np.arange(len(rows), dtype=np.uint64)
+    cols = gen.below(gen.hash3(len(rows), 1, ctr), n_cols)
+    vals = gen.sym_unit(gen.hash3(len(rows), 2, ctr))
+    vals[::13] = 0.0
+    A = gpu_lock(ctx, n_rows, n_cols, [(rows, cols, vals)])
+    assert_csr_equal(A.download(), oracle.lock_epochs(n_rows, n_cols, [(rows, cols, vals)]))
+
+
+def test_lock_row_grouped_sparse_rows(ctx):
+    """Grouped inserts whose rows are far apart (large row spans per tile)."""
+    n = 3_000_000
+    rows = np.repeat(np.array([0, 5, 1_000_000, 2_999_999], np.uint32), [700, 3000, 2, 40])
+    ctr = np.arange(len(rows), dtype=np.uint64)
+    cols = gen.below(gen.hash3(8, 1, ctr), n)
+    vals = gen.sym_unit(gen.hash3(8, 2, ctr))
+    A = gpu_lock(ctx, n, n, [(rows, cols, vals)])
+    assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(rows, cols, vals)]))
+
+
 def test_lock_zipf_long_rows(ctx):
     r, c, v = gen.zipf_rows(100_000, seed=9)
     b = gen.relock_batch(100_000, 100_000, len(r), seed=10, zero_frac=0.05)
