@@ -194,13 +194,15 @@ inline uint64_t csr_alloc_elems(uint64_t cap) { return ((cap + 15) & ~15ull) + 1
 // stays inside the allocation.
 inline uint64_t csr_off_elems(uint64_t n_rows) { return n_rows + 3; }
 
-// Lanes of the (full) warp whose 9-bit value d (a radix digit, or 256 for
-// "no key") equals this lane's: nine ballots on the ALU pipe, cheaper on
-// GB300 than match.any, which issues on the narrow address-divergence unit.
+// Lanes of the (full) warp whose NB-bit value d (a radix digit, or 256 for
+// "no key" when NB = 9) equals this lane's: NB ballots on the ALU pipe,
+// cheaper on GB300 than match.any, which issues on the narrow
+// address-divergence unit.
+template <int NB = 9>
 __device__ __forceinline__ unsigned warp_match_digit(unsigned d) {
     unsigned peers = 0xffffffffu;
 #pragma unroll
-    for (int b = 0; b < 9; ++b) {
+    for (int b = 0; b < NB; ++b) {
         const unsigned bit = (d >> b) & 1u;
         const unsigned bal = __ballot_sync(0xffffffffu, bit);
         peers &= bit ? bal : ~bal;
