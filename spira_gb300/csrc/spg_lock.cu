@@ -61,173 +61,6 @@ __global__ void keys_descent(const uint64_t *__restrict__ keys, uint64_t m, int 
     }
 }
 
-// Row-grouped inserts (rows non-decreasing, columns in any order): sort each
-// row's entries by column in shared memory, tile by tile. Tile t holds the
-// rows whose first entry lies in [t*TS_SPAN, (t+1)*TS_SPAN): its entries
-// [start_t, start_{t+1}) are contiguous and already in row order, so sorting
-// inside the tile by (row, column), stably, puts them in their final global
-// places. The sort is an LSD radix sort (8-bit digits) of 32-bit composite
-// keys (row - first row of the tile, column) with 16-bit tile indices,
-// ping-ponged in shared memory. Warp w owns positions [512 w, 512 w + 512) of
-// every pass; each scatter also counts, per destination slice, the digit of
-// the next pass, so a pass is one sweep. Two launches share the tiles: tiles
-// of at most TS_SMALL entries (the common case; three blocks per SM) and
-// tiles of up to TS_MAX (one holding a long row; one block per SM). A tile
-// longer than TS_MAX (a row of more than ~10 000 entries) or whose key does
-// not fit 32 bits sets *overflow and the caller sorts globally instead.
-constexpr int TS_SPAN = 2048;
-constexpr int TS_SLICE = 512;
-constexpr int TS_SMALL = 4096;
-constexpr int TS_MAX = 12288;
-
-template <int MAXE>
-struct TileSortSmem {
-    uint32_t key[2][MAXE];
-    uint16_t idx[2][MAXE];
-    unsigned cnt[2][MAXE / TS_SLICE][256];
-    unsigned wsum[8];
-};
-
-__device__ __forceinline__ uint64_t first_row_at_or_after(const uint64_t *__restrict__ s_off, uint64_t n,
-                                                          uint64_t pos) {
-    uint64_t lo = 0, hi = n;  // first r in [0, n] with s_off[r] >= pos
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if (s_off[mid] < pos) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ unsigned lane_lt() {
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
-// First row of every tile (entry n_tiles: n_rows), and the tiles sorted into
-// a list of small ones (<= TS_SMALL entries) and a list of large ones (<=
-// TS_MAX); *overflow = 1 if a tile is longer. List order does not matter: the
-// tiles are independent.
-__global__ void tile_plan(const uint64_t *__restrict__ s_off, uint64_t n_rows, uint64_t n_tiles,
-                          uint64_t *__restrict__ tile_r0, unsigned *__restrict__ small_list,
-                          unsigned *__restrict__ large_list, unsigned *__restrict__ counts /* [2] */,
-                          unsigned *__restrict__ overflow) {
-    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (t > n_tiles) return;
-    const uint64_t r0 = t == n_tiles ? n_rows : first_row_at_or_after(s_off, n_rows, t * TS_SPAN);
-    tile_r0[t] = r0;
-    if (t == n_tiles) return;
-    const uint64_t r1 = first_row_at_or_after(s_off, n_rows, (t + 1) * TS_SPAN);
-    const uint64_t E = s_off[r1] - s_off[r0];
-    if (E == 0) return;
-    if (E <= (uint64_t)TS_SMALL) small_list[atomicAdd(counts, 1u)] = (unsigned)t;
-    else if (E <= (uint64_t)TS_MAX) large_list[atomicAdd(counts + 1, 1u)] = (unsigned)t;
-    else *overflow = 1u;
-}
-
-// Sorts the tiles of `list` (each of at most MAXE entries); one warp per
-// 512 entries.
-template <int MAXE>
-__global__ void __launch_bounds__(MAXE / TS_SLICE * 32)
-lock_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
-               const uint64_t *__restrict__ tile_r0, const unsigned *__restrict__ list, int cbits,
-               uint64_t *__restrict__ keys_out, uint32_t *__restrict__ idx_out, unsigned *__restrict__ overflow) {
-    constexpr int W = MAXE / TS_SLICE, T = W * 32;
-    extern __shared__ __align__(16) unsigned char ts_raw[];
-    TileSortSmem<MAXE> &S = *reinterpret_cast<TileSortSmem<MAXE> *>(ts_raw);
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const unsigned tile = list[blockIdx.x];
-    const uint64_t r0 = tile_r0[tile], r1 = tile_r0[tile + 1];
-    const uint64_t start = s_off[r0], end = s_off[r1];
-    const uint64_t E64 = end - start;
-    if (E64 == 0 || E64 > (uint64_t)MAXE) return;  // (the plan never lists such tiles)
-    const int E = (int)E64;
-    const unsigned span = (unsigned)(r1 - r0 - 1);  // largest row offset inside the tile
-    const int bits = (span ? 32 - __clz(span) : 0) + cbits;
-    if (bits > 32 || cbits >= 32) {
-        if (t == 0) *overflow = 1u;
-        return;
-    }
-    const int passes = (bits + 7) / 8;
-    for (int e = t; e < E; e += T) {
-        S.key[0][e] = ((rows[start + e] - (uint32_t)r0) << cbits) | cols[start + e];
-        S.idx[0][e] = (uint16_t)e;
-    }
-    for (int i = t; i < 2 * W * 256; i += T) (&S.cnt[0][0][0])[i] = 0;
-    __syncthreads();
-    const int q0 = warp * TS_SLICE, q1 = min(E, q0 + TS_SLICE);
-    // digit counts of the first pass, per warp slice
-    for (int q = q0; q < q1 && passes > 0; q += 32) {
-        const int qq = q + lane;
-        const bool ok = qq < q1;
-        const unsigned valid = __ballot_sync(0xffffffffu, ok);
-        const unsigned d = ok ? (S.key[0][qq] & 0xFFu) : 0u;
-        const unsigned peers = warp_match_digit<8>(d) & valid;
-        if (ok && (peers & lane_lt()) == 0) S.cnt[0][warp][d] += __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    int cur = 0;
-    for (int p = 0; p < passes; ++p) {
-        const int c = p & 1, shift = 8 * p;
-        // digit t: start of each warp slice's run, then across digits
-        unsigned excl = 0;
-        if (t < 256) {
-            unsigned tot = 0;
-            for (int w = 0; w < W; ++w) {
-                const unsigned v = S.cnt[c][w][t];
-                S.cnt[c][w][t] = tot;
-                tot += v;
-            }
-            unsigned inc = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += v;
-            }
-            if (lane == 31) S.wsum[warp] = inc;
-            excl = inc - tot;
-        }
-        for (int i = t; i < W * 256; i += T) (&S.cnt[c ^ 1][0][0])[i] = 0;  // next pass's counts
-        __syncthreads();
-        if (t < 256) {
-            unsigned pre = 0;
-            for (int w = 0; w < warp; ++w) pre += S.wsum[w];
-            const unsigned base = excl + pre;
-            for (int w = 0; w < W; ++w) S.cnt[c][w][t] += base;
-        }
-        __syncthreads();
-        // stable scatter; count the next pass's digits per destination slice
-        for (int q = q0; q < q1; q += 32) {
-            const int qq = q + lane;
-            const bool ok = qq < q1;
-            const unsigned valid = __ballot_sync(0xffffffffu, ok);
-            const uint32_t k = ok ? S.key[cur][qq] : 0u;
-            const unsigned d = (k >> shift) & 0xFFu;
-            const unsigned peers = warp_match_digit<8>(d) & valid;
-            unsigned before = 0;
-            if (ok) before = S.cnt[c][warp][d];
-            __syncwarp();
-            if (ok) {
-                const unsigned lt = peers & lane_lt();
-                const unsigned pos = before + __popc(lt);
-                S.key[cur ^ 1][pos] = k;
-                S.idx[cur ^ 1][pos] = S.idx[cur][qq];
-                if (lt == 0) S.cnt[c][warp][d] = before + __popc(peers);
-                if (p + 1 < passes) atomicAdd(&S.cnt[c ^ 1][pos / TS_SLICE][(k >> (shift + 8)) & 0xFFu], 1u);
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-        cur ^= 1;
-    }
-    for (int q = t; q < E; q += T) {
-        keys_out[start + q] = ((uint64_t)r0 << cbits) + S.key[cur][q];
-        idx_out[start + q] = (uint32_t)(start + S.idx[cur][q]);
-    }
-}
-
 // flag[i] = 1 iff sorted key i is the last of its run (the last write).
 __global__ void lock_last_flags(const uint64_t *__restrict__ keys, uint64_t m, uint64_t *__restrict__ flag) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
@@ -481,9 +314,9 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
     // stable sort of a non-decreasing sequence is the identity. Inserts staged
     // row by row with columns in any order are sorted row by row on chip.
     DevBuf flag;
-    // [0] unsorted, [1] rows not grouped, [2] tile overflow, [3] small tiles, [4] large tiles
-    SPG_TRY(flag.alloc(5 * sizeof(unsigned), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, 5 * sizeof(unsigned), s));
+    // [0] keys unsorted, [1] rows not grouped
+    SPG_TRY(flag.alloc(2 * sizeof(unsigned), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, 2 * sizeof(unsigned), s));
     keys_descent<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, cbits, flag.as<unsigned>());
     SPG_LAUNCH_CHECK();
     unsigned f[2] = {1u, 1u};
@@ -496,45 +329,12 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
         offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
             rows, m, n_rows, s_off.as<uint64_t>());
         SPG_LAUNCH_CHECK();
-        const uint64_t n_tiles = (m + TS_SPAN - 1) / TS_SPAN;
-        DevBuf tile_r0, lists;
-        SPG_TRY(tile_r0.alloc((n_tiles + 1) * sizeof(uint64_t), s));
-        SPG_TRY(lists.alloc(2 * n_tiles * sizeof(unsigned), s));
-        unsigned *small_list = lists.as<unsigned>(), *large_list = small_list + n_tiles;
-        unsigned *counts = flag.as<unsigned>() + 3, *overflow_d = flag.as<unsigned>() + 2;
-        tile_plan<<<grid_for(n_tiles + 1, LB), LB, 0, s>>>(s_off.as<uint64_t>(), n_rows, n_tiles,
-                                                         tile_r0.as<uint64_t>(), small_list, large_list, counts,
-                                                         overflow_d);
-        SPG_LAUNCH_CHECK();
-        unsigned h[3] = {1u, 0u, 0u};  // overflow, small tiles, large tiles
-        SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow_d, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
-        if (!h[0]) {
-            SPG_TRY(keys2.alloc(m * sizeof(uint64_t), s));
-            SPG_TRY(idx2.alloc(m * sizeof(uint32_t), s));
-            constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL>);
-            constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX>);
-            constexpr unsigned small_threads = TS_SMALL / TS_SLICE * 32, large_threads = TS_MAX / TS_SLICE * 32;
-            auto small_k = lock_tile_sort<TS_SMALL>;
-            auto large_k = lock_tile_sort<TS_MAX>;
-            SPG_CUDA_TRY(cudaFuncSetAttribute(small_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
-            SPG_CUDA_TRY(cudaFuncSetAttribute(large_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)large_smem));
-            if (h[1]) {
-                small_k<<<h[1], small_threads, small_smem, s>>>(rows, cols, s_off.as<uint64_t>(),
-                                                                tile_r0.as<uint64_t>(), small_list, cbits,
-                                                                keys2.as<uint64_t>(), idx2.as<uint32_t>(), overflow_d);
-                SPG_LAUNCH_CHECK();
-            }
-            if (h[2]) {
-                large_k<<<h[2], large_threads, large_smem, s>>>(rows, cols, s_off.as<uint64_t>(),
-                                                                tile_r0.as<uint64_t>(), large_list, cbits,
-                                                                keys2.as<uint64_t>(), idx2.as<uint32_t>(), overflow_d);
-                SPG_LAUNCH_CHECK();
-            }
-            SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow_d, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-            SPG_CUDA_TRY(cudaStreamSynchronize(s));
-        }
-        if (!h[0]) {
+        SPG_TRY(keys2.alloc(m * sizeof(uint64_t), s));
+        SPG_TRY(idx2.alloc(m * sizeof(uint32_t), s));
+        bool done = false;
+        SPG_TRY(sort_grouped_rows(c, rows, cols, s_off.as<uint64_t>(), m, n_rows, cbits, keys2.as<uint64_t>(),
+                                  idx2.as<uint32_t>(), &done, s));
+        if (done) {
             keys = std::move(keys2);
             idx = std::move(idx2);
             return SPG_OK;

@@ -370,6 +370,220 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 }
 
 // ---------------------------------------------------------------------------
+// Row-grouped sort: pairs (row, col) whose rows are already non-decreasing
+// (rows[i] <= rows[i+1]) are put in stable (row, col) order by sorting each
+// row's entries by column in shared memory, tile by tile. Tile t holds the
+// rows whose first entry lies in [t*TS_SPAN, (t+1)*TS_SPAN): its entries
+// [start_t, start_{t+1}) are contiguous and already in row order, so sorting
+// inside the tile by (row, column), stably, puts them in their final global
+// places. The sort is an LSD radix sort (8-bit digits) of 32-bit composite
+// keys (row - first row of the tile, column) with 16-bit tile indices,
+// ping-ponged in shared memory. Warp w owns positions [512 w, 512 w + 512) of
+// every pass; each scatter also counts, per destination slice, the digit of
+// the next pass, so a pass is one sweep. Tiles of at most TS_SMALL entries
+// (three blocks per SM) and tiles of up to TS_MAX (one holding a long row;
+// one block per SM) run as two launches over a tile plan. A tile longer than
+// TS_MAX (a row of more than ~10 000 entries) or whose key needs more than 32
+// bits makes the sort report failure; callers then sort globally.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int TS_SPAN = 2048;
+constexpr int TS_SLICE = 512;
+constexpr int TS_SMALL = 4096;
+constexpr int TS_MAX = 12288;
+
+template <int MAXE>
+struct TileSortSmem {
+    uint32_t key[2][MAXE];
+    uint16_t idx[2][MAXE];
+    unsigned cnt[2][MAXE / TS_SLICE][256];
+    unsigned wsum[8];
+};
+
+__device__ __forceinline__ uint64_t first_row_at_or_after(const uint64_t *__restrict__ s_off, uint64_t n,
+                                                          uint64_t pos) {
+    uint64_t lo = 0, hi = n;  // first r in [0, n] with s_off[r] >= pos
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (s_off[mid] < pos) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// First row of every tile (entry n_tiles: n_rows), and the tiles sorted into
+// a list of small ones (<= TS_SMALL entries) and a list of large ones (<=
+// TS_MAX); *overflow = 1 if a tile is longer. List order does not matter: the
+// tiles are independent.
+__global__ void tile_plan(const uint64_t *__restrict__ s_off, uint64_t n_rows, uint64_t n_tiles,
+                          uint64_t *__restrict__ tile_r0, unsigned *__restrict__ small_list,
+                          unsigned *__restrict__ large_list, unsigned *__restrict__ counts /* [2] */,
+                          unsigned *__restrict__ overflow) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (t > n_tiles) return;
+    const uint64_t r0 = t == n_tiles ? n_rows : first_row_at_or_after(s_off, n_rows, t * TS_SPAN);
+    tile_r0[t] = r0;
+    if (t == n_tiles) return;
+    const uint64_t r1 = first_row_at_or_after(s_off, n_rows, (t + 1) * TS_SPAN);
+    const uint64_t E = s_off[r1] - s_off[r0];
+    if (E == 0) return;
+    if (E <= (uint64_t)TS_SMALL) small_list[atomicAdd(counts, 1u)] = (unsigned)t;
+    else if (E <= (uint64_t)TS_MAX) large_list[atomicAdd(counts + 1, 1u)] = (unsigned)t;
+    else *overflow = 1u;
+}
+
+// Sorts the tiles of `list` (each of at most MAXE entries); one warp per
+// 512 entries.
+template <int MAXE>
+__global__ void __launch_bounds__(MAXE / TS_SLICE * 32)
+grouped_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
+                  const uint64_t *__restrict__ s_off, const uint64_t *__restrict__ tile_r0,
+                  const unsigned *__restrict__ list, int cbits, uint64_t *__restrict__ keys_out,
+                  uint32_t *__restrict__ idx_out, unsigned *__restrict__ overflow) {
+    constexpr int W = MAXE / TS_SLICE, T = W * 32;
+    extern __shared__ __align__(16) unsigned char ts_raw[];
+    TileSortSmem<MAXE> &S = *reinterpret_cast<TileSortSmem<MAXE> *>(ts_raw);
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const unsigned tile = list[blockIdx.x];
+    const uint64_t r0 = tile_r0[tile], r1 = tile_r0[tile + 1];
+    const uint64_t start = s_off[r0], end = s_off[r1];
+    const uint64_t E64 = end - start;
+    if (E64 == 0 || E64 > (uint64_t)MAXE) return;  // (the plan never lists such tiles)
+    const int E = (int)E64;
+    const unsigned span = (unsigned)(r1 - r0 - 1);  // largest row offset inside the tile
+    const int bits = (span ? 32 - __clz(span) : 0) + cbits;
+    if (bits > 32 || cbits >= 32) {
+        if (t == 0) *overflow = 1u;
+        return;
+    }
+    const int passes = (bits + 7) / 8;
+    for (int e = t; e < E; e += T) {
+        S.key[0][e] = ((rows[start + e] - (uint32_t)r0) << cbits) | cols[start + e];
+        S.idx[0][e] = (uint16_t)e;
+    }
+    for (int i = t; i < 2 * W * 256; i += T) (&S.cnt[0][0][0])[i] = 0;
+    __syncthreads();
+    const int q0 = warp * TS_SLICE, q1 = min(E, q0 + TS_SLICE);
+    // digit counts of the first pass, per warp slice
+    for (int q = q0; q < q1 && passes > 0; q += 32) {
+        const int qq = q + lane;
+        const bool ok = qq < q1;
+        const unsigned valid = __ballot_sync(0xffffffffu, ok);
+        const unsigned d = ok ? (S.key[0][qq] & 0xFFu) : 0u;
+        const unsigned peers = warp_match_digit<8>(d) & valid;
+        if (ok && (peers & lanemask_lt()) == 0) S.cnt[0][warp][d] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        const int c = p & 1, shift = 8 * p;
+        // digit t: start of each warp slice's run, then across digits
+        unsigned excl = 0;
+        if (t < 256) {
+            unsigned tot = 0;
+            for (int w = 0; w < W; ++w) {
+                const unsigned v = S.cnt[c][w][t];
+                S.cnt[c][w][t] = tot;
+                tot += v;
+            }
+            unsigned inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if (lane == 31) S.wsum[warp] = inc;
+            excl = inc - tot;
+        }
+        for (int i = t; i < W * 256; i += T) (&S.cnt[c ^ 1][0][0])[i] = 0;  // next pass's counts
+        __syncthreads();
+        if (t < 256) {
+            unsigned pre = 0;
+            for (int w = 0; w < warp; ++w) pre += S.wsum[w];
+            const unsigned base = excl + pre;
+            for (int w = 0; w < W; ++w) S.cnt[c][w][t] += base;
+        }
+        __syncthreads();
+        // stable scatter; count the next pass's digits per destination slice
+        for (int q = q0; q < q1; q += 32) {
+            const int qq = q + lane;
+            const bool ok = qq < q1;
+            const unsigned valid = __ballot_sync(0xffffffffu, ok);
+            const uint32_t k = ok ? S.key[cur][qq] : 0u;
+            const unsigned d = (k >> shift) & 0xFFu;
+            const unsigned peers = warp_match_digit<8>(d) & valid;
+            unsigned before = 0;
+            if (ok) before = S.cnt[c][warp][d];
+            __syncwarp();
+            if (ok) {
+                const unsigned lt = peers & lanemask_lt();
+                const unsigned pos = before + __popc(lt);
+                S.key[cur ^ 1][pos] = k;
+                S.idx[cur ^ 1][pos] = S.idx[cur][qq];
+                if (lt == 0) S.cnt[c][warp][d] = before + __popc(peers);
+                if (p + 1 < passes) atomicAdd(&S.cnt[c ^ 1][pos / TS_SLICE][(k >> (shift + 8)) & 0xFFu], 1u);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (int q = t; q < E; q += T) {
+        keys_out[start + q] = ((uint64_t)r0 << cbits) + S.key[cur][q];
+        idx_out[start + q] = (uint32_t)(start + S.idx[cur][q]);
+    }
+}
+
+}  // namespace
+
+int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
+                      uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s) {
+    *done = false;
+    if (m == 0) {
+        *done = true;
+        return SPG_OK;
+    }
+    const uint64_t n_tiles = (m + TS_SPAN - 1) / TS_SPAN;
+    DevBuf tile_r0, lists, flags;
+    SPG_TRY(tile_r0.alloc((n_tiles + 1) * sizeof(uint64_t), s));
+    SPG_TRY(lists.alloc(2 * n_tiles * sizeof(unsigned), s));
+    SPG_TRY(flags.alloc(3 * sizeof(unsigned), s));  // overflow, small tiles, large tiles
+    SPG_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, 3 * sizeof(unsigned), s));
+    unsigned *small_list = lists.as<unsigned>(), *large_list = small_list + n_tiles;
+    unsigned *overflow = flags.as<unsigned>();
+    tile_plan<<<grid_for(n_tiles + 1, 256), 256, 0, s>>>(s_off, n_rows, n_tiles, tile_r0.as<uint64_t>(), small_list,
+                                                        large_list, overflow + 1, overflow);
+    SPG_LAUNCH_CHECK();
+    unsigned h[3] = {1u, 0u, 0u};
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h[0]) return SPG_OK;
+    constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL>);
+    constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX>);
+    constexpr unsigned small_threads = TS_SMALL / TS_SLICE * 32, large_threads = TS_MAX / TS_SLICE * 32;
+    auto small_k = grouped_tile_sort<TS_SMALL>;
+    auto large_k = grouped_tile_sort<TS_MAX>;
+    SPG_CUDA_TRY(cudaFuncSetAttribute(small_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+    SPG_CUDA_TRY(cudaFuncSetAttribute(large_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)large_smem));
+    if (h[1]) {
+        small_k<<<h[1], small_threads, small_smem, s>>>(rows, cols, s_off, tile_r0.as<uint64_t>(), small_list, cbits,
+                                                        keys_out, idx_out, overflow);
+        SPG_LAUNCH_CHECK();
+    }
+    if (h[2]) {
+        large_k<<<h[2], large_threads, large_smem, s>>>(rows, cols, s_off, tile_r0.as<uint64_t>(), large_list, cbits,
+                                                        keys_out, idx_out, overflow);
+        SPG_LAUNCH_CHECK();
+    }
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    *done = h[0] == 0;
+    return SPG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Max reduction (used for device-side index range checks)
 // ---------------------------------------------------------------------------
 namespace {
