@@ -565,6 +565,7 @@ PROFILE_CASES = {
     # lock / transpose / SpGEMM: `--reps` calls of the operation
     "lock_zipf1m": (1_000_000, "lock"),
     "lock_laplacian2d": (GRID * GRID, "lock"),
+    "relock_zipf1m": (1_000_000, "relock"),
     "transpose_laplacian3d": (100 ** 3, "transpose"),
     "spgemm_laplacian3d": (100 ** 3, "spgemm"),
     "spgemm_uniform200k": (200_000, "spgemm"),
@@ -576,7 +577,26 @@ def run_profile_op(ctx, case, n, kind, reps):
     import spira_gb300 as sg
     from spira_gb300 import gen, gen_device
     ms = []
-    if kind == "lock":
+    if kind == "relock":
+        import torch
+        r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
+        A = sg.Csr(ctx, n, n)
+        A.lock_device(r, c, v, m)
+        del r, c, v
+        dr, dc, dv = gen.relock_batch(n, n, A.nnz, seed=32)
+        d = (torch.from_numpy(dr.view(np.int32)).cuda(), torch.from_numpy(dc.view(np.int32)).cuda(),
+             torch.from_numpy(dv).cuda())
+        pristine = sg.Csr(ctx, n, n)
+        pristine.copy_from(A)
+        for _ in range(reps + 1):
+            A.copy_from(pristine)
+            ctx.sync()
+            t0 = time.perf_counter()
+            A.lock_device(d[0], d[1], d[2], len(dr))
+            ctx.sync()
+            ms.append((time.perf_counter() - t0) * 1e3)
+        nnz = A.nnz
+    elif kind == "lock":
         if case == "lock_laplacian2d":
             import torch
             hr, hc, hv = gen.laplacian_2d(GRID)
@@ -619,7 +639,7 @@ def run_profile_case(args):
     ctx = sg.Context(0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     n, kind = PROFILE_CASES[args.profile_case]
-    if kind in ("lock", "transpose", "spgemm"):
+    if kind in ("lock", "relock", "transpose", "spgemm"):
         run_profile_op(ctx, args.profile_case, n, kind, args.reps)
         return
     if kind == "zipf":

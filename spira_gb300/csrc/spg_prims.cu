@@ -379,25 +379,25 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 // places. The sort is an LSD radix sort (8-bit digits) of 32-bit composite
 // keys (row - first row of the tile, column) with 16-bit tile indices,
 // ping-ponged in shared memory. Warp w owns positions [512 w, 512 w + 512) of
-// every pass; each scatter also counts, per destination slice, the digit of
-// the next pass, so a pass is one sweep. Tiles of at most TS_SMALL entries
-// (three blocks per SM) and tiles of up to TS_MAX (one holding a long row;
-// one block per SM) run as two launches over a tile plan. A tile longer than
+// every pass (16 warps of 256 measured slower); each scatter also counts, per
+// destination slice, the digit of the next pass, so a pass is one sweep.
+// Tiles of at most TS_SMALL entries (three blocks per SM) and tiles of up to
+// TS_MAX (one holding a long row; one block per SM) run as two launches over
+// a tile plan. A tile longer than
 // TS_MAX (a row of more than ~10 000 entries) or whose key needs more than 32
 // bits makes the sort report failure; callers then sort globally.
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr int TS_SPAN = 2048;
-constexpr int TS_SLICE = 512;
-constexpr int TS_SMALL = 4096;
-constexpr int TS_MAX = 12288;
+constexpr int TS_SMALL = 4096, TS_SLICE_SMALL = 512;  // 8 warps
+constexpr int TS_MAX = 12288, TS_SLICE_LARGE = 512;   // 24 warps
 
-template <int MAXE>
+template <int MAXE, int SLICE>
 struct TileSortSmem {
     uint32_t key[2][MAXE];
     uint16_t idx[2][MAXE];
-    unsigned cnt[2][MAXE / TS_SLICE][256];
+    unsigned cnt[2][MAXE / SLICE][256];
     unsigned wsum[8];
 };
 
@@ -434,8 +434,8 @@ __global__ void tile_plan(const uint64_t *__restrict__ s_off, uint64_t n_rows, u
 }
 
 // Sorts the tiles of `list` (each of at most MAXE entries); one warp per
-// 512 entries.
-template <int MAXE>
+// TS_SLICE entries.
+template <int MAXE, int TS_SLICE>
 __global__ void __launch_bounds__(MAXE / TS_SLICE * 32)
 grouped_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
                   const uint64_t *__restrict__ s_off, const uint64_t *__restrict__ tile_r0,
@@ -443,7 +443,7 @@ grouped_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict_
                   uint32_t *__restrict__ idx_out, unsigned *__restrict__ overflow) {
     constexpr int W = MAXE / TS_SLICE, T = W * 32;
     extern __shared__ __align__(16) unsigned char ts_raw[];
-    TileSortSmem<MAXE> &S = *reinterpret_cast<TileSortSmem<MAXE> *>(ts_raw);
+    TileSortSmem<MAXE, TS_SLICE> &S = *reinterpret_cast<TileSortSmem<MAXE, TS_SLICE> *>(ts_raw);
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const unsigned tile = list[blockIdx.x];
     const uint64_t r0 = tile_r0[tile], r1 = tile_r0[tile + 1];
@@ -560,11 +560,12 @@ int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const 
     SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
     if (h[0]) return SPG_OK;
-    constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL>);
-    constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX>);
-    constexpr unsigned small_threads = TS_SMALL / TS_SLICE * 32, large_threads = TS_MAX / TS_SLICE * 32;
-    auto small_k = grouped_tile_sort<TS_SMALL>;
-    auto large_k = grouped_tile_sort<TS_MAX>;
+    constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL, TS_SLICE_SMALL>);
+    constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX, TS_SLICE_LARGE>);
+    constexpr unsigned small_threads = TS_SMALL / TS_SLICE_SMALL * 32;
+    constexpr unsigned large_threads = TS_MAX / TS_SLICE_LARGE * 32;
+    auto small_k = grouped_tile_sort<TS_SMALL, TS_SLICE_SMALL>;
+    auto large_k = grouped_tile_sort<TS_MAX, TS_SLICE_LARGE>;
     SPG_CUDA_TRY(cudaFuncSetAttribute(small_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
     SPG_CUDA_TRY(cudaFuncSetAttribute(large_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)large_smem));
     if (h[1]) {
