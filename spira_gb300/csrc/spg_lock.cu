@@ -196,22 +196,29 @@ __device__ __forceinline__ uint64_t row_of(const uint64_t *__restrict__ off, uin
 // rows (long runs of empty rows) search the global arrays instead.
 constexpr int MO_WIN = 1536;
 
+// Rows of the first and last entry of every chunk (thread per chunk: the
+// searches run in parallel instead of serialising each block's start).
+__global__ void merge_windows(const uint64_t *__restrict__ off, uint64_t n_rows, uint64_t nnz_old,
+                              uint64_t n_chunks, uint64_t *__restrict__ win) {
+    const uint64_t ch = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (ch >= n_chunks) return;
+    const uint64_t k0 = ch * MO_CHUNK, k1 = min(k0 + (uint64_t)MO_CHUNK, nnz_old);
+    const uint64_t lo = row_of(off, 0, n_rows, k0);
+    win[2 * ch] = lo;
+    win[2 * ch + 1] = row_of(off, lo, n_rows, k1 - 1);
+}
+
 __global__ void __launch_bounds__(LB)
 merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
-                const double *__restrict__ vals, uint64_t n_rows, uint64_t nnz_old,
+                const double *__restrict__ vals, const uint64_t *__restrict__ win, uint64_t nnz_old,
                 const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dcol,
                 const int64_t *__restrict__ P, const uint64_t *__restrict__ new_off,
                 uint32_t *__restrict__ out_cols, double *__restrict__ out_vals) {
-    __shared__ uint64_t win[2];
     __shared__ uint64_t s_off[MO_WIN + 1], s_new[MO_WIN + 1], s_doff[MO_WIN + 1];
+    __shared__ uint16_t s_row[MO_CHUNK];  // row of each entry of the chunk, relative to rlo
     const uint64_t k0 = (uint64_t)blockIdx.x * MO_CHUNK;
     const uint64_t k1 = min(k0 + (uint64_t)MO_CHUNK, nnz_old);
-    if (threadIdx.x == 0) {
-        win[0] = row_of(off, 0, n_rows, k0);
-        win[1] = row_of(off, win[0], n_rows, k1 - 1);
-    }
-    __syncthreads();
-    const uint64_t rlo = win[0], rhi = win[1];
+    const uint64_t rlo = win[2 * blockIdx.x], rhi = win[2 * blockIdx.x + 1];
     const bool local = rhi - rlo < (uint64_t)MO_WIN;
     if (local) {
         for (uint64_t t = threadIdx.x; t <= rhi - rlo + 1; t += LB) {
@@ -219,20 +226,20 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
             s_new[t] = new_off[rlo + t];
             s_doff[t] = doff[rlo + t];
         }
+        __syncthreads();
+        // label the chunk's entries with their rows: warp per row
+        const int lane = threadIdx.x & 31;
+        for (int rr = threadIdx.x >> 5; rr <= (int)(rhi - rlo); rr += LB / 32) {
+            const uint64_t b = max(s_off[rr], k0), e = min(s_off[rr + 1], k1);
+            for (uint64_t k = b + lane; k < e; k += 32) s_row[k - k0] = (uint16_t)rr;
+        }
     }
     __syncthreads();
-    // consecutive threads on consecutive entries (coalesced); each finds its
-    // row by binary search (a per-thread forward walk over runs of 8 entries
-    // measured 30 % slower: its loads no longer coalesce)
+    // consecutive threads on consecutive entries (coalesced)
     for (uint64_t k = k0 + threadIdx.x; k < k1; k += LB) {
         uint64_t p, ds, de, nb;
         if (local) {
-            int lo = 0, hi = (int)(rhi - rlo);  // last t with s_off[t] <= k
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (s_off[mid] <= k) lo = mid;
-                else hi = mid - 1;
-            }
+            const int lo = s_row[k - k0];
             p = k - s_off[lo];
             ds = s_doff[lo];
             de = s_doff[lo + 1];
@@ -588,10 +595,14 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     SPG_TRY(out_vals.alloc(csr_alloc_elems(cap) * sizeof(double), s));
     if (has_old && A->nnz) {
         const uint64_t chunks = (A->nnz + MO_CHUNK - 1) / MO_CHUNK;
-        merge_write_old<<<(unsigned)chunks, LB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), n, A->nnz,
-                                                        doff.as<uint64_t>(), D.col.as<uint32_t>(), P.as<int64_t>(),
-                                                        new_off.as<uint64_t>(), out_cols.as<uint32_t>(),
-                                                        out_vals.as<double>());
+        DevBuf win;
+        SPG_TRY(win.alloc(2 * chunks * sizeof(uint64_t), s));
+        merge_windows<<<grid_for(chunks, LB), LB, 0, s>>>(A->d_off(), n, A->nnz, chunks, win.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+        merge_write_old<<<(unsigned)chunks, LB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), win.as<uint64_t>(),
+                                                        A->nnz, doff.as<uint64_t>(), D.col.as<uint32_t>(),
+                                                        P.as<int64_t>(), new_off.as<uint64_t>(),
+                                                        out_cols.as<uint32_t>(), out_vals.as<double>());
         SPG_LAUNCH_CHECK();
     }
     if (u) {

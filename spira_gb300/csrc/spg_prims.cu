@@ -180,9 +180,9 @@ namespace {
 
 constexpr int RS_WARPS = 8;
 constexpr int RS_BLOCK = RS_WARPS * 32;
-constexpr int RS_ITERS = 16;
-constexpr int RS_TILE = RS_BLOCK * RS_ITERS;  // 4096
 constexpr int RS_RADIX = 256;
+// Keys per thread: 16 (tiles of 4096) for large sorts; small sorts use
+// shorter tiles so that enough blocks run.
 
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
@@ -190,9 +190,11 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+template <int RS_ITERS>
 __global__ void __launch_bounds__(RS_BLOCK)
 radix_upsweep(const uint64_t *__restrict__ keys, uint64_t n, int shift, unsigned n_tiles,
               unsigned *__restrict__ hist /* [RADIX][n_tiles] */) {
+    constexpr int RS_TILE = RS_BLOCK * RS_ITERS;
     __shared__ unsigned cnt[RS_WARPS][RS_RADIX];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&cnt[0][0])[i] = 0;
@@ -227,6 +229,7 @@ radix_upsweep(const uint64_t *__restrict__ keys, uint64_t n, int shift, unsigned
 }
 
 // Shared memory of radix_scatter (dynamic: above the 48 KB static limit).
+template <int RS_TILE>
 struct ScatterSmem {
     uint64_t key[RS_TILE];
     uint32_t val[RS_TILE];
@@ -238,12 +241,14 @@ struct ScatterSmem {
 
 static_assert(RS_BLOCK == RS_RADIX, "one thread per digit in the tile-local scan");
 
+template <int RS_ITERS>
 __global__ void __launch_bounds__(RS_BLOCK)
 radix_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
               uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, uint64_t n,
               int shift, unsigned n_tiles, const unsigned long long *__restrict__ offs /* scanned */) {
+    constexpr int RS_TILE = RS_BLOCK * RS_ITERS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem_raw);
+    ScatterSmem<RS_TILE> &S = *reinterpret_cast<ScatterSmem<RS_TILE> *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int t = threadIdx.x;
     for (int i = t; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&S.cnt[0][0])[i] = 0;
@@ -330,12 +335,11 @@ __global__ void scan_u32_to_u64_copy(const unsigned *in, unsigned long long *out
 
 }  // namespace
 
-int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n, int key_bits,
-                         cudaStream_t s) {
-    if (n <= 1 || key_bits <= 0) return SPG_OK;
-    if (n >= (1ull << 32))
-        return set_error(SPG_ERR_UNSUPPORTED, "radix sort of %llu keys exceeds 2^32-1",
-                         (unsigned long long)n);
+namespace {
+
+template <int RS_ITERS>
+int radix_sort_impl(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n, int key_bits, cudaStream_t s) {
+    constexpr int RS_TILE = RS_BLOCK * RS_ITERS;
     const unsigned n_tiles = (unsigned)((n + RS_TILE - 1) / RS_TILE);
     const uint64_t hist_n = (uint64_t)RS_RADIX * n_tiles;
     DevBuf kalt, valt, hist, offs;
@@ -346,18 +350,19 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
     uint64_t *kin = d_keys, *kout = kalt.as<uint64_t>();
     uint32_t *vin = d_vals, *vout = valt.as<uint32_t>();
     const int passes = (key_bits + 7) / 8;
-    SPG_CUDA_TRY(cudaFuncSetAttribute(radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(ScatterSmem)));
+    constexpr size_t smem = sizeof(ScatterSmem<RS_TILE>);
+    SPG_CUDA_TRY(cudaFuncSetAttribute(radix_scatter<RS_ITERS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
     for (int p = 0; p < passes; ++p) {
         const int shift = p * 8;
-        radix_upsweep<<<n_tiles, RS_BLOCK, 0, s>>>(kin, n, shift, n_tiles, hist.as<unsigned>());
+        radix_upsweep<RS_ITERS><<<n_tiles, RS_BLOCK, 0, s>>>(kin, n, shift, n_tiles, hist.as<unsigned>());
         SPG_LAUNCH_CHECK();
         scan_u32_to_u64_copy<<<grid_for(hist_n, 256, 4096), 256, 0, s>>>(
             hist.as<unsigned>(), offs.as<unsigned long long>(), hist_n);
         SPG_LAUNCH_CHECK();
         SPG_TRY(exclusive_scan_u64(c, offs.as<uint64_t>(), hist_n, nullptr, s));
-        radix_scatter<<<n_tiles, RS_BLOCK, sizeof(ScatterSmem), s>>>(kin, vin, kout, vout, n, shift, n_tiles,
-                                                                     offs.as<unsigned long long>());
+        radix_scatter<RS_ITERS><<<n_tiles, RS_BLOCK, smem, s>>>(kin, vin, kout, vout, n, shift, n_tiles,
+                                                                offs.as<unsigned long long>());
         SPG_LAUNCH_CHECK();
         std::swap(kin, kout);
         std::swap(vin, vout);
@@ -367,6 +372,21 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
         SPG_CUDA_TRY(cudaMemcpyAsync(d_vals, vin, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     }
     return SPG_OK;
+}
+
+}  // namespace
+
+int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n, int key_bits,
+                         cudaStream_t s) {
+    if (n <= 1 || key_bits <= 0) return SPG_OK;
+    if (n >= (1ull << 32))
+        return set_error(SPG_ERR_UNSUPPORTED, "radix sort of %llu keys exceeds 2^32-1",
+                         (unsigned long long)n);
+    // at least ~4 tiles per SM
+    const uint64_t want = 4ull * (uint64_t)c->n_sms;
+    if (n >= want * RS_BLOCK * 16) return radix_sort_impl<16>(c, d_keys, d_vals, n, key_bits, s);
+    if (n >= want * RS_BLOCK * 4) return radix_sort_impl<4>(c, d_keys, d_vals, n, key_bits, s);
+    return radix_sort_impl<1>(c, d_keys, d_vals, n, key_bits, s);
 }
 
 // ---------------------------------------------------------------------------
