@@ -46,23 +46,24 @@ __global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t
 
 // One pass over the staged inserts: keys and staging indices, plus
 // stats[0] = max row, stats[1] = max column (range check), stats[2] = 1 if
-// some key is greater than its successor, stats[3] = 1 if some row is.
+// some key is greater than its successor (not sorted), stats[3] = 1 if some
+// row is (rows not grouped), stats[4] = 1 if some key is not below its
+// successor (not strictly increasing: duplicates or unsorted).
 __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols, uint64_t m,
-                             int cbits, uint64_t *__restrict__ keys, uint32_t *__restrict__ idx,
-                             unsigned *__restrict__ stats) {
+                             int cbits, unsigned *__restrict__ stats) {
     unsigned mr = 0, mc = 0;
-    bool d = false, g = false;
+    bool d = false, g = false, e = false;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t r = rows[i], c = cols[i];
         const uint64_t k = ((uint64_t)r << cbits) | c;
-        keys[i] = k;
-        idx[i] = (uint32_t)i;
         mr = max(mr, r);
         mc = max(mc, c);
         if (i + 1 < m) {
             const uint32_t r2 = rows[i + 1];
-            d |= k > (((uint64_t)r2 << cbits) | cols[i + 1]);
+            const uint64_t k2 = ((uint64_t)r2 << cbits) | cols[i + 1];
+            d |= k > k2;
+            e |= k >= k2;
             g |= r > r2;
         }
     }
@@ -71,13 +72,31 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
         mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
         mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
     }
-    const bool wd = __any_sync(0xffffffffu, d), wg = __any_sync(0xffffffffu, g);
+    const bool wd = __any_sync(0xffffffffu, d), wg = __any_sync(0xffffffffu, g), we = __any_sync(0xffffffffu, e);
     if ((threadIdx.x & 31) == 0) {
         atomicMax(stats, mr);
         atomicMax(stats + 1, mc);
         if (wd) stats[2] = 1u;
         if (wg) stats[3] = 1u;
+        if (we) stats[4] = 1u;
     }
+}
+
+// First lock of inserts in strictly increasing (row, col) order: the CSR is
+// the staged arrays themselves unless a value is zero (*zero = 1; then the
+// caller takes the general path).
+__global__ void first_direct_copy(const uint32_t *__restrict__ cols, const double *__restrict__ vals, uint64_t m,
+                                  uint32_t *__restrict__ out_cols, double *__restrict__ out_vals,
+                                  unsigned *__restrict__ zero) {
+    bool z = false;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const double v = vals[i];
+        z |= is_zero(v);
+        out_cols[i] = cols[i];
+        out_vals[i] = v;
+    }
+    if (__any_sync(0xffffffffu, z) && (threadIdx.x & 31) == 0) *zero = 1u;
 }
 
 // flags[0] = 1 if some key is greater than its successor (not sorted);
@@ -350,8 +369,7 @@ __global__ void first_gather(const uint64_t *__restrict__ keys, const uint32_t *
 // Keys, indices and order flags of a staged epoch, made once by lock_prepare
 // alongside the range check.
 struct Prepared {
-    DevBuf keys, idx;
-    unsigned unsorted = 1, ungrouped = 1;
+    unsigned unsorted = 1, ungrouped = 1, not_strict = 1;
     bool ready = false;
 };
 
@@ -364,17 +382,21 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
     // stable sort of a non-decreasing sequence is the identity. Inserts staged
     // row by row with columns in any order are sorted row by row on chip.
     unsigned f[2] = {1u, 1u};
-    if (pre && pre->ready) {
-        keys = std::move(pre->keys);
-        idx = std::move(pre->idx);
-        f[0] = pre->unsorted;
-        f[1] = pre->ungrouped;
-        pre->ready = false;
-    } else {
-        SPG_TRY(keys.alloc(m * sizeof(uint64_t), s));
-        SPG_TRY(idx.alloc(m * sizeof(uint32_t), s));
+    SPG_TRY(keys.alloc(m * sizeof(uint64_t), s));
+    SPG_TRY(idx.alloc(m * sizeof(uint32_t), s));
+    bool have_keys = false;
+    auto make_keys = [&]() -> int {
+        if (have_keys) return SPG_OK;
         lock_make_keys<<<g, LB, 0, s>>>(rows, cols, m, cbits, keys.as<uint64_t>(), idx.as<uint32_t>());
         SPG_LAUNCH_CHECK();
+        have_keys = true;
+        return SPG_OK;
+    };
+    if (pre && pre->ready) {
+        f[0] = pre->unsorted;
+        f[1] = pre->ungrouped;
+    } else {
+        SPG_TRY(make_keys());
         DevBuf flag;  // [0] keys unsorted, [1] rows not grouped
         SPG_TRY(flag.alloc(2 * sizeof(unsigned), s));
         SPG_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, 2 * sizeof(unsigned), s));
@@ -383,8 +405,8 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
         SPG_CUDA_TRY(cudaMemcpyAsync(f, flag.ptr, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
     }
-    if (!f[0]) return SPG_OK;
-    if (!f[1]) {
+    if (!f[0]) return make_keys();  // already sorted: the keys in input order
+    if (!f[1]) {  // the row-grouped sort reads rows and columns directly
         DevBuf s_off, keys2, idx2;
         SPG_TRY(s_off.alloc((n_rows + 1) * sizeof(uint64_t), s));
         offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
@@ -401,6 +423,7 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
             return SPG_OK;
         }
     }
+    SPG_TRY(make_keys());
     SPG_TRY(radix_sort_pairs_u64(c, keys.as<uint64_t>(), idx.as<uint32_t>(), m, rbits + cbits, s));
     return SPG_OK;
 }
@@ -444,6 +467,40 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
     const int cbits = bits_for(A->n_cols);
     DevBuf keys, idx, pos, orow, out_cols, out_vals, new_off;
     uint64_t nnz = 0;
+    if (m && pre && pre->ready && !pre->not_strict) {
+        // strictly increasing keys: no duplicates to resolve, nothing to sort;
+        // unless a value is zero, the staged arrays are the CSR
+        const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
+        DevBuf zero;
+        SPG_TRY(zero.alloc(sizeof(unsigned), s));
+        SPG_CUDA_TRY(cudaMemsetAsync(zero.ptr, 0, sizeof(unsigned), s));
+        SPG_TRY(out_cols.alloc(csr_alloc_elems(m) * sizeof(uint32_t), s));
+        SPG_TRY(out_vals.alloc(csr_alloc_elems(m) * sizeof(double), s));
+        first_direct_copy<<<g, LB, 0, s>>>(cols, vals, m, out_cols.as<uint32_t>(), out_vals.as<double>(),
+                                           zero.as<unsigned>());
+        SPG_LAUNCH_CHECK();
+        unsigned hz = 1;
+        SPG_CUDA_TRY(cudaMemcpyAsync(&hz, zero.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!hz) {
+            SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
+            offsets_from_sorted_rows<<<grid_for(n + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
+                rows, m, n, new_off.as<uint64_t>());
+            SPG_LAUNCH_CHECK();
+            A->invalidate_derived();
+            A->off = std::move(new_off);
+            A->cols = std::move(out_cols);
+            A->vals = std::move(out_vals);
+            A->nnz = m;
+            A->capacity = m;  // build_csr: exact
+            A->built = true;
+            A->may_have_zeros = false;
+            SPG_CUDA_TRY(cudaStreamSynchronize(s));
+            return SPG_OK;
+        }
+        out_cols.release();
+        out_vals.release();
+    }
     if (m) {
         const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
         SPG_TRY(sort_keys(c, rows, cols, m, n, A->n_cols, keys, idx, pre, s));
@@ -493,15 +550,13 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     Prepared pre;
     if (m) {
         DevBuf stats;
-        SPG_TRY(stats.alloc(4 * sizeof(unsigned), s));
-        SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 4 * sizeof(unsigned), s));
-        SPG_TRY(pre.keys.alloc(m * sizeof(uint64_t), s));
-        SPG_TRY(pre.idx.alloc(m * sizeof(uint32_t), s));
-        lock_prepare<<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
-            rows, cols, m, bits_for(A->n_cols), pre.keys.as<uint64_t>(), pre.idx.as<uint32_t>(), stats.as<unsigned>());
+        SPG_TRY(stats.alloc(5 * sizeof(unsigned), s));
+        SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 5 * sizeof(unsigned), s));
+        lock_prepare<<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(rows, cols, m, bits_for(A->n_cols),
+                                                                           stats.as<unsigned>());
         SPG_LAUNCH_CHECK();
-        unsigned h[4] = {0u, 0u, 1u, 1u};
-        SPG_CUDA_TRY(cudaMemcpyAsync(h, stats.ptr, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        unsigned h[5] = {0u, 0u, 1u, 1u, 1u};
+        SPG_CUDA_TRY(cudaMemcpyAsync(h, stats.ptr, 5 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
         if ((uint64_t)h[0] >= A->n_rows)
             return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: row_index out of range (%u >= %llu)", h[0],
@@ -511,6 +566,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
                              (unsigned long long)A->n_cols);
         pre.unsorted = h[2];
         pre.ungrouped = h[3];
+        pre.not_strict = h[4];
         pre.ready = true;
     }
     const uint64_t n = A->n_rows;

@@ -87,22 +87,29 @@ sg_merge_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ ac
         if (R == MG_RSMALL) rowcnt[i] = 0;
         return;
     }
+    // per list: cursor, entries left, and the head's column and value (loaded
+    // one step ahead, so a step waits for at most one round of loads)
+    constexpr bool PF = R <= MG_RSMALL;  // head values in registers (the wide version would spill)
     uint64_t cur[R];
     uint32_t left[R], head[R];
-    double a[R];
+    double a[R], hv[PF ? R : 1];
 #pragma unroll
     for (int t = 0; t < R; ++t) {
         cur[t] = 0;
         left[t] = 0;
         head[t] = 0;
         a[t] = 0.0;
+        if constexpr (PF) hv[t] = 0.0;
         if ((uint64_t)t < r) {
             const uint32_t k = acols[ab + t];
             const uint64_t b0 = boff[k];
             cur[t] = b0;
             left[t] = (uint32_t)(boff[k + 1] - b0);
             a[t] = avals[ab + t];
-            if (left[t]) head[t] = bcols[b0];
+            if (left[t]) {
+                head[t] = bcols[b0];
+                if constexpr (PF) hv[t] = bvals[b0];
+            }
         }
     }
     constexpr uint64_t NONE = 1ull << 32;
@@ -117,9 +124,15 @@ sg_merge_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ ac
 #pragma unroll
         for (int t = 0; t < R; ++t) {
             if (left[t] && head[t] == j) {
-                acc = __dadd_rn(acc, __dmul_rn(a[t], bvals[cur[t]]));
+                double bv;
+                if constexpr (PF) bv = hv[t];
+                else bv = bvals[cur[t]];
+                acc = __dadd_rn(acc, __dmul_rn(a[t], bv));
                 ++cur[t];
-                if (--left[t]) head[t] = bcols[cur[t]];
+                if (--left[t]) {
+                    head[t] = bcols[cur[t]];
+                    if constexpr (PF) hv[t] = bvals[cur[t]];
+                }
             }
         }
         if (acc != 0.0) {  // spgemm.hpp:44: v != V{}

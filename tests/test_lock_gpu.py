@@ -89,6 +89,18 @@ def test_lock_laplacian_relock_matches_oracle(ctx):
     assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(r, c, v), b]))
 
 
+@pytest.mark.parametrize("vals", [[1.0, 2.5, 2.0, -3.0, 7.0], [1.0, 0.0, 2.0, -0.0, 7.0]])
+def test_lock_strictly_sorted_input(ctx, vals):
+    """Strictly increasing (row, col) inserts install the staged arrays as
+    the CSR directly; a zero among them sends the lock down the general
+    path, which drops it."""
+    rows = np.array([0, 0, 1, 2, 4], np.uint32)
+    cols = np.array([1, 3, 0, 2, 0], np.uint32)
+    vals = np.array(vals)
+    A = gpu_lock(ctx, 5, 4, [(rows, cols, vals)])
+    assert_csr_equal(A.download(), oracle.lock_epochs(5, 4, [(rows, cols, vals)]))
+
+
 def test_lock_presorted_input_with_duplicates(ctx):
     """Inserts already in (row, col) order skip the sort; duplicates still
     resolve to the last write and a last zero still deletes."""
