@@ -148,7 +148,7 @@ def run_ours(args):
 
     for m in mats:
         m["selected"] = m["A"].selected_spmv()  # SPMV_AUTO: the learned selector's pick
-        t_all, best = m["A"].autotune(5)  # exhaustive autotuner: the judge
+        t_all, best = m["A"].autotune(5)  # exhaustive autotuner: the yardstick of the selector
         m["autotuned"] = best
         m["autotune_ms"] = t_all
 

@@ -39,7 +39,7 @@ enum spg_status {
     SPG_ERR_NO_MEMORY = 4,        /* std::bad_alloc: device allocation failed */
     SPG_ERR_CUDA = 5,             /* CUDA runtime error (no device, launch failure, ...) */
     SPG_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up; context stays usable */
-    SPG_ERR_UNSUPPORTED = 7       /* valid request this build does not serve */
+    SPG_ERR_UNSUPPORTED = 7       /* valid request that libspg does not serve */
 };
 
 /* ---- SpMV variants (spg_spmv `variant`) --------------------------------- */

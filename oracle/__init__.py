@@ -3,8 +3,8 @@ the Spira source tree is present, Spira itself compiled from its sources
 (oracle/_ref/libspira_ref.so via oracle/Makefile).
 
 TEST INFRASTRUCTURE ONLY. Imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline / reference arm as the checker and the CPU
-baseline; never by the product (spira_gb300), which has no CPU path.
+by bench.py's CPU-baseline / reference arm as the reference results and the
+CPU baseline; never by the product (spira_gb300), which has no CPU path.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 /*
  * spira_oracle.c — CPU restatement of Spira's sparse hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker the GPU engine is
+ * TEST INFRASTRUCTURE ONLY. This file is the reference the GPU engine is
  * compared against and the CPU baseline bench.py times beside it. The
  * product (libspg.so) never links, loads or calls it.
  *

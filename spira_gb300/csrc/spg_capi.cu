@@ -95,7 +95,7 @@ int spg_ctx_create(int device, spg_ctx **out) {
     cudaDeviceProp prop;
     SPG_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
     if (prop.major < 10)
-        return set_error(SPG_ERR_UNSUPPORTED, "spg_ctx_create: device %d is sm_%d%d; this build targets sm_103a",
+        return set_error(SPG_ERR_UNSUPPORTED, "spg_ctx_create: device %d is sm_%d%d; libspg targets sm_103a",
                          device, prop.major, prop.minor);
     spg_ctx *c = new (std::nothrow) spg_ctx();
     if (!c) return set_error(SPG_ERR_NO_MEMORY, "spg_ctx_create: host allocation failed");

@@ -121,17 +121,43 @@ sg_merge_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ ac
             if (left[t] && head[t] < j) j = head[t];
         if (j == NONE) break;
         double acc = 0.0;  // ValueTraits zero; acc[j] default-constructs to V{}
+        if constexpr (PF) {
+            // One multiply and one add per contribution, issued for the whole
+            // warp: pick the lowest list whose head is j, add its product,
+            // advance it, repeat. (An add per list and per step, masked to the
+            // lanes that need it, kept the FP64 pipe busy with idle lanes:
+            // a warp FP64 instruction costs the same whatever its mask.)
+            while (true) {
+                int sel = -1;
+                double av = 0.0, bv = 0.0;
 #pragma unroll
-        for (int t = 0; t < R; ++t) {
-            if (left[t] && head[t] == j) {
-                double bv;
-                if constexpr (PF) bv = hv[t];
-                else bv = bvals[cur[t]];
-                acc = __dadd_rn(acc, __dmul_rn(a[t], bv));
-                ++cur[t];
-                if (--left[t]) {
-                    head[t] = bcols[cur[t]];
-                    if constexpr (PF) hv[t] = bvals[cur[t]];
+                for (int t = R - 1; t >= 0; --t) {
+                    if (left[t] && head[t] == j) {
+                        sel = t;
+                        av = a[t];
+                        bv = hv[t];
+                    }
+                }
+                if (sel < 0) break;
+                acc = __dadd_rn(acc, __dmul_rn(av, bv));
+#pragma unroll
+                for (int t = 0; t < R; ++t) {
+                    if (t == sel) {
+                        ++cur[t];
+                        if (--left[t]) {
+                            head[t] = bcols[cur[t]];
+                            hv[t] = bvals[cur[t]];
+                        }
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int t = 0; t < R; ++t) {
+                if (left[t] && head[t] == j) {
+                    acc = __dadd_rn(acc, __dmul_rn(a[t], bvals[cur[t]]));
+                    ++cur[t];
+                    if (--left[t]) head[t] = bcols[cur[t]];
                 }
             }
         }

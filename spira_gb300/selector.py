@@ -6,7 +6,7 @@ device) and predicts, for each of the K SpMV variants, log(time / fastest
 time). SPG_SPMV_AUTO then takes the argmin. The network is trained on the GPU
 with libspg's own forward / backward / Adam kernels on timings that the
 exhaustive autotuner (spg_spmv_autotune) measures on a generated corpus; the
-autotuner stays the fallback and the judge (regret is reported against it).
+autotuner stays the fallback and the yardstick (regret is reported against it).
 
 Corpus: five families (banded with bandwidth 3..201, block-diagonal with
 blocks 4..64, power-law with Zipf alpha 1.5..2.5, uniform-random with
