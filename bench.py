@@ -566,6 +566,7 @@ PROFILE_CASES = {
     "lock_zipf1m": (1_000_000, "lock"),
     "lock_laplacian2d": (GRID * GRID, "lock"),
     "relock_zipf1m": (1_000_000, "relock"),
+    "batched256": (256, "batched"),  # the batched workload's first 256 matrices
     "transpose_laplacian3d": (100 ** 3, "transpose"),
     "spgemm_laplacian3d": (100 ** 3, "spgemm"),
     "spgemm_uniform200k": (200_000, "spgemm"),
@@ -577,6 +578,21 @@ def run_profile_op(ctx, case, n, kind, reps):
     import spira_gb300 as sg
     from spira_gb300 import gen, gen_device
     ms = []
+    if kind == "batched":
+        import torch
+        from spira_gb300 import batched as bt
+        mats, Xs, Ys, ks, nz = bt.build(ctx, n, 2024)
+        B = sg.Batch(ctx, mats, Xs, Ys, ks, config=-1)
+        B.run(ctx.stream)
+        for _ in range(reps):
+            ctx.sync()
+            t0 = time.perf_counter()
+            B.run(ctx.stream)
+            ctx.sync()
+            ms.append((time.perf_counter() - t0) * 1e3)
+        print(json.dumps({"profile_case": case, "matrices": n, "nnz": int(sum(nz)), "config": B.config(),
+                          "ms_per_call": [round(t, 3) for t in ms]}))
+        return
     if kind == "relock":
         import torch
         r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
@@ -639,7 +655,7 @@ def run_profile_case(args):
     ctx = sg.Context(0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     n, kind = PROFILE_CASES[args.profile_case]
-    if kind in ("lock", "relock", "transpose", "spgemm"):
+    if kind in ("lock", "relock", "transpose", "spgemm", "batched"):
         run_profile_op(ctx, args.profile_case, n, kind, args.reps)
         return
     if kind == "zipf":
@@ -655,6 +671,21 @@ def run_profile_case(args):
     y = torch.empty(n, dtype=torch.float64, device="cuda:0")
     ctx.sync()
     out = {}
+    if args.host:  # host-buffer SpMV through the C ABI (pinned x and y), wall time per call
+        xh = torch.from_numpy(gen.dense_x(n, 3)).pin_memory()
+        yh = torch.empty(n, dtype=torch.float64).pin_memory()
+        for name in args.variants.split(","):
+            vid = sg.SPMV_VARIANTS[name]
+            A.spmv_host(xh.numpy(), yh.numpy(), variant=vid)
+            ts = []
+            for _ in range(args.reps):
+                t0 = time.perf_counter()
+                A.spmv_host(xh.numpy(), yh.numpy(), variant=vid)
+                ts.append((time.perf_counter() - t0) * 1e3)
+            out[name] = [round(t, 4) for t in ts]
+        print(json.dumps({"profile_case": args.profile_case, "host": True, "n_rows": n, "nnz": A.nnz,
+                          "ms_per_call": out}))
+        return
     with torch.cuda.stream(stream):
         for name in args.variants.split(","):
             vid = sg.SPMV_VARIANTS[name]
@@ -676,6 +707,7 @@ def main():
                     help="run a few SpMVs of one matrix (for ncu captures) instead of the bench")
     ap.add_argument("--variants", default="adaptive16", help="with --profile-case: comma-separated variant names")
     ap.add_argument("--reps", type=int, default=2, help="with --profile-case: SpMVs per variant after one warm-up")
+    ap.add_argument("--host", action="store_true", help="with --profile-case: time host-buffer SpMV calls")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)

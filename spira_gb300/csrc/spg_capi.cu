@@ -103,6 +103,9 @@ int spg_ctx_create(int device, spg_ctx **out) {
     c->n_sms = prop.multiProcessorCount;
     c->l2_bytes = prop.l2CacheSize;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < Ctx::N_HOST_EVENTS && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&c->host_events[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&c->pool, device);
     if (e == cudaSuccess) {
         uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
@@ -118,6 +121,9 @@ int spg_ctx_create(int device, spg_ctx **out) {
     }
     if (e != cudaSuccess) {
         if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+        for (cudaEvent_t ev : c->host_events)
+            if (ev) cudaEventDestroy(ev);
         if (c->h_status) cudaFreeHost(c->h_status);
         delete c;
         return set_error(SPG_ERR_CUDA, "spg_ctx_create: %s", cudaGetErrorString(e));
@@ -139,8 +145,12 @@ int spg_ctx_destroy(spg_ctx *c) {
     c->xbuf.release();
     c->ybuf.release();
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->copy_stream);
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->h_status) cudaFreeHost(c->h_status);
+    for (cudaEvent_t ev : c->host_events)
+        if (ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(c->copy_stream);
     cudaStreamDestroy(c->stream);
     delete c;
     return SPG_OK;
@@ -390,10 +400,57 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
     if (c->ybuf.bytes < y_len * sizeof(double)) SPG_TRY(c->ybuf.alloc(y_len * sizeof(double), s));
     if (x_len)
         SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
-    SPG_TRY(spmv_launch(c, A, c->xbuf.as<double>(), c->ybuf.as<double>(), variant, s));
-    if (y_len)
-        SPG_CUDA_TRY(cudaMemcpyAsync(y, c->ybuf.ptr, y_len * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const double *dx = c->xbuf.as<double>();
+    double *dy = c->ybuf.as<double>();
+    // Large matrices: compute y in row blocks and copy each block back on a
+    // second stream while the next block computes (the host link, ~200 GB/s,
+    // otherwise idles during the SpMV).
+    constexpr uint64_t PIPELINE_MIN_NNZ = 4u << 20;
+    constexpr int NB = 4;  // the last block's copy and the one-block fix-up look-ahead stay exposed;
+                           // 8 blocks measured slower (per-block launch and tail costs)
+    const bool row_parallel = variant == SPG_SPMV_SCALAR || (variant >= SPG_SPMV_VECTOR2 && variant <= SPG_SPMV_VECTOR32);
+    const bool adaptive =
+        variant == SPG_SPMV_ADAPTIVE || variant == SPG_SPMV_ADAPTIVE16 || variant == SPG_SPMV_INTERLEAVED;
+    std::vector<uint64_t> rows;
+    if (A->nnz >= PIPELINE_MIN_NNZ && y_len && (row_parallel || adaptive)) {
+        if (row_parallel) {
+            rows.resize(NB + 1);
+            for (int b = 0; b <= NB; ++b) rows[b] = y_len * (uint64_t)b / NB;
+        } else {
+            SPG_TRY(spmv_adaptive_blocks(c, A, variant, NB, &rows, s));
+        }
+    }
+    const int nb = rows.empty() ? 0 : (int)rows.size() - 1;
+    if (nb < 2) {
+        SPG_TRY(spmv_launch(c, A, dx, dy, variant, s));
+        if (y_len) SPG_CUDA_TRY(cudaMemcpyAsync(y, dy, y_len * sizeof(double), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        return c->take_status();
+    }
+    // stage i makes rows [rows[i-1], rows[i]) final (row-parallel: stage i
+    // computes block i, so its rows are [rows[i], rows[i+1]))
+    const int stages = row_parallel ? nb : nb + 1;
+    for (int i = 0; i < stages; ++i) {
+        uint64_t r0, r1;
+        if (row_parallel) {
+            r0 = rows[i];
+            r1 = rows[i + 1];
+            SPG_TRY(spmv_launch_rows(c, A, dx, dy, variant, r0, r1, s));
+        } else {
+            SPG_TRY(spmv_adaptive_stage(c, A, dx, dy, variant, i, s));
+            if (i == 0) continue;
+            r0 = rows[i - 1];
+            r1 = rows[i];
+        }
+        if (r1 <= r0) continue;
+        cudaEvent_t ev = c->host_events[i % Ctx::N_HOST_EVENTS];
+        SPG_CUDA_TRY(cudaEventRecord(ev, s));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, ev, 0));
+        SPG_CUDA_TRY(cudaMemcpyAsync(y + r0, dy + r0, (r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                     c->copy_stream));
+    }
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(c->copy_stream));
     return c->take_status();
 }
 

@@ -87,6 +87,10 @@ struct SpmvPlan {
     DevBuf aux;              // variant-specific scratch (carry-outs)
     DevBuf extra0, extra1, extra2;
     DevBuf extra3, extra4;
+    // Host-side block split for the pipelined host SpMV (adaptive variants):
+    // host_rows[b] = first row of block b, host_rows[host_nb] = n_rows.
+    int host_nb = 0;
+    std::vector<uint64_t> host_rows;
 };
 
 struct Csr;
@@ -120,8 +124,12 @@ struct Ctx {
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
     int ensure_pinned(size_t bytes);
-    // Device vectors reused by spg_spmv_host.
+    // Device vectors reused by spg_spmv_host, the stream that copies y back
+    // while later row blocks compute, and the events between the two.
     DevBuf xbuf, ybuf;
+    cudaStream_t copy_stream = nullptr;
+    static constexpr int N_HOST_EVENTS = 8;
+    cudaEvent_t host_events[N_HOST_EVENTS] = {};
     // SpMV variant choice: policy and the loaded selector (spg_tune.cu).
     int spmv_policy = SPG_POLICY_SELECTOR;
     DevBuf model;  // FP32 selector blob
@@ -255,6 +263,17 @@ int selector_load_default(Ctx *c);
 // (spg_spmv_adaptive.cu); each builds and caches its plan on first use.
 int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s);
 int build_adaptive_plan(Ctx *c, Csr *A, int variant, cudaStream_t s);
+// Pipelined form for the host entry point: splits the chunks into at most nb
+// blocks (fewer if a row could outrun the one-block look-ahead of the fix-up)
+// and returns the first row of each block (rows->back() = n_rows). Stage i
+// (0 <= i <= blocks) enqueues block i's chunks (i < blocks) and block i-1's
+// fix-up (i >= 1): after stage i, rows [rows[i-1], rows[i]) are final.
+int spmv_adaptive_blocks(Ctx *c, Csr *A, int variant, int nb, std::vector<uint64_t> *rows, cudaStream_t s);
+int spmv_adaptive_stage(Ctx *c, Csr *A, const double *x, double *y, int variant, int i, cudaStream_t s);
+// Rows [r0, r1) of a row-parallel variant (SCALAR, VECTOR*); others give
+// SPG_ERR_UNSUPPORTED.
+int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, uint64_t r0, uint64_t r1,
+                     cudaStream_t s);
 // The cached plan slot of one of those variants.
 inline SpmvPlan &adaptive_plan_of(Csr *A, int variant) {
     return variant == SPG_SPMV_INTERLEAVED ? A->plan_inter : A->plan_adaptive;

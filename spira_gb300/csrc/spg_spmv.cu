@@ -444,6 +444,36 @@ static int build_merge_plan(Ctx *c, Csr *A, cudaStream_t s) {
     return SPG_OK;
 }
 
+int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, uint64_t r0, uint64_t r1,
+                     cudaStream_t s) {
+    (void)c;
+    if (r1 <= r0) return SPG_OK;
+    const uint64_t n = r1 - r0;
+    const uint64_t *off = A->d_off() + r0;  // offsets stay absolute positions in cols / vals
+    const uint32_t *cols = A->d_cols();
+    const double *vals = A->d_vals();
+    double *yb = y + r0;
+    switch (variant) {
+        case SPG_SPMV_SCALAR:
+            spmv_scalar<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(off, cols, vals, x, yb, n);
+            break;
+#define SPG_VEC_CASE(ID, G)                                                                  \
+    case ID:                                                                                 \
+        spmv_vector<G><<<grid_for(n * G, BLOCK), BLOCK, 0, s>>>(off, cols, vals, x, yb, n);  \
+        break;
+        SPG_VEC_CASE(SPG_SPMV_VECTOR2, 2)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR4, 4)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR8, 8)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR16, 16)
+        SPG_VEC_CASE(SPG_SPMV_VECTOR32, 32)
+#undef SPG_VEC_CASE
+        default:
+            return SPG_ERR_UNSUPPORTED;
+    }
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
 int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s) {
     const uint64_t n = A->n_rows;
     if (n == 0) return SPG_OK;

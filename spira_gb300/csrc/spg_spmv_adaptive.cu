@@ -92,15 +92,15 @@ __global__ void __launch_bounds__(256, 4)
 spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, const double *__restrict__ x,
          double *__restrict__ y, uint64_t nnz, const unsigned *__restrict__ bitmap,
          const uint32_t *__restrict__ chunk_base, const uint32_t *__restrict__ nzrow, Rec *__restrict__ recs,
-         uint64_t n_chunks) {
-    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+         uint64_t c0, uint64_t c1) {  // chunks [c0, c1)
+    const uint64_t w = c0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (w >= n_chunks) return;
+    if (w >= c1) return;
     const uint64_t p0 = w * (32ull * ITEMS) + (uint64_t)lane * ITEMS;
     unsigned word = 0;
     if (p0 < nnz) {
         word = bitmap[p0 >> 5] >> (p0 & 31);
-        if (ITEMS < 32) word &= (1u << ITEMS) - 1u;
+        if constexpr (ITEMS < 32) word &= (1u << ITEMS) - 1u;
         if (nnz - p0 < (uint64_t)ITEMS) word &= (1u << (unsigned)(nnz - p0)) - 1u;
     }
     // row starts before my first item
@@ -250,10 +250,12 @@ __global__ void seg_interleave(const uint32_t *__restrict__ cols, const double *
 // Rows crossing chunk boundaries: each run of records with the same row
 // (at most one NONE record between two of them) is summed in chunk order by
 // the thread holding its first record.
-__global__ void seg_fixup(const Rec *__restrict__ recs, uint64_t n_recs, const uint32_t *__restrict__ nzrow,
-                          double *__restrict__ y) {
-    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n_recs) return;
+// Runs starting at records [q0, q1) are summed (a run may read on up to
+// n_recs).
+__global__ void seg_fixup(const Rec *__restrict__ recs, uint64_t q0, uint64_t q1, uint64_t n_recs,
+                          const uint32_t *__restrict__ nzrow, double *__restrict__ y) {
+    const uint64_t q = q0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= q1) return;
     const uint32_t row = recs[q].row;
     if (row == NONE) return;
     if (q > 0) {
@@ -274,6 +276,15 @@ __global__ void seg_fixup(const Rec *__restrict__ recs, uint64_t n_recs, const u
         ++k;
     }
     y[nzrow ? nzrow[row] : row] = s;
+}
+
+__global__ void seg_max_row(const uint64_t *__restrict__ off, uint64_t n, unsigned long long *__restrict__ mx) {
+    unsigned long long m = 0;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x)
+        m = max(m, (unsigned long long)(off[r + 1] - off[r]));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
 }
 
 __global__ void seg_empty_rows(const uint32_t *__restrict__ empty, uint64_t n_empty, double *__restrict__ y) {
@@ -348,33 +359,118 @@ int build_adaptive_plan(Ctx *c, Csr *A, int variant, cudaStream_t s) {
     return SPG_OK;
 }
 
+namespace {
+
+// The chunk kernel over chunks [c0, c1).
+int launch_seg(const SpmvPlan &P, const Csr *A, const double *x, double *y, int variant, uint64_t c0, uint64_t c1,
+               cudaStream_t s) {
+    if (c1 <= c0) return SPG_OK;
+    const uint32_t *nzrow = P.count1 ? P.extra1.as<uint32_t>() : nullptr;
+    const unsigned grid = grid_for((c1 - c0) * 32, 256);
+    if (variant == SPG_SPMV_INTERLEAVED)
+        spmv_seg<16, 8, true><<<grid, 256, 0, s>>>(P.extra3.as<uint32_t>(), P.extra4.as<double>(), x, y, A->nnz,
+                                                P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
+                                                P.aux.as<Rec>(), c0, c1);
+    else if (variant == SPG_SPMV_ADAPTIVE16)
+        spmv_seg<16, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
+                                                 P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), c0, c1);
+    else
+        spmv_seg<32, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
+                                                 P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), c0, c1);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+// The fix-up of the runs starting at records of chunks [c0, c1).
+int launch_fixup(const SpmvPlan &P, double *y, uint64_t c0, uint64_t c1, cudaStream_t s) {
+    if (c1 <= c0) return SPG_OK;
+    const uint32_t *nzrow = P.count1 ? P.extra1.as<uint32_t>() : nullptr;
+    seg_fixup<<<grid_for(2 * (c1 - c0), 256), 256, 0, s>>>(P.aux.as<Rec>(), 2 * c0, 2 * c1, 2 * P.n_items, nzrow, y);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+int launch_empty_rows(const SpmvPlan &P, double *y, cudaStream_t s) {
+    if (!P.count1) return SPG_OK;
+    seg_empty_rows<<<grid_for(P.count1, 256), 256, 0, s>>>(P.extra2.as<uint32_t>(), P.count1, y);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+}  // namespace
+
 int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s) {
     SPG_TRY(build_adaptive_plan(c, A, variant, s));
     const SpmvPlan &P = adaptive_plan_of(A, variant);
+    SPG_TRY(launch_seg(P, A, x, y, variant, 0, P.n_items, s));
+    SPG_TRY(launch_fixup(P, y, 0, P.n_items, s));
+    SPG_TRY(launch_empty_rows(P, y, s));
+    return SPG_OK;
+}
+
+int spmv_adaptive_blocks(Ctx *c, Csr *A, int variant, int nb, std::vector<uint64_t> *rows, cudaStream_t s) {
+    SPG_TRY(build_adaptive_plan(c, A, variant, s));
+    SpmvPlan &P = adaptive_plan_of(A, variant);
     const uint64_t nch = P.n_items;
-    const uint32_t *nzrow = P.count1 ? P.extra1.as<uint32_t>() : nullptr;
-    if (nch) {
-        const unsigned grid = grid_for(nch * 32, 256);
-        if (variant == SPG_SPMV_INTERLEAVED)
-            spmv_seg<16, 8, true><<<grid, 256, 0, s>>>(P.extra3.as<uint32_t>(), P.extra4.as<double>(), x, y, A->nnz,
-                                                    P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
-                                                    P.aux.as<Rec>(), nch);
-        else if (variant == SPG_SPMV_ADAPTIVE16)
-            spmv_seg<16, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz,
-                                                     P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
-                                                     P.aux.as<Rec>(), nch);
-        else
-            spmv_seg<32, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz,
-                                                     P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
-                                                     P.aux.as<Rec>(), nch);
-        SPG_LAUNCH_CHECK();
-        seg_fixup<<<grid_for(2 * nch, 256), 256, 0, s>>>(P.aux.as<Rec>(), 2 * nch, nzrow, y);
-        SPG_LAUNCH_CHECK();
+    if (P.host_nb == nb && (int)P.host_rows.size() == nb + 1) {
+        *rows = P.host_rows;
+        return SPG_OK;
     }
-    if (P.count1) {
-        seg_empty_rows<<<grid_for(P.count1, 256), 256, 0, s>>>(P.extra2.as<uint32_t>(), P.count1, y);
+    // Blocks must be long enough that a row starting in block b ends by the
+    // end of block b + 1 (the fix-up of block b reads ahead one block).
+    uint64_t max_row = 0;
+    if (A->n_rows) {
+        DevBuf mx;
+        SPG_TRY(mx.alloc(sizeof(unsigned long long), s));
+        SPG_CUDA_TRY(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned long long), s));
+        seg_max_row<<<grid_for(A->n_rows, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(
+            A->d_off(), A->n_rows, mx.as<unsigned long long>());
         SPG_LAUNCH_CHECK();
+        unsigned long long h = 0;
+        SPG_CUDA_TRY(cudaMemcpyAsync(&h, mx.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        max_row = h;
     }
+    const uint64_t chunk_nnz = 32ull * (variant == SPG_SPMV_ADAPTIVE ? 32 : 16);
+    while (nb > 1 && (nch / nb) * chunk_nnz < max_row + 2 * chunk_nnz) --nb;
+    if (nb < 1) nb = 1;
+    // first (actual) row starting at or after each block's first chunk
+    rows->assign(nb + 1, 0);
+    const uint64_t n_nonempty = A->n_rows - P.count1;
+    for (int b = 1; b < nb; ++b) {
+        const uint64_t ch = nch * (uint64_t)b / (uint64_t)nb;  // < nch
+        uint32_t v = 0;  // non-empty rows starting before chunk ch = index of the first one at or after it
+        SPG_CUDA_TRY(cudaMemcpyAsync(&v, P.extra0.as<uint32_t>() + ch, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        uint64_t r = A->n_rows;
+        if (v < n_nonempty) {
+            r = v;
+            if (P.count1) {  // map to the actual row
+                uint32_t a = 0;
+                SPG_CUDA_TRY(cudaMemcpyAsync(&a, P.extra1.as<uint32_t>() + v, sizeof(uint32_t),
+                                             cudaMemcpyDeviceToHost, s));
+                SPG_CUDA_TRY(cudaStreamSynchronize(s));
+                r = a;
+            }
+        }
+        (*rows)[b] = r;
+    }
+    (*rows)[0] = 0;
+    (*rows)[nb] = A->n_rows;
+    P.host_nb = nb;
+    P.host_rows = *rows;
+    return SPG_OK;
+}
+
+int spmv_adaptive_stage(Ctx *c, Csr *A, const double *x, double *y, int variant, int i, cudaStream_t s) {
+    (void)c;
+    const SpmvPlan &P = adaptive_plan_of(A, variant);
+    const int nb = P.host_nb;
+    const uint64_t nch = P.n_items;
+    auto cb = [&](int b) { return nch * (uint64_t)b / (uint64_t)nb; };
+    if (i == 0) SPG_TRY(launch_empty_rows(P, y, s));
+    if (i < nb) SPG_TRY(launch_seg(P, A, x, y, variant, cb(i), cb(i + 1), s));
+    if (i >= 1) SPG_TRY(launch_fixup(P, y, cb(i - 1), cb(i), s));
     return SPG_OK;
 }
 

@@ -121,6 +121,28 @@ def test_plans_follow_relock(ctx):
     check_all_variants(A, x)
 
 
+def test_host_spmv_pipelined_blocks_match_device_path(ctx):
+    """Host-buffer SpMV of a large matrix runs in row blocks whose results are
+    copied back while the next block computes; y must be bit-identical to the
+    one-launch device path, with empty rows and long rows crossing blocks."""
+    import torch
+    n = 700_000
+    lengths = np.where(np.arange(n) % 3 == 1, 0, 10).astype(np.int64)
+    lengths[::50_000] = 12_000  # long rows (their chunks straddle block boundaries)
+    r, c, v = _csr_from_rows(lengths, n, seed=77)
+    A = build(ctx, n, n, [(r, c, v)])
+    assert A.nnz >= (4 << 20)
+    x = gen.dense_x(n, 78)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty(n, dtype=torch.float64, device="cuda")
+    for name, var in VARIANTS:
+        if var == sg.SPMV_AUTO:
+            continue
+        A.spmv(xd, yd, var)
+        ctx.sync()
+        np.testing.assert_array_equal(A.spmv_host(x, variant=var), yd.cpu().numpy(), err_msg=name)
+
+
 def test_gather_probe(ctx):
     r = ctx.probe_gather_rate(1 << 20, 1 << 22)
     assert 1e9 < r < 1e13
