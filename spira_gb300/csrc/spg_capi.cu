@@ -60,6 +60,17 @@ __global__ void csr_get_kernel(const uint64_t *__restrict__ off, const uint32_t 
 }
 
 }  // namespace
+
+// True for page-locked (pinned or registered) host memory.
+static bool host_pinned(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 }  // namespace spg
 
 using namespace spg;
@@ -104,8 +115,11 @@ int spg_ctx_create(int device, spg_ctx **out) {
     c->l2_bytes = prop.l2CacheSize;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
-    for (int i = 0; i < Ctx::N_HOST_EVENTS && e == cudaSuccess; ++i)
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->upload_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < Ctx::N_HOST_EVENTS && e == cudaSuccess; ++i) {
         e = cudaEventCreateWithFlags(&c->host_events[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->upload_events[i], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&c->pool, device);
     if (e == cudaSuccess) {
         uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
@@ -122,8 +136,11 @@ int spg_ctx_create(int device, spg_ctx **out) {
     if (e != cudaSuccess) {
         if (c->stream) cudaStreamDestroy(c->stream);
         if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
-        for (cudaEvent_t ev : c->host_events)
-            if (ev) cudaEventDestroy(ev);
+        if (c->upload_stream) cudaStreamDestroy(c->upload_stream);
+        for (int i = 0; i < Ctx::N_HOST_EVENTS; ++i) {
+            if (c->host_events[i]) cudaEventDestroy(c->host_events[i]);
+            if (c->upload_events[i]) cudaEventDestroy(c->upload_events[i]);
+        }
         if (c->h_status) cudaFreeHost(c->h_status);
         delete c;
         return set_error(SPG_ERR_CUDA, "spg_ctx_create: %s", cudaGetErrorString(e));
@@ -146,10 +163,14 @@ int spg_ctx_destroy(spg_ctx *c) {
     c->ybuf.release();
     cudaStreamSynchronize(c->stream);
     cudaStreamSynchronize(c->copy_stream);
+    cudaStreamSynchronize(c->upload_stream);
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->h_status) cudaFreeHost(c->h_status);
-    for (cudaEvent_t ev : c->host_events)
-        if (ev) cudaEventDestroy(ev);
+    for (int i = 0; i < Ctx::N_HOST_EVENTS; ++i) {
+        if (c->host_events[i]) cudaEventDestroy(c->host_events[i]);
+        if (c->upload_events[i]) cudaEventDestroy(c->upload_events[i]);
+    }
+    cudaStreamDestroy(c->upload_stream);
     cudaStreamDestroy(c->copy_stream);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -398,8 +419,6 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
         return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: unknown variant %d", variant);
     if (c->xbuf.bytes < x_len * sizeof(double)) SPG_TRY(c->xbuf.alloc(x_len * sizeof(double), s));
     if (c->ybuf.bytes < y_len * sizeof(double)) SPG_TRY(c->ybuf.alloc(y_len * sizeof(double), s));
-    if (x_len)
-        SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
     const double *dx = c->xbuf.as<double>();
     double *dy = c->ybuf.as<double>();
     // Large matrices: compute y in row blocks and copy each block back on a
@@ -422,35 +441,103 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
     }
     const int nb = rows.empty() ? 0 : (int)rows.size() - 1;
     if (nb < 2) {
+        if (x_len) SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
         SPG_TRY(spmv_launch(c, A, dx, dy, variant, s));
         if (y_len) SPG_CUDA_TRY(cudaMemcpyAsync(y, dy, y_len * sizeof(double), cudaMemcpyDeviceToHost, s));
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
         return c->take_status();
     }
-    // stage i makes rows [rows[i-1], rows[i]) final (row-parallel: stage i
-    // computes block i, so its rows are [rows[i], rows[i+1]))
-    const int stages = row_parallel ? nb : nb + 1;
-    for (int i = 0; i < stages; ++i) {
-        uint64_t r0, r1;
-        if (row_parallel) {
-            r0 = rows[i];
-            r1 = rows[i + 1];
-            SPG_TRY(spmv_launch_rows(c, A, dx, dy, variant, r0, r1, s));
-        } else {
-            SPG_TRY(spmv_adaptive_stage(c, A, dx, dy, variant, i, s));
-            if (i == 0) continue;
-            r0 = rows[i - 1];
-            r1 = rows[i];
+    // Row-parallel variants: x also goes up in nb column pieces on a third
+    // stream, and a row block starts once the pieces up to the largest column
+    // it reads have arrived (banded and stencil matrices overlap all three:
+    // upload, compute, download). Other variants read x anywhere: whole upload.
+    const uint64_t xc = (x_len + nb - 1) / (uint64_t)nb;  // columns per piece
+    if (row_parallel && x_len) SPG_TRY(spmv_row_block_reach(c, A, nb, s));
+    cudaEvent_t fork = c->host_events[Ctx::N_HOST_EVENTS - 1], copy_join = c->host_events[Ctx::N_HOST_EVENTS - 2];
+    cudaEvent_t upload_join = c->upload_events[Ctx::N_HOST_EVENTS - 1];
+    // everything on s, with the side streams forked from and joined back to it
+    auto enqueue = [&]() -> int {
+        SPG_CUDA_TRY(cudaEventRecord(fork, s));  // the staging buffers are ordered on s
+        SPG_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, fork, 0));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(c->upload_stream, fork, 0));
+        if (row_parallel && x_len) {
+            for (int j = 0; j < nb; ++j) {
+                const uint64_t c0 = std::min(x_len, xc * j), c1 = std::min(x_len, xc * (j + 1));
+                if (c1 > c0)
+                    SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.as<double>() + c0, x + c0, (c1 - c0) * sizeof(double),
+                                                 cudaMemcpyHostToDevice, c->upload_stream));
+                SPG_CUDA_TRY(cudaEventRecord(c->upload_events[j], c->upload_stream));
+            }
+        } else if (x_len) {
+            SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
         }
-        if (r1 <= r0) continue;
-        cudaEvent_t ev = c->host_events[i % Ctx::N_HOST_EVENTS];
-        SPG_CUDA_TRY(cudaEventRecord(ev, s));
-        SPG_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, ev, 0));
-        SPG_CUDA_TRY(cudaMemcpyAsync(y + r0, dy + r0, (r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost,
-                                     c->copy_stream));
+        // stage i makes rows [rows[i-1], rows[i]) final (row-parallel: stage i
+        // computes block i, so its rows are [rows[i], rows[i+1]))
+        const int stages = row_parallel ? nb : nb + 1;
+        for (int i = 0; i < stages; ++i) {
+            uint64_t r0, r1;
+            if (row_parallel) {
+                r0 = rows[i];
+                r1 = rows[i + 1];
+                if (x_len) {
+                    const int64_t reach = A->host_reach[i];
+                    const int piece = reach < 0 ? 0 : (int)std::min<uint64_t>(nb - 1, (uint64_t)reach / xc);
+                    SPG_CUDA_TRY(cudaStreamWaitEvent(s, c->upload_events[piece], 0));
+                }
+                SPG_TRY(spmv_launch_rows(c, A, dx, dy, variant, r0, r1, s));
+            } else {
+                SPG_TRY(spmv_adaptive_stage(c, A, dx, dy, variant, i, s));
+                if (i == 0) continue;
+                r0 = rows[i - 1];
+                r1 = rows[i];
+            }
+            if (r1 <= r0) continue;
+            cudaEvent_t ev = c->host_events[i];
+            SPG_CUDA_TRY(cudaEventRecord(ev, s));
+            SPG_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, ev, 0));
+            SPG_CUDA_TRY(cudaMemcpyAsync(y + r0, dy + r0, (r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                         c->copy_stream));
+        }
+        SPG_CUDA_TRY(cudaEventRecord(copy_join, c->copy_stream));
+        SPG_CUDA_TRY(cudaEventRecord(upload_join, c->upload_stream));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(s, copy_join, 0));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(s, upload_join, 0));
+        return SPG_OK;
+    };
+    // With pinned x and y the whole sequence is recorded once as a CUDA graph
+    // and replayed while the same buffers come back: one launch instead of a
+    // few dozen API calls, whose host time otherwise exceeds the transfers of
+    // a matrix this size.
+    if (host_pinned(x) && host_pinned(y)) {
+        if (!(A->host_graph && A->host_gx == x && A->host_gy == y && A->host_gvariant == variant &&
+              A->host_gdx == dx && A->host_gdy == dy)) {
+            A->drop_host_graph();
+            cudaGraph_t g = nullptr;
+            SPG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            const int rc = enqueue();
+            cudaError_t ec = cudaStreamEndCapture(s, &g);
+            cudaGraphExec_t ex = nullptr;
+            if (rc == SPG_OK && ec == cudaSuccess) ec = cudaGraphInstantiate(&ex, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (rc == SPG_OK && ec == cudaSuccess) {
+                A->host_graph = ex;
+                A->host_gx = x;
+                A->host_gy = y;
+                A->host_gdx = dx;
+                A->host_gdy = dy;
+                A->host_gvariant = variant;
+            } else {
+                cudaGetLastError();  // not recordable: run the sequence directly below
+            }
+        }
+        if (A->host_graph) {
+            SPG_CUDA_TRY(cudaGraphLaunch(A->host_graph, s));
+            SPG_CUDA_TRY(cudaStreamSynchronize(s));
+            return c->take_status();
+        }
     }
+    SPG_TRY(enqueue());
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(c->copy_stream));
     return c->take_status();
 }
 

@@ -127,9 +127,10 @@ struct Ctx {
     // Device vectors reused by spg_spmv_host, the stream that copies y back
     // while later row blocks compute, and the events between the two.
     DevBuf xbuf, ybuf;
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr, upload_stream = nullptr;
     static constexpr int N_HOST_EVENTS = 8;
     cudaEvent_t host_events[N_HOST_EVENTS] = {};
+    cudaEvent_t upload_events[N_HOST_EVENTS] = {};
     // SpMV variant choice: policy and the loaded selector (spg_tune.cu).
     int spmv_policy = SPG_POLICY_SELECTOR;
     DevBuf model;  // FP32 selector blob
@@ -153,6 +154,26 @@ struct Csr {
     uint64_t max_row = 0;
     int selected_spmv = -1;
     SpmvPlan plan_stream, plan_merge, plan_adaptive, plan_inter;
+    // For the host-buffer SpMV of row-parallel variants: the largest column
+    // each of host_reach.size() equal row blocks reads (-1: empty block), so a
+    // block can start once the part of x up to that column has arrived.
+    std::vector<int64_t> host_reach;
+    // The pipelined host SpMV recorded as a CUDA graph for one pinned (x, y)
+    // pair and variant, replayed while the same pair comes back.
+    cudaGraphExec_t host_graph = nullptr;
+    const double *host_gx = nullptr;  // the pair, the variant and the device staging it was recorded with
+    double *host_gy = nullptr;
+    const void *host_gdx = nullptr, *host_gdy = nullptr;
+    int host_gvariant = -1;
+    void drop_host_graph() {
+        if (host_graph) cudaGraphExecDestroy(host_graph);
+        host_graph = nullptr;
+        host_gx = nullptr;
+        host_gy = nullptr;
+        host_gdx = host_gdy = nullptr;
+        host_gvariant = -1;
+    }
+    ~Csr() { drop_host_graph(); }
     void invalidate_derived() {
         stats_valid = false;
         selected_spmv = -1;
@@ -160,6 +181,8 @@ struct Csr {
         plan_merge = SpmvPlan{};
         plan_adaptive = SpmvPlan{};
         plan_inter = SpmvPlan{};
+        host_reach.clear();
+        drop_host_graph();
     }
     const uint64_t *d_off() const { return off.as<uint64_t>(); }
     const uint32_t *d_cols() const { return cols.as<uint32_t>(); }
@@ -274,6 +297,8 @@ int spmv_adaptive_stage(Ctx *c, Csr *A, const double *x, double *y, int variant,
 // SPG_ERR_UNSUPPORTED.
 int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, uint64_t r0, uint64_t r1,
                      cudaStream_t s);
+// A->host_reach for nb equal row blocks (cached until the next lock).
+int spmv_row_block_reach(Ctx *c, Csr *A, int nb, cudaStream_t s);
 // The cached plan slot of one of those variants.
 inline SpmvPlan &adaptive_plan_of(Csr *A, int variant) {
     return variant == SPG_SPMV_INTERLEAVED ? A->plan_inter : A->plan_adaptive;

@@ -444,6 +444,37 @@ static int build_merge_plan(Ctx *c, Csr *A, cudaStream_t s) {
     return SPG_OK;
 }
 
+namespace {
+// reach[b] = largest column of the rows of block b, blocks [n b / nb, n (b+1) / nb)
+__global__ void row_block_reach(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols, uint64_t n,
+                                int nb, long long *__restrict__ reach) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b0 = off[r], b1 = off[r + 1];
+        if (b1 == b0) continue;
+        int b = 0;
+        while (b + 1 < nb && r >= n * (uint64_t)(b + 1) / (uint64_t)nb) ++b;
+        atomicMax(reach + b, (long long)cols[b1 - 1]);  // columns ascend within a row
+    }
+}
+}  // namespace
+
+int spmv_row_block_reach(Ctx *c, Csr *A, int nb, cudaStream_t s) {
+    if ((int)A->host_reach.size() == nb) return SPG_OK;
+    DevBuf d;
+    SPG_TRY(d.alloc(nb * sizeof(long long), s));
+    std::vector<long long> h(nb, -1);
+    SPG_CUDA_TRY(cudaMemcpyAsync(d.ptr, h.data(), nb * sizeof(long long), cudaMemcpyHostToDevice, s));
+    if (A->n_rows) {
+        row_block_reach<<<grid_for(A->n_rows, BLOCK, (unsigned)c->n_sms * 8), BLOCK, 0, s>>>(
+            A->d_off(), A->d_cols(), A->n_rows, nb, d.as<long long>());
+        SPG_LAUNCH_CHECK();
+    }
+    SPG_CUDA_TRY(cudaMemcpyAsync(h.data(), d.ptr, nb * sizeof(long long), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    A->host_reach.assign(h.begin(), h.end());
+    return SPG_OK;
+}
+
 int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, uint64_t r0, uint64_t r1,
                      cudaStream_t s) {
     (void)c;

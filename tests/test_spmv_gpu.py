@@ -135,12 +135,25 @@ def test_host_spmv_pipelined_blocks_match_device_path(ctx):
     x = gen.dense_x(n, 78)
     xd = torch.from_numpy(x).cuda()
     yd = torch.empty(n, dtype=torch.float64, device="cuda")
+    xp = torch.from_numpy(x).pin_memory()  # pinned buffers take the recorded-graph path
+    yp = torch.empty(n, dtype=torch.float64).pin_memory()
     for name, var in VARIANTS:
         if var == sg.SPMV_AUTO:
             continue
         A.spmv(xd, yd, var)
         ctx.sync()
-        np.testing.assert_array_equal(A.spmv_host(x, variant=var), yd.cpu().numpy(), err_msg=name)
+        want = yd.cpu().numpy()
+        np.testing.assert_array_equal(A.spmv_host(x, variant=var), want, err_msg=name)
+        for _ in range(2):  # record, then replay
+            yp.zero_()
+            A.spmv_host(xp.numpy(), yp.numpy(), variant=var)
+            np.testing.assert_array_equal(yp.numpy(), want, err_msg=name + " (pinned)")
+    # a re-lock drops the recorded graph: the next call sees the new matrix
+    A.lock(np.array([5], np.uint32), np.array([7], np.uint32), np.array([3.0]))
+    A.spmv(xd, yd, sg.SPMV_SCALAR)
+    ctx.sync()
+    A.spmv_host(xp.numpy(), yp.numpy(), variant=sg.SPMV_SCALAR)
+    np.testing.assert_array_equal(yp.numpy(), yd.cpu().numpy())
 
 
 def test_gather_probe(ctx):
