@@ -220,9 +220,12 @@ int spg_mlp_argmin(spg_ctx *ctx, const float *d_pred, uint32_t B, int n_outputs,
  * (n_cols x k, X[c * k + j]) into Y (n_rows x k). spg_batch_create builds the
  * work list of (matrix, row tile) items and captures one persistent launch in
  * a CUDA graph; config < 0 autotunes the tile size and CTAs per SM on the
- * batch (runs it a few times), config 0..7 picks one directly. k must be a
- * power of two <= 32. Matrices and vectors must outlive the batch and keep
- * their device arrays (no lock in between). */
+ * batch (runs it a few times), config 0..7 picks one directly. For k < 32 it
+ * also records a row order (rows by length inside windows of 256) so the
+ * rows sharing a warp are of near-equal length; each Y row is still the same
+ * FMA chain over its row. k must be a power of two <= 32. Matrices and
+ * vectors must outlive the batch and keep their device arrays (no lock in
+ * between). */
 typedef struct spg_batch spg_batch;
 int spg_batch_create(spg_ctx *ctx, uint32_t n, const spg_csr *const *mats, const double *const *d_X,
                      double *const *d_Y, const uint32_t *k, int config, spg_batch **out);

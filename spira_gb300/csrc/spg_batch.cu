@@ -31,6 +31,7 @@ struct BatchMat {
     const double *vals;
     const double *X;
     double *Y;
+    const uint32_t *perm;  // rows in ascending length (k < 32), or null: rows in order
     uint32_t n_rows;
     uint32_t k;
 };
@@ -61,7 +62,12 @@ batch_persistent(const BatchMat *__restrict__ mats, const BatchItem *__restrict_
         const uint32_t k = M.k;  // power of two, 1..32
         const uint32_t slots = 32u / k;
         const uint32_t slot = (uint32_t)lane / k, j = (uint32_t)lane % k;
-        for (uint32_t r = itm.row0 + slot; r < itm.row1; r += slots) {
+        for (uint32_t p = itm.row0 + slot; p < itm.row1; p += slots) {
+            // With k < 32 a warp pass runs 32 / k rows side by side and issues
+            // FP64 work for the longest; visiting rows in ascending length
+            // keeps the rows of a pass nearly equal (a masked FP64 lane costs
+            // the same issue slot as a busy one).
+            const uint32_t r = M.perm ? M.perm[p] : p;
             const uint64_t b = M.off[r], e = M.off[r + 1];
             double acc0 = 0.0, acc1 = 0.0;
             uint64_t q = b;
@@ -74,6 +80,46 @@ batch_persistent(const BatchMat *__restrict__ mats, const BatchItem *__restrict_
             if (q < e) acc0 = fma(M.vals[q], __ldg(M.X + (uint64_t)M.cols[q] * k + j), acc0);
             M.Y[(uint64_t)r * k + j] = acc0 + acc1;
         }
+    }
+}
+
+// Row order for the k < 32 matrices: rows sorted by length (ties by index)
+// inside windows of WIN consecutive rows. Windows keep the rows a warp
+// touches close together (row offsets and Y stay in the same L2 lines)
+// while the rows of one warp pass come out with nearly equal lengths.
+constexpr int WIN = 256;
+
+// Block per window; win_base[m] = first window of matrix m (n + 1 entries),
+// perm + row_base[m] = matrix m's permutation.
+__global__ void __launch_bounds__(WIN)
+batch_window_sort(const BatchMat *__restrict__ mats, const uint64_t *__restrict__ win_base,
+                  const uint64_t *__restrict__ row_base, uint32_t n, uint32_t *__restrict__ perm) {
+    __shared__ uint32_t s_len[WIN];
+    const uint64_t w = blockIdx.x;
+    uint32_t lo = 0, hi = n - 1;  // matrix m with win_base[m] <= w < win_base[m + 1]
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (win_base[mid] <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchMat M = mats[lo];
+    const uint32_t r0 = (uint32_t)(w - win_base[lo]) * WIN;
+    const uint32_t cnt = min((uint32_t)WIN, M.n_rows - r0);
+    const uint32_t i = threadIdx.x;
+    uint32_t len = 0xFFFFFFFFu;
+    if (i < cnt) {
+        const uint64_t l = M.off[r0 + i + 1] - M.off[r0 + i];
+        len = l < 0xFFFFFFFEull ? (uint32_t)l : 0xFFFFFFFEu;
+    }
+    s_len[i] = len;
+    __syncthreads();
+    if (i < cnt) {
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint32_t lj = s_len[j];
+            rank += (lj < len) || (lj == len && j < i);
+        }
+        perm[row_base[lo] + r0 + rank] = r0 + i;
     }
 }
 
@@ -95,7 +141,7 @@ struct Batch {
     uint32_t n_mats = 0;
     std::vector<BatchMat> host_mats;
     std::vector<uint64_t> mat_nnz;
-    DevBuf d_mats, d_items, d_counter;
+    DevBuf d_mats, d_items, d_counter, d_perm;
     uint32_t n_items = 0;
     int tile_nnzk = 0;  // target nnz * k per work item
     int ctas_per_sm = 0;
@@ -109,6 +155,7 @@ struct Batch {
         d_mats.release();
         d_items.release();
         d_counter.release();
+        d_perm.release();
     }
     ~Batch() { release(); }
 };
@@ -221,15 +268,49 @@ int spg_batch_create(spg_ctx *c, uint32_t n, const spg_csr *const *mats, const d
             delete B;
             return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_batch_create: bad matrix %u", m);
         }
-        B->host_mats.push_back({A->d_off(), A->d_cols(), A->d_vals(), d_X[m], d_Y[m], (uint32_t)A->n_rows, km});
+        B->host_mats.push_back(
+            {A->d_off(), A->d_cols(), A->d_vals(), d_X[m], d_Y[m], nullptr, (uint32_t)A->n_rows, km});
         B->mat_nnz.push_back(A->nnz);
     }
-    int rc = B->d_mats.alloc(std::max<size_t>(1, n) * sizeof(BatchMat), s);
+    // length-sorted row windows for the matrices that share a warp pass
+    std::vector<uint64_t> row_base(n + 1, 0), win_base(n + 1, 0);
+    for (uint32_t m = 0; m < n; ++m) {
+        const BatchMat &M = B->host_mats[m];
+        const uint64_t rows = M.k < 32 ? M.n_rows : 0;
+        row_base[m + 1] = row_base[m] + rows;
+        win_base[m + 1] = win_base[m] + (rows + WIN - 1) / WIN;
+    }
+    int rc = SPG_OK;
+    DevBuf d_bases;
+    if (win_base[n]) {
+        rc = B->d_perm.alloc(row_base[n] * sizeof(uint32_t), s);
+        if (rc == SPG_OK) rc = d_bases.alloc(2 * (n + 1) * sizeof(uint64_t), s);
+        if (rc == SPG_OK)
+            for (uint32_t m = 0; m < n; ++m)
+                if (row_base[m + 1] > row_base[m]) B->host_mats[m].perm = B->d_perm.as<uint32_t>() + row_base[m];
+    }
+    if (rc == SPG_OK) rc = B->d_mats.alloc(std::max<size_t>(1, n) * sizeof(BatchMat), s);
     if (rc == SPG_OK && n)
         rc = cudaMemcpyAsync(B->d_mats.ptr, B->host_mats.data(), n * sizeof(BatchMat), cudaMemcpyHostToDevice, s) ==
                      cudaSuccess
                  ? SPG_OK
                  : set_error(SPG_ERR_CUDA, "spg_batch_create: copy failed");
+    if (rc == SPG_OK && win_base[n]) {
+        uint64_t *bases = d_bases.as<uint64_t>();
+        if (cudaMemcpyAsync(bases, win_base.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(bases + n + 1, row_base.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s) !=
+                cudaSuccess)
+            rc = set_error(SPG_ERR_CUDA, "spg_batch_create: copy failed");
+        if (rc == SPG_OK) {
+            batch_window_sort<<<(unsigned)win_base[n], WIN, 0, s>>>(B->d_mats.as<BatchMat>(), bases, bases + n + 1, n,
+                                                                  B->d_perm.as<uint32_t>());
+            if (cudaPeekAtLastError() != cudaSuccess) rc = set_error(SPG_ERR_CUDA, "spg_batch_create: row sort failed");
+        }
+        // the bases must outlive the sort: host vectors back the copies
+        if (rc == SPG_OK && cudaStreamSynchronize(s) != cudaSuccess)
+            rc = set_error(SPG_ERR_CUDA, "spg_batch_create: row sort failed");
+    }
     if (rc == SPG_OK) rc = B->d_counter.alloc(sizeof(unsigned), s);
     if (rc != SPG_OK) {
         delete B;

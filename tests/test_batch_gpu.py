@@ -49,6 +49,41 @@ def test_batch_plain_path_matches(ctx):
     _check(mats, Xs, Ys, ks)
 
 
+def test_batch_ragged_rows_every_k(ctx):
+    """Row lengths from empty to long, row counts around the 256-row sort
+    windows, every k: each Y entry is written (NaN-filled before the run)
+    and matches the oracle."""
+    import torch
+    from spira_gb300 import gen
+    shapes = [(1, 1), (255, 1), (257, 2), (256, 4), (1000, 8), (513, 16), (300, 32), (4000, 1), (777, 2)]
+    mats, Xs, Ys, ks = [], [], [], []
+    for i, (n, k) in enumerate(shapes):
+        ctr = np.arange(n, dtype=np.uint64)
+        lengths = gen.below(gen.hash3(90 + i, 1, ctr), 40).astype(np.int64)
+        lengths[::7] = 0
+        lengths[5::97] = 3000
+        rows = np.repeat(np.arange(n, dtype=np.uint32), lengths)
+        c2 = np.arange(len(rows), dtype=np.uint64)
+        cols = gen.below(gen.hash3(90 + i, 2, c2), n)
+        vals = gen.sym_unit(gen.hash3(90 + i, 3, c2))
+        A = sg.Csr(ctx, n, n)
+        A.lock(rows, cols, vals)
+        mats.append(A)
+        Xs.append(torch.from_numpy(gen.dense_x(n * k, 95 + i)).cuda())
+        Ys.append(torch.full((n * k,), float("nan"), dtype=torch.float64, device="cuda"))
+        ks.append(k)
+    for config in (-1, 2):
+        B = sg.Batch(ctx, mats, Xs, Ys, ks, config=config)
+        B.run()
+        ctx.sync()
+        for Y in Ys:
+            assert not torch.isnan(Y).any()
+        _check(mats, Xs, Ys, ks)
+        for Y in Ys:
+            Y.fill_(float("nan"))
+        B.close()
+
+
 def test_batch_rejects_bad_k(ctx):
     mats, Xs, Ys, ks, nnz = batched.build(ctx, 2, seed=5, rows_lo=100, rows_hi=200)
     with pytest.raises(sg.InvalidArgument):
