@@ -69,16 +69,20 @@ batch_persistent(const BatchMat *__restrict__ mats, const BatchItem *__restrict_
             // the same issue slot as a busy one).
             const uint32_t r = M.perm ? M.perm[p] : p;
             const uint64_t b = M.off[r], e = M.off[r + 1];
-            double acc0 = 0.0, acc1 = 0.0;
+            // One FMA chain in column order (Spira's scalar order with fused
+            // multiply-adds): the FP64 pipe, not FMA latency, bounds this
+            // loop, so a second accumulator would only add a final DADD per
+            // row. Pairs keep two gathers in flight per lane.
+            double acc = 0.0;
             uint64_t q = b;
             for (; q + 1 < e; q += 2) {
                 const uint32_t c0 = M.cols[q], c1 = M.cols[q + 1];
                 const double v0 = M.vals[q], v1 = M.vals[q + 1];
-                acc0 = fma(v0, __ldg(M.X + (uint64_t)c0 * k + j), acc0);
-                acc1 = fma(v1, __ldg(M.X + (uint64_t)c1 * k + j), acc1);
+                const double x0 = __ldg(M.X + (uint64_t)c0 * k + j), x1 = __ldg(M.X + (uint64_t)c1 * k + j);
+                acc = fma(v1, x1, fma(v0, x0, acc));
             }
-            if (q < e) acc0 = fma(M.vals[q], __ldg(M.X + (uint64_t)M.cols[q] * k + j), acc0);
-            M.Y[(uint64_t)r * k + j] = acc0 + acc1;
+            if (q < e) acc = fma(M.vals[q], __ldg(M.X + (uint64_t)M.cols[q] * k + j), acc);
+            M.Y[(uint64_t)r * k + j] = acc;
         }
     }
 }

@@ -42,11 +42,27 @@ def test_batch_matches_oracle(ctx, config):
 
 
 def test_batch_plain_path_matches(ctx):
+    """Both paths run one FMA chain per (row, right-hand side) in column
+    order: the same bits as each other and as the oracle's fused scalar
+    SpMV of every column."""
     mats, Xs, Ys, ks, nnz = batched.build(ctx, 10, seed=4, rows_lo=100, rows_hi=5_000)
     B = sg.Batch(ctx, mats, Xs, Ys, ks, config=1)
     B.run_plain()
     ctx.sync()
     _check(mats, Xs, Ys, ks)
+    plain = [Y.cpu().numpy().copy() for Y in Ys]
+    for Y in Ys:
+        Y.zero_()
+    B.run()
+    ctx.sync()
+    for A, X, Y, k, want in zip(mats, Xs, Ys, ks, plain):
+        got = Y.cpu().numpy()
+        np.testing.assert_array_equal(got, want)
+        H = A.download()
+        Xh = X.cpu().numpy().reshape(A.n_cols, k)
+        for j in range(k):
+            np.testing.assert_array_equal(got.reshape(A.n_rows, k)[:, j],
+                                          oracle.spmv_scalar(H, Xh[:, j].copy(), fused=True))
 
 
 def test_batch_ragged_rows_every_k(ctx):
