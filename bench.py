@@ -319,6 +319,10 @@ def run_batched(ctx, stream, n_mats=4096, seed=2024):
 
     ms_graph = time_it(lambda: B.run(ctx.stream), 20)
     ms_plain = time_it(lambda: B.run_plain(ctx.stream), 3)
+    # every (nonzero, right-hand side) pair is one FP64 FMA: the FP64 pipe is
+    # this workload's bound, measured by the FMA-rate probe in the same run
+    fmas = sum(int(z) * int(k) for z, k in zip(nnz, ks))
+    fp64_peak = ctx.probe_fp64_rate(4096)
     # spot-check 3 matrices against the compensated oracle
     import oracle
     worst = 0.0
@@ -338,6 +342,10 @@ def run_batched(ctx, stream, n_mats=4096, seed=2024):
         "rhs_total": int(sum(ks)), "bytes_per_run": int(by),
         "persistent_graph": {"ms": round(ms_graph, 4), "gbs": round(by / (ms_graph * 1e-3) / 1e9, 1),
                              "launches": 1, "config": cfg, "work_items": n_items},
+        "fp64_roofline": {"fmas_per_run": fmas, "achieved_fma_per_s": round(fmas / (ms_graph * 1e-3) / 1e9, 1),
+                          "peak_fma_per_s": round(fp64_peak / 1e9, 1), "unit": "G FMA/s",
+                          "peak": "FMA-rate probe (8 chains x 256 threads x 8 CTAs per SM), same run",
+                          "frac": round(fmas / (ms_graph * 1e-3) / fp64_peak, 3)},
         "plain_per_matrix_per_rhs": {"ms": round(ms_plain, 3), "gbs": round(by / (ms_plain * 1e-3) / 1e9, 1),
                                      "launches": int(sum(ks))},
         "speedup": round(ms_plain / ms_graph, 2),
@@ -490,6 +498,62 @@ def run_ops(ctx, peak):
                                  gproducts_per_s=round(prods / (t_g * 1e-3) / 1e9, 2), bit_exact=same_g))
         Cm.close()
         A.close()
+
+    # ---- element-wise: A + B, A * s (copy and in place), row sums on the 2a
+    # Laplacian and the 2b Zipf matrix, B = A after the 1 % re-lock
+    out["elementwise"] = []
+    r, c, v = gen.laplacian_2d(GRID)
+    zr, zc, zv, zm = gen_device.zipf_rows(ctx, ZIPF_N, seed=31)
+    for name, n in (("laplacian2d", GRID * GRID), ("zipf4m", ZIPF_N)):
+        A = sg.Csr(ctx, n, n)
+        if name == "laplacian2d":
+            A.lock(r, c, v)
+        else:
+            A.lock_device(zr, zc, zv, zm)
+        B = sg.Csr(ctx, n, n)
+        B.copy_from(A)
+        B.lock(*gen.relock_batch(n, n, A.nnz, seed=21 if name == "laplacian2d" else 32))
+        HA, HB = A.download(), B.download()
+        res = {}
+
+        def do_add():
+            if "C" in res:
+                res["C"].close()
+            res["C"] = A.add(B)
+
+        t_add = wall(do_add)
+        cpu_add, C_ref = cpu(lambda: oracle.add(HA, HB))
+        Cm = res["C"]
+        by = csr_bytes(n, A.nnz) + csr_bytes(n, B.nnz) + csr_bytes(n, Cm.nnz)
+        out["elementwise"].append(rec(f"add_{name}", t_add, by, cpu_add, nnz_a=int(A.nnz), nnz_b=int(B.nnz),
+                                      nnz_c=int(Cm.nnz),
+                                      bit_exact=oracle.csr_digest(Cm.download()) == oracle.csr_digest(C_ref)))
+        Cm.close()
+        res.clear()
+
+        def do_scale():
+            if "S" in res:
+                res["S"].close()
+            res["S"] = A.scaled(2.5)
+
+        t_sc = wall(do_scale)
+        cpu_sc, S_ref = cpu(lambda: oracle.scale(HA, 2.5))
+        out["elementwise"].append(rec(f"scale_copy_{name}", t_sc, 2 * csr_bytes(n, A.nnz), cpu_sc, nnz=int(A.nnz),
+                                      bit_exact=oracle.csr_digest(res["S"].download()) == oracle.csr_digest(S_ref)))
+        res["S"].close()
+        t_ip = wall(lambda: A.scale_(-1.0))  # exact: three sign flips
+        out["elementwise"].append(rec(f"scale_in_place_{name}", t_ip, 16 * A.nnz, None, nnz=int(A.nnz)))
+        sums = torch.empty(n, dtype=torch.float64, device=dev)
+        t_rs = wall(lambda: A.row_sums(sums))
+        cpu_rs, rs_ref = cpu(lambda: oracle.row_sums(A.download()))
+        out["elementwise"].append(rec(f"row_sums_{name}", t_rs, 8 * A.nnz + 8 * (n + 1) + 8 * n, cpu_rs,
+                                      bit_exact=bool(np.array_equal(sums.cpu().numpy().view(np.uint64),
+                                                                    rs_ref.view(np.uint64)))))
+        A.close()
+        B.close()
+        del sums
+    del zr, zc, zv
+    torch.cuda.empty_cache()
     return out
 
 
@@ -570,6 +634,7 @@ PROFILE_CASES = {
     "transpose_laplacian3d": (100 ** 3, "transpose"),
     "spgemm_laplacian3d": (100 ** 3, "spgemm"),
     "spgemm_uniform200k": (200_000, "spgemm"),
+    "add_zipf1m": (1_000_000, "add"),  # A + (A after a 1 % re-lock)
 }
 
 
@@ -592,6 +657,24 @@ def run_profile_op(ctx, case, n, kind, reps):
             ms.append((time.perf_counter() - t0) * 1e3)
         print(json.dumps({"profile_case": case, "matrices": n, "nnz": int(sum(nz)), "config": B.config(),
                           "ms_per_call": [round(t, 3) for t in ms]}))
+        return
+    if kind == "add":
+        r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
+        A = sg.Csr(ctx, n, n)
+        A.lock_device(r, c, v, m)
+        del r, c, v
+        B = sg.Csr(ctx, n, n)
+        B.copy_from(A)
+        B.lock(*gen.relock_batch(n, n, A.nnz, seed=32))
+        for _ in range(reps + 1):
+            ctx.sync()
+            t0 = time.perf_counter()
+            Cm = A.add(B)
+            ctx.sync()
+            ms.append((time.perf_counter() - t0) * 1e3)
+            nnz = Cm.nnz
+            Cm.close()
+        print(json.dumps({"profile_case": case, "n_rows": n, "nnz": nnz, "ms_per_call": [round(t, 3) for t in ms]}))
         return
     if kind == "relock":
         import torch
@@ -655,7 +738,7 @@ def run_profile_case(args):
     ctx = sg.Context(0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     n, kind = PROFILE_CASES[args.profile_case]
-    if kind in ("lock", "relock", "transpose", "spgemm", "batched"):
+    if kind in ("lock", "relock", "transpose", "spgemm", "batched", "add"):
         run_profile_op(ctx, args.profile_case, n, kind, args.reps)
         return
     if kind == "zipf":

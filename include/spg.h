@@ -39,7 +39,8 @@ enum spg_status {
     SPG_ERR_NO_MEMORY = 4,        /* std::bad_alloc: device allocation failed */
     SPG_ERR_CUDA = 5,             /* CUDA runtime error (no device, launch failure, ...) */
     SPG_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up; context stays usable */
-    SPG_ERR_UNSUPPORTED = 7       /* valid request that libspg does not serve */
+    SPG_ERR_UNSUPPORTED = 7,      /* valid request that libspg does not serve */
+    SPG_ERR_DOMAIN = 8            /* std::domain_error: division by a zero scalar */
 };
 
 /* ---- SpMV variants (spg_spmv `variant`) --------------------------------- */
@@ -192,6 +193,13 @@ int spg_spmv_autotune(spg_ctx *ctx, const spg_csr *A, int reps, float *times_ms,
  * on matrices with randomly spread columns, where every nonzero's x read hits
  * its own L2 sector. */
 int spg_probe_gather_rate(spg_ctx *ctx, uint64_t n_x, uint64_t n_gathers, double *gathers_per_s);
+/* Device probe, no Spira counterpart: the FP64 fused multiply-add rate (FMAs
+ * per second, median of 5 timed runs after 2 warm-up runs) of a launch of 8
+ * CTAs of 256 threads per SM, each thread running 8 independent FMA chains of
+ * `iters` steps. It is the ceiling of the batched multi-RHS SpMV, where every
+ * (nonzero, right-hand side) pair is one FP64 FMA and the FP64 pipe, not
+ * memory, is the bound. */
+int spg_probe_fp64_rate(spg_ctx *ctx, uint32_t iters, double *fma_per_s);
 /* Installs a trained selector (NULL blob removes it). Blob layout, FP32:
  * mean[40] scale[40] W1[64][40] b1[64] W2[64][64] b2[64] W3[K][64] b3[K];
  * output k predicts log(time of variant k / fastest time). */
@@ -235,6 +243,44 @@ int spg_batch_run(spg_ctx *ctx, spg_batch *batch, void *stream);
 /* The comparison path: one plain SpMV launch per matrix per right-hand side. */
 int spg_batch_run_plain(spg_ctx *ctx, spg_batch *batch, void *stream);
 int spg_batch_destroy(spg_batch *batch);
+
+/* ---- element-wise operations and queries -----------------------------------
+ * spg_csr_add: C <- A + B. Per row a merge of the two CSR slices: equal
+ * columns give a + b (one IEEE add) and are kept unless the sum is +-0, other
+ * entries are copied, stored zeros are dropped; C is reshaped to A's shape
+ * with tight capacity (serial/matrix_addition.hpp:34-110,
+ * parallel/algorithms/matrix_addition.hpp:24-99). A and B of different shapes
+ * give SPG_ERR_INVALID_ARGUMENT, an unlocked A or B SPG_ERR_LOGIC; C must not
+ * be A or B. */
+int spg_csr_add(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, spg_csr *C);
+/* spg_csr_scale: C <- A * scalar (divide == 0) or A / scalar (divide != 0),
+ * every committed value once (IEEE multiply / divide), results that are +-0
+ * dropped (serial/scalars.hpp:10-67). C may be A (in place; Spira's in-place
+ * form stages the scaled values and the next lock installs them, which ends
+ * in the same CSR). Division by +-0 gives SPG_ERR_DOMAIN, checked first; an
+ * unlocked A gives SPG_ERR_LOGIC. */
+int spg_csr_scale(spg_ctx *ctx, spg_csr *A, spg_csr *C, double scalar, int divide);
+/* spg_csr_row_sums: d_out[r] = sum of row r's values in CSR order from 0.0,
+ * one IEEE add per entry (matrix.hpp:438-443, row.hpp:208-216,
+ * csr_storage_soa.hpp:114-120: a locked row's accumulate()). Asynchronous on
+ * `stream`. */
+int spg_csr_row_sums(spg_ctx *ctx, const spg_csr *A, double *d_out, void *stream);
+/* The same for rows [row0, row0 + n) into host out[n]; returns when done.
+ * Rows beyond n_rows give SPG_ERR_OUT_OF_RANGE. */
+int spg_csr_row_sums_host(spg_ctx *ctx, const spg_csr *A, uint64_t row0, uint64_t n, double *out);
+/* spg_csr_lookup: n point queries (d_rows[i], d_cols[i]) against the
+ * committed CSR, binary search per query (row.hpp:190-204, locked rows):
+ * d_vals[i] = the stored value or 0.0, d_found[i] = 1 or 0 (either output may
+ * be NULL). Queries outside the shape report not found. Asynchronous on
+ * `stream`. */
+int spg_csr_lookup(spg_ctx *ctx, const spg_csr *A, uint64_t n, const uint64_t *d_rows, const uint32_t *d_cols,
+                   double *d_vals, uint8_t *d_found, void *stream);
+/* spg_csr_partition: nnz-balanced row boundaries for n_parts partitions into
+ * host bounds[n_parts + 1]: bounds[t] = first row whose nnz prefix reaches
+ * max(1, t * nnz / n_parts), a uniform row split when nnz == 0, {0, n, ...}
+ * for one part or no rows (parallel/partition.hpp:78-126, the boundaries
+ * parallel_matrix::rebalance installs, parallel_matrix.hpp:434-452). */
+int spg_csr_partition(spg_ctx *ctx, const spg_csr *A, uint64_t n_parts, uint64_t *bounds);
 
 /* ---- transpose / SpGEMM ----------------------------------------------------
  * spg_transpose: AT <- A^T (AT is reshaped to n_cols x n_rows, capacity ==

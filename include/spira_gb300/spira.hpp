@@ -23,6 +23,7 @@
 #include <spg.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -82,6 +83,7 @@ inline void check(int status) {
         case SPG_ERR_LOGIC: throw std::logic_error(msg);
         case SPG_ERR_OUT_OF_RANGE: throw std::out_of_range(msg);
         case SPG_ERR_NO_MEMORY: throw std::bad_alloc();
+        case SPG_ERR_DOMAIN: throw std::domain_error(msg);
         default: throw std::runtime_error(std::string(spg_strerror(status)) + ": " + msg);
     }
 }
@@ -324,17 +326,108 @@ public:
         swap(host_, o.host_);
     }
 
-    // operators (matrix_operators.hpp:67-150)
+    // matrix.hpp:438-443 via row.hpp:208-231. Locked: the row's committed
+    // values summed left to right from 0 (on the device). Open: the staged
+    // entries of the row (last write per column, in order of each column's
+    // first insert: the iteration order of the row buffer's column index),
+    // then the committed entries no staged entry shadows, in CSR order.
+    [[nodiscard]] value_type accumulate(index_type r) const {
+        validate_row(r);
+        const auto i = dev_.info();
+        if (is_locked() || st_rows_.empty()) {
+            if (!i.built) return 0.0;
+            double v = 0.0;
+            gpu::check(spg_csr_row_sums_host(gpu::context(), dev_.get(), r, 1, &v));
+            return v;
+        }
+        std::vector<uint32_t> order;  // columns by first staged insert
+        std::vector<double> last;
+        for (size_type k = 0; k < st_rows_.size(); ++k) {
+            if (st_rows_[k] != r) continue;
+            const auto it = std::find(order.begin(), order.end(), st_cols_[k]);
+            if (it == order.end()) {
+                order.push_back(st_cols_[k]);
+                last.push_back(st_vals_[k]);
+            } else {
+                last[static_cast<size_type>(it - order.begin())] = st_vals_[k];
+            }
+        }
+        double acc = 0.0;
+        for (double v : last) acc += v;
+        if (const auto *s = csr()) {
+            for (std::size_t k = s->offsets[r]; k < s->offsets[r + 1]; ++k) {
+                I col;
+                V val;
+                if constexpr (std::is_same_v<LayoutTag, layout::tags::soa_tag>) {
+                    col = s->cols[k];
+                    val = s->vals[k];
+                } else {
+                    col = s->pairs[k].column;
+                    val = s->pairs[k].value;
+                }
+                if (std::find(order.begin(), order.end(), col) == order.end()) acc += val;
+            }
+        }
+        return acc;
+    }
+
+    // Engine side of the in-place scalers (scalars.hpp:10-18, 37-49): every
+    // committed value times / over s on the device, results that are +-0
+    // removed. Staged inserts at committed positions are dropped (Spira
+    // stages the scaled committed value after them, so it is the last write);
+    // before the first lock the staged values themselves are scaled, as
+    // Spira's row walks its buffer when no CSR slice is installed.
+    void scale_in_place(value_type s, bool divide) {
+        const auto i = dev_.info();
+        if (!i.built) {
+            for (auto &v : st_vals_) v = divide ? v / s : v * s;
+            return;
+        }
+        if (!st_rows_.empty()) {
+            const auto *snap = csr();
+            size_type w = 0;
+            for (size_type k = 0; k < st_rows_.size(); ++k) {
+                const std::size_t b = snap->offsets[st_rows_[k]], e = snap->offsets[st_rows_[k] + 1];
+                bool committed = false;
+                for (std::size_t q = b; q < e && !committed; ++q) {
+                    if constexpr (std::is_same_v<LayoutTag, layout::tags::soa_tag>) committed = snap->cols[q] == st_cols_[k];
+                    else committed = snap->pairs[q].column == st_cols_[k];
+                }
+                if (committed) continue;
+                st_rows_[w] = st_rows_[k];
+                st_cols_[w] = st_cols_[k];
+                st_vals_[w] = st_vals_[k];
+                ++w;
+            }
+            st_rows_.resize(w);
+            st_cols_.resize(w);
+            st_vals_.resize(w);
+        }
+        gpu::check(spg_csr_scale(gpu::context(), dev_.get(), dev_.get(), s, divide ? 1 : 0));
+        host_.reset();
+    }
+
+    // operators (matrix_operators.hpp:18-150)
+    matrix operator+(const matrix &other) const;
+    matrix operator-(const matrix &other) const;
+    matrix &operator+=(const matrix &other);
+    matrix &operator-=(const matrix &other);
     std::vector<value_type> operator*(const std::vector<value_type> &x) const;
     matrix operator*(const matrix &other) const;
     matrix &operator*=(const matrix &other) {
         *this = *this * other;
         return *this;
     }
+    matrix operator*(value_type s) const;
+    matrix &operator*=(value_type s);
+    matrix operator/(value_type s) const;
+    matrix &operator/=(value_type s);
     matrix operator~() const;
 
     // engine access
     [[nodiscard]] spg_csr *device_handle() const noexcept { return dev_.get(); }
+    [[nodiscard]] bool csr_built() const { return dev_.info().built != 0; }
+    [[nodiscard]] size_type staged_count() const noexcept { return st_rows_.size(); }
     // Adopts a device result (transpose / spgemm): locked, shape from the handle.
     static matrix adopt(gpu::csr_handle &&h) {
         const auto i = h.info();
@@ -420,7 +513,138 @@ inline void transpose_itself(spira::matrix<L, I, V, BT, BN, LP> &mat) {
     mat.open();
 }
 
+// serial/matrix_addition.hpp:86-110 (checks in the same order).
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline spira::matrix<L, I, V, BT, BN, LP> MatrixAddition(const spira::matrix<L, I, V, BT, BN, LP> &A,
+                                                         const spira::matrix<L, I, V, BT, BN, LP> &B) {
+    if (A.shape() != B.shape()) throw std::invalid_argument("Matrices aren't the same size");
+    if (!A.is_locked()) throw std::logic_error("MatrixAddition: A must be locked");
+    if (!B.is_locked()) throw std::logic_error("MatrixAddition: B must be locked");
+    gpu::csr_handle out(A.n_rows(), A.n_cols());  // (a locked matrix always holds a device CSR)
+    gpu::check(spg_csr_add(gpu::context(), A.device_handle(), B.device_handle(), out.get()));
+    return spira::matrix<L, I, V, BT, BN, LP>::adopt(std::move(out));
+}
+
+// serial/scalars.hpp:9-18 (in place: the matrix must be open).
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline void multiplication_scaler(spira::matrix<L, I, V, BT, BN, LP> &mat, V scaler) {
+    if (!mat.is_open()) throw std::logic_error("multiplication_scaler: matrix must be open");
+    mat.scale_in_place(scaler, false);
+}
+
+// serial/scalars.hpp:22-35 (copy path: mat locked, out replaced).
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline void multiplication_scaler(const spira::matrix<L, I, V, BT, BN, LP> &mat, spira::matrix<L, I, V, BT, BN, LP> &out,
+                                  V scaler) {
+    if (!mat.is_locked()) throw std::logic_error("multiplication_scaler: input matrix must be locked");
+    gpu::csr_handle h(mat.n_rows(), mat.n_cols());
+    gpu::check(spg_csr_scale(gpu::context(), mat.device_handle(), h.get(), scaler, 0));
+    out = spira::matrix<L, I, V, BT, BN, LP>::adopt(std::move(h));
+}
+
+// serial/scalars.hpp:37-49: the zero check fires before the mode check.
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline void division_scaler(spira::matrix<L, I, V, BT, BN, LP> &mat, V scaler) {
+    if (std::fabs(scaler) <= 0.0) throw std::domain_error("Divison by zero");
+    if (!mat.is_open()) throw std::logic_error("division_scaler: matrix must be open");
+    mat.scale_in_place(scaler, true);
+}
+
+// serial/scalars.hpp:51-67
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline void division_scaler(const spira::matrix<L, I, V, BT, BN, LP> &mat, spira::matrix<L, I, V, BT, BN, LP> &out,
+                            V scaler) {
+    if (std::fabs(scaler) <= 0.0) throw std::domain_error("Divison by zero");
+    if (!mat.is_locked()) throw std::logic_error("division_scaler: input matrix must be locked");
+    gpu::csr_handle h(mat.n_rows(), mat.n_cols());
+    gpu::check(spg_csr_scale(gpu::context(), mat.device_handle(), h.get(), scaler, 1));
+    out = spira::matrix<L, I, V, BT, BN, LP>::adopt(std::move(h));
+}
+
+// serial/accumulate.hpp:12-32
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline V accumulate(const spira::matrix<L, I, V, BT, BN, LP> &mat, std::size_t i) {
+    if (i >= mat.shape().first) throw std::out_of_range("Row does not exist in matrix");
+    return mat.accumulate(static_cast<I>(i));
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+inline std::vector<V> accumulate(const spira::matrix<L, I, V, BT, BN, LP> &mat) {
+    std::vector<V> acc(mat.n_rows(), 0.0);
+    if (mat.n_rows() == 0) return acc;
+    if (mat.csr_built() && (mat.is_locked() || mat.staged_count() == 0)) {  // every row at once, on the device
+        gpu::check(spg_csr_row_sums_host(gpu::context(), mat.device_handle(), 0, mat.n_rows(), acc.data()));
+        return acc;
+    }
+    for (std::size_t r = 0; r < mat.n_rows(); ++r) acc[r] = mat.accumulate(static_cast<I>(r));
+    return acc;
+}
+
 }  // namespace serial::algorithms
+
+// matrix_operators.hpp:18-62: A - B is A + (B * -1).
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> matrix<L, I, V, BT, BN, LP>::operator+(const matrix &other) const {
+    return serial::algorithms::MatrixAddition(*this, other);
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> matrix<L, I, V, BT, BN, LP>::operator-(const matrix &other) const {
+    if (this->shape() != other.shape()) throw std::invalid_argument("operator-: matrix shapes must match");
+    matrix out(other.n_rows(), other.n_cols());
+    serial::algorithms::multiplication_scaler(other, out, V{-1});
+    return serial::algorithms::MatrixAddition(*this, out);
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> &matrix<L, I, V, BT, BN, LP>::operator+=(const matrix &other) {
+    *this = serial::algorithms::MatrixAddition(*this, other);
+    return *this;
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> &matrix<L, I, V, BT, BN, LP>::operator-=(const matrix &other) {
+    if (this->shape() != other.shape()) throw std::invalid_argument("operator-=: matrix shapes must match");
+    matrix out(other.n_rows(), other.n_cols());
+    serial::algorithms::multiplication_scaler(other, out, V{-1});
+    *this = serial::algorithms::MatrixAddition(*this, out);
+    return *this;
+}
+
+// matrix_operators.hpp:104-140
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> matrix<L, I, V, BT, BN, LP>::operator*(V s) const {
+    matrix out(n_rows(), n_cols());
+    serial::algorithms::multiplication_scaler(*this, out, s);
+    return out;
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> &matrix<L, I, V, BT, BN, LP>::operator*=(V s) {
+    serial::algorithms::multiplication_scaler(*this, s);
+    return *this;
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> matrix<L, I, V, BT, BN, LP>::operator/(V s) const {
+    matrix out(n_rows(), n_cols());
+    serial::algorithms::division_scaler(*this, out, s);
+    return out;
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
+    requires layout::ValidLayoutTag<L>
+inline matrix<L, I, V, BT, BN, LP> &matrix<L, I, V, BT, BN, LP>::operator/=(V s) {
+    serial::algorithms::division_scaler(*this, s);
+    return *this;
+}
 
 template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP>
     requires layout::ValidLayoutTag<L>
@@ -505,6 +729,7 @@ class parallel_matrix {
     using base_matrix = spira::matrix<LayoutTag, I, V, BufferTag, BufferN, LP>;
 
 public:
+    using base_type = base_matrix;
     using index_type = I;
     using value_type = V;
     using size_type = std::size_t;
@@ -570,14 +795,20 @@ public:
     void open() { m_.open(); }
     void clear() { m_.clear(); }
 
-    // parallel_matrix.hpp:434-497: nnz-balanced partition boundaries. The
+    // parallel_matrix.hpp:434-497: nnz-balanced partition boundaries
+    // (partition.hpp:78-126) computed on the device from the CSR offsets. The
     // device CSR is one array, so only the bookkeeping moves.
     void rebalance() {
         if (!is_locked()) throw std::logic_error("rebalance: matrix must be locked");
-        std::vector<size_type> row_nnz(n_rows());
-        const auto *s = m_.csr();
-        for (size_type r = 0; r < n_rows(); ++r) row_nnz[r] = s->offsets[r + 1] - s->offsets[r];
-        bounds_ = compute_partition_boundaries(row_nnz, n_threads_);
+        std::vector<uint64_t> b(n_threads_ + 1);
+        gpu::check(spg_csr_partition(gpu::context(), m_.device_handle(), n_threads_, b.data()));
+        for (size_type t = 0; t <= n_threads_; ++t) bounds_[t] = static_cast<size_type>(b[t]);
+    }
+
+    // parallel_matrix.hpp:568-580
+    [[nodiscard]] V accumulate(size_type r) const {
+        if (r >= n_rows()) throw std::out_of_range("parallel_matrix: row index out of range");
+        return m_.accumulate(static_cast<I>(r));
     }
 
     [[nodiscard]] size_type nnz() const { return m_.nnz(); }
@@ -671,6 +902,81 @@ inline parallel_matrix<L, I, V, BT, BN, LP, IP, SN> transpose(parallel_matrix<L,
     if (!mat.is_locked()) throw std::logic_error("transpose: matrix must be locked");
     auto m = serial::algorithms::transpose(mat.engine_matrix());
     return parallel_matrix<L, I, V, BT, BN, LP, IP, SN>::adopt(std::move(m), mat.n_threads());
+}
+
+// parallel/algorithms/matrix_addition.hpp:24-99
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline parallel_matrix<L, I, V, BT, BN, LP, IP, SN> MatrixAddition(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &A,
+                                                                   parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &B) {
+    if (A.shape() != B.shape()) throw std::invalid_argument("MatrixAddition: matrices must have the same shape");
+    if (A.n_threads() != B.n_threads())
+        throw std::invalid_argument("MatrixAddition: matrices must have the same thread count");
+    if (!A.is_locked()) throw std::logic_error("MatrixAddition: A must be locked");
+    if (!B.is_locked()) throw std::logic_error("MatrixAddition: B must be locked");
+    auto m = serial::algorithms::MatrixAddition(A.engine_matrix(), B.engine_matrix());
+    return parallel_matrix<L, I, V, BT, BN, LP, IP, SN>::adopt(std::move(m), A.n_threads());
+}
+
+// parallel/algorithms/scalars.hpp:16-31, 69-84 (in place; open matrix)
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline void multiplication_scaler(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat, V scaler) {
+    if (!mat.is_open()) throw std::logic_error("multiplication_scaler: matrix must be open");
+    mat.engine_matrix().scale_in_place(scaler, false);
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline void division_scaler(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat, V scaler) {
+    if (std::fabs(scaler) <= 0.0) throw std::domain_error("division by zero");
+    if (!mat.is_open()) throw std::logic_error("division_scaler: matrix must be open");
+    mat.engine_matrix().scale_in_place(scaler, true);
+}
+
+// parallel/algorithms/scalars.hpp:37-62, 91-116 (copy: mat locked, out open,
+// same shape and thread count; out ends locked)
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline void scale_into(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat,
+                       parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &out, V scaler, bool divide, const char *who) {
+    if (!mat.is_locked()) throw std::logic_error(std::string(who) + ": input matrix must be locked");
+    if (!out.is_open()) throw std::logic_error(std::string(who) + ": output matrix must be open");
+    if (mat.shape() != out.shape()) throw std::invalid_argument(std::string(who) + ": shape mismatch");
+    if (mat.n_threads() != out.n_threads()) throw std::invalid_argument(std::string(who) + ": thread count mismatch");
+    typename parallel_matrix<L, I, V, BT, BN, LP, IP, SN>::base_type r(mat.n_rows(), mat.n_cols());
+    if (divide) serial::algorithms::division_scaler(mat.engine_matrix(), r, scaler);
+    else serial::algorithms::multiplication_scaler(mat.engine_matrix(), r, scaler);
+    out = parallel_matrix<L, I, V, BT, BN, LP, IP, SN>::adopt(std::move(r), out.n_threads());
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline void multiplication_scaler(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat,
+                                  parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &out, V scaler) {
+    scale_into(mat, out, scaler, false, "multiplication_scaler");
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline void division_scaler(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat,
+                            parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &out, V scaler) {
+    if (std::fabs(scaler) <= 0.0) throw std::domain_error("division by zero");
+    scale_into(mat, out, scaler, true, "division_scaler");
+}
+
+// parallel/algorithms/accumulate.hpp:16-53
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline V accumulate(const parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat, std::size_t row) {
+    if (row >= mat.n_rows()) throw std::out_of_range("accumulate: row index out of range");
+    return mat.accumulate(row);
+}
+
+template <class L, class I, class V, class BT, std::size_t BN, config::lock_policy LP, config::insert_policy IP,
+          std::size_t SN>
+inline std::vector<V> accumulate(parallel_matrix<L, I, V, BT, BN, LP, IP, SN> &mat) {
+    return serial::algorithms::accumulate(mat.engine_matrix());
 }
 
 }  // namespace algorithms

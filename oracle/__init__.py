@@ -61,6 +61,10 @@ def orc():
         _orc.orc_spgemm_products.argtypes = [P, P]
         _orc.orc_spgemm_products.restype = C.c_uint64
         _orc.orc_transpose.argtypes = [P, P]
+        _orc.orc_add.argtypes = [P, P, P]
+        _orc.orc_scale.argtypes = [P, C.c_double, C.c_int, P]
+        _orc.orc_row_sums.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        _orc.orc_partition.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p]
     return _orc
 
 
@@ -85,6 +89,10 @@ def ref():
         _ref.ref_spgemm.argtypes = [C.c_int, C.c_int, P, P, P]
         _ref.ref_transpose.argtypes = [C.c_int, C.c_int, P, P]
         _ref.ref_load_check.argtypes = [P]
+        _ref.ref_add.argtypes = [C.c_int, C.c_int, P, P, P]
+        _ref.ref_scale.argtypes = [C.c_int, C.c_int, P, C.c_double, P]
+        _ref.ref_row_sums.argtypes = [P, C.c_void_p]
+        _ref.ref_partition.argtypes = [P, C.c_uint64, C.c_void_p]
     return _ref
 
 
@@ -199,6 +207,37 @@ def transpose(A) -> Csr:
     return _take(out, orc().orc_csr_free)
 
 
+def add(A, B) -> Csr:
+    sa, ka = _as_c(A)
+    sb, kb = _as_c(B)
+    out = _OrcCsr()
+    rc = orc().orc_add(C.byref(sa), C.byref(sb), C.byref(out))
+    assert rc == 0
+    return _take(out, orc().orc_csr_free)
+
+
+def scale(A, s: float, divide: bool = False) -> Csr:
+    sa, ka = _as_c(A)
+    out = _OrcCsr()
+    rc = orc().orc_scale(C.byref(sa), float(s), int(divide), C.byref(out))
+    assert rc == 0
+    return _take(out, orc().orc_csr_free)
+
+
+def row_sums(A) -> np.ndarray:
+    off, vals = _arr(A.off, np.uint64), _arr(A.vals, np.float64)
+    out = np.empty(A.n_rows, np.float64)
+    orc().orc_row_sums(off.ctypes.data, vals.ctypes.data, A.n_rows, out.ctypes.data)
+    return out
+
+
+def partition(A, n_parts: int) -> np.ndarray:
+    off = _arr(A.off, np.uint64)
+    b = np.empty(n_parts + 1, np.uint64)
+    orc().orc_partition(off.ctypes.data, A.n_rows, n_parts, b.ctypes.data)
+    return b
+
+
 # ---------------------------------------------------------------- Spira itself
 class RefError(Exception):
     pass
@@ -208,7 +247,7 @@ def _ref_rc(rc):
     if rc == 0:
         return
     msg = ref().ref_last_error().decode()
-    raise {1: ValueError, 2: RuntimeError, 3: IndexError}.get(rc, RefError)(msg)
+    raise {1: ValueError, 2: RuntimeError, 3: IndexError, 4: ArithmeticError}.get(rc, RefError)(msg)
 
 
 def ref_lock_epochs(n_rows, n_cols, epochs, layout=1, n_threads=4) -> Csr:
@@ -253,6 +292,35 @@ def ref_transpose(A, parallel=False, n_threads=4) -> Csr:
     out = _OrcCsr()
     _ref_rc(ref().ref_transpose(int(parallel), n_threads, C.byref(sa), C.byref(out)))
     return _take(out, ref().ref_csr_free)
+
+
+def ref_add(A, B, parallel=False, n_threads=4) -> Csr:
+    sa, ka = _as_c(A)
+    sb, kb = _as_c(B)
+    out = _OrcCsr()
+    _ref_rc(ref().ref_add(int(parallel), n_threads, C.byref(sa), C.byref(sb), C.byref(out)))
+    return _take(out, ref().ref_csr_free)
+
+
+def ref_scale(A, s, divide=False, in_place=False) -> Csr:
+    sa, ka = _as_c(A)
+    out = _OrcCsr()
+    _ref_rc(ref().ref_scale(int(in_place), int(divide), C.byref(sa), float(s), C.byref(out)))
+    return _take(out, ref().ref_csr_free)
+
+
+def ref_row_sums(A) -> np.ndarray:
+    sa, ka = _as_c(A)
+    out = np.empty(A.n_rows, np.float64)
+    ref().ref_row_sums(C.byref(sa), out.ctypes.data)
+    return out
+
+
+def ref_partition(A, n_parts: int) -> np.ndarray:
+    sa, ka = _as_c(A)
+    b = np.empty(n_parts + 1, np.uint64)
+    ref().ref_partition(C.byref(sa), n_parts, b.ctypes.data)
+    return b
 
 
 # ---------------------------------------------------------------- host inputs

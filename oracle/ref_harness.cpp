@@ -272,6 +272,72 @@ int ref_transpose(int parallel, int n_threads, const RefCsr *A, RefCsr *T) {
     }
 }
 
+// C = A + B: serial MatrixAddition (parallel == 0) or the parallel one with
+// n_threads partitions.
+int ref_add(int parallel, int n_threads, const RefCsr *A, const RefCsr *B, RefCsr *C) {
+    try {
+        if (!parallel) {
+            MatS a = load(A), b = load(B);
+            MatS c = spira::serial::algorithms::MatrixAddition(a, b);
+            export_soa(*c.csr(), A->n_rows, A->n_cols, C);
+        } else {
+            PMatS a(A->n_rows, A->n_cols, n_threads), b(B->n_rows, B->n_cols, n_threads);
+            fill_parallel(a, A);
+            fill_parallel(b, B);
+            PMatS c = spira::parallel::algorithms::MatrixAddition(a, b);
+            export_parallel(c, C);
+        }
+        return 0;
+    } catch (const std::invalid_argument &e) {
+        return fail(e, 1);
+    } catch (const std::logic_error &e) {
+        return fail(e, 2);
+    }
+}
+
+// A * s or A / s: the copy path (in_place == 0: multiplication_scaler(mat,
+// out, s)) or the in-place path on the re-opened matrix followed by lock().
+// Returns 4 for std::domain_error.
+int ref_scale(int in_place, int divide, const RefCsr *A, double s, RefCsr *C) {
+    try {
+        MatS a = load(A);
+        if (in_place) {
+            a.open();
+            if (divide) spira::serial::algorithms::division_scaler(a, s);
+            else spira::serial::algorithms::multiplication_scaler(a, s);
+            a.lock();
+            export_soa(*a.csr(), A->n_rows, A->n_cols, C);
+        } else {
+            MatS out(A->n_rows, A->n_cols);
+            if (divide) spira::serial::algorithms::division_scaler(a, out, s);
+            else spira::serial::algorithms::multiplication_scaler(a, out, s);
+            export_soa(*out.csr(), A->n_rows, A->n_cols, C);
+        }
+        return 0;
+    } catch (const std::domain_error &e) {
+        return fail(e, 4);
+    } catch (const std::invalid_argument &e) {
+        return fail(e, 1);
+    } catch (const std::logic_error &e) {
+        return fail(e, 2);
+    }
+}
+
+// accumulate(mat) on a locked matrix: every row's sum.
+void ref_row_sums(const RefCsr *A, double *out) {
+    MatS a = load(A);
+    const std::vector<double> acc = spira::serial::algorithms::accumulate(a);
+    std::memcpy(out, acc.data(), A->n_rows * sizeof(double));
+}
+
+// compute_partition_boundaries over the CSR's row lengths.
+void ref_partition(const RefCsr *A, uint64_t n_parts, uint64_t *bounds) {
+    std::vector<std::size_t> row_nnz(A->n_rows);
+    for (uint64_t r = 0; r < A->n_rows; ++r) row_nnz[r] = A->off[r + 1] - A->off[r];
+    const auto b = spira::parallel::compute_partition_boundaries(row_nnz, n_parts);
+    for (uint64_t t = 0; t <= n_parts; ++t) bounds[t] = b[t];
+}
+
 // load_csr validation: 0 if Spira accepts the CSR, 1 (invalid_argument) else.
 int ref_load_check(const RefCsr *A) {
     try {

@@ -419,3 +419,119 @@ int orc_transpose(const orc_csr *A, orc_csr *T) {
     T->capacity = nnz;
     return ORC_OK;
 }
+
+/* ------------------------------------------------------------------------
+ * Matrix addition — serial/matrix_addition.hpp:34-110: per row a two-pointer
+ * merge of A's and B's slices; equal columns give a + b, inserted unless the
+ * sum is zero; other entries are inserted as they are; the output matrix is
+ * then locked, and build_csr drops every zero value (csr_build.hpp:49,71).
+ * ---------------------------------------------------------------------- */
+int orc_add(const orc_csr *A, const orc_csr *B, orc_csr *C) {
+    const uint64_t n = A->n_rows, cap = A->nnz + B->nnz;
+    uint64_t *off = (uint64_t *)calloc(n + 1, sizeof(uint64_t));
+    uint32_t *cc = (uint32_t *)malloc((cap ? cap : 1) * sizeof(uint32_t));
+    double *cv = (double *)malloc((cap ? cap : 1) * sizeof(double));
+    if (!off || !cc || !cv) return ORC_ERR_ALLOC;
+    uint64_t w = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        uint64_t i = A->off ? A->off[r] : 0, ie = A->off ? A->off[r + 1] : 0;
+        uint64_t j = B->off ? B->off[r] : 0, je = B->off ? B->off[r + 1] : 0;
+        while (i < ie || j < je) {
+            uint32_t col;
+            double v;
+            if (j >= je || (i < ie && A->cols[i] < B->cols[j])) {
+                col = A->cols[i];
+                v = A->vals[i++];
+            } else if (i >= ie || B->cols[j] < A->cols[i]) {
+                col = B->cols[j];
+                v = B->vals[j++];
+            } else {
+                col = A->cols[i];
+                v = A->vals[i++] + B->vals[j++];
+            }
+            if (!is_zero(v)) { /* the sum test of the merge, and the lock's zero drop */
+                cc[w] = col;
+                cv[w] = v;
+                ++w;
+            }
+        }
+        off[r + 1] = w;
+    }
+    C->n_rows = n;
+    C->n_cols = A->n_cols;
+    C->off = off;
+    C->cols = cc;
+    C->vals = cv;
+    C->nnz = w;
+    C->capacity = w;
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------
+ * Scalar multiply / divide — serial/scalars.hpp:22-35 and 51-67 (copy path):
+ * every value times (or over) the scalar, inserted into a fresh matrix that
+ * is then locked (zero results dropped).
+ * ---------------------------------------------------------------------- */
+int orc_scale(const orc_csr *A, double s, int divide, orc_csr *C) {
+    const uint64_t n = A->n_rows, m = A->nnz;
+    uint64_t *off = (uint64_t *)calloc(n + 1, sizeof(uint64_t));
+    uint32_t *cc = (uint32_t *)malloc((m ? m : 1) * sizeof(uint32_t));
+    double *cv = (double *)malloc((m ? m : 1) * sizeof(double));
+    if (!off || !cc || !cv) return ORC_ERR_ALLOC;
+    uint64_t w = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        for (uint64_t k = A->off[r]; k < A->off[r + 1]; ++k) {
+            const double v = divide ? A->vals[k] / s : A->vals[k] * s;
+            if (!is_zero(v)) {
+                cc[w] = A->cols[k];
+                cv[w] = v;
+                ++w;
+            }
+        }
+        off[r + 1] = w;
+    }
+    C->n_rows = n;
+    C->n_cols = A->n_cols;
+    C->off = off;
+    C->cols = cc;
+    C->vals = cv;
+    C->nnz = w;
+    C->capacity = w;
+    return ORC_OK;
+}
+
+/* Row sums of a locked matrix — csr_storage_soa.hpp:114-120 via
+ * row.hpp:208-216: acc += v in CSR order from 0. */
+void orc_row_sums(const uint64_t *off, const double *vals, uint64_t n_rows, double *out) {
+    for (uint64_t r = 0; r < n_rows; ++r) {
+        double acc = 0.0;
+        for (uint64_t k = off[r]; k < off[r + 1]; ++k) acc += vals[k];
+        out[r] = acc;
+    }
+}
+
+/* nnz-balanced boundaries — parallel/partition.hpp:78-126, with the row nnz
+ * prefix taken from the CSR offsets: bounds[t] = lower_bound(prefix from
+ * bounds[t - 1], max(1, t * nnz / T)), clamped to n; uniform when nnz == 0;
+ * {0, n, ..., n} for T <= 1 or no rows. */
+void orc_partition(const uint64_t *off, uint64_t n_rows, uint64_t T, uint64_t *bounds) {
+    bounds[0] = 0;
+    for (uint64_t t = 1; t <= T; ++t) bounds[t] = n_rows;
+    if (T <= 1 || n_rows == 0) return;
+    const uint64_t total = off[n_rows];
+    if (total == 0) {
+        for (uint64_t t = 1; t < T; ++t) bounds[t] = t * n_rows / T;
+        return;
+    }
+    for (uint64_t t = 1; t < T; ++t) {
+        uint64_t target = t * total / T;
+        if (target < 1) target = 1;
+        uint64_t lo = bounds[t - 1], hi = n_rows + 1;
+        while (lo < hi) {
+            const uint64_t mid = lo + (hi - lo) / 2;
+            if (off[mid] < target) lo = mid + 1;
+            else hi = mid;
+        }
+        bounds[t] = lo < n_rows ? lo : n_rows;
+    }
+}

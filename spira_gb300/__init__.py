@@ -65,8 +65,13 @@ class Unsupported(SpgError):
     code = 7
 
 
+class DomainError(SpgError, ArithmeticError):
+    """std::domain_error in Spira (division by a zero scalar)."""
+    code = 8
+
+
 _ERRORS = {c.code: c for c in (InvalidArgument, LogicError, OutOfRange, NoMemory, CudaError, DeviceTimeout,
-                               Unsupported)}
+                               Unsupported, DomainError)}
 
 
 class _Info(C.Structure):
@@ -108,6 +113,7 @@ _SIGS = [
     ("spg_spmv_features", _I, [_P, _P, _P]),
     ("spg_spmv_autotune", _I, [_P, _P, _I, _P, C.POINTER(_I)]),
     ("spg_probe_gather_rate", _I, [_P, _U64, _U64, C.POINTER(C.c_double)]),
+    ("spg_probe_fp64_rate", _I, [_P, C.c_uint32, C.POINTER(C.c_double)]),
     ("spg_selector_load", _I, [_P, _P, _U64, _I]),
     ("spg_mlp_param_count", _U64, [_I]),
     ("spg_selector_predict", _I, [_P, _P, _U32, _P, _P]),
@@ -121,6 +127,12 @@ _SIGS = [
     ("spg_batch_run", _I, [_P, _P, _P]),
     ("spg_batch_run_plain", _I, [_P, _P, _P]),
     ("spg_batch_destroy", _I, [_P]),
+    ("spg_csr_add", _I, [_P, _P, _P, _P]),
+    ("spg_csr_scale", _I, [_P, _P, _P, C.c_double, _I]),
+    ("spg_csr_row_sums", _I, [_P, _P, _P, _P]),
+    ("spg_csr_row_sums_host", _I, [_P, _P, _U64, _U64, _P]),
+    ("spg_csr_lookup", _I, [_P, _P, _U64, _P, _P, _P, _P, _P]),
+    ("spg_csr_partition", _I, [_P, _P, _U64, _P]),
     ("spg_transpose", _I, [_P, _P, _P]),
     ("spg_spgemm", _I, [_P, _P, _P, _P]),
     # spg_gen.h
@@ -214,6 +226,13 @@ class Context:
         ceiling of SpMV on matrices with randomly spread columns."""
         r = C.c_double()
         _check(lib().spg_probe_gather_rate(self.h, n_x, n_gathers, C.byref(r)))
+        return r.value
+
+    def probe_fp64_rate(self, iters: int = 4096) -> float:
+        """FP64 fused multiply-adds per second over every SM: the ceiling of
+        the batched multi-RHS SpMV (one FMA per nonzero and right-hand side)."""
+        r = C.c_double()
+        _check(lib().spg_probe_fp64_rate(self.h, iters, C.byref(r)))
         return r.value
 
 
@@ -343,6 +362,54 @@ class Csr:
         Cm = Csr(self.ctx, 0, 0)
         _check(lib().spg_spgemm(self.ctx.h, self.h, B.h, Cm.h))
         return Cm
+
+    def add(self, B: "Csr") -> "Csr":
+        """A new device matrix holding self + B (MatrixAddition)."""
+        Cm = Csr(self.ctx, 0, 0)
+        _check(lib().spg_csr_add(self.ctx.h, self.h, B.h, Cm.h))
+        return Cm
+
+    def scaled(self, s: float, divide: bool = False) -> "Csr":
+        """A new device matrix holding self * s (or self / s)."""
+        Cm = Csr(self.ctx, 0, 0)
+        _check(lib().spg_csr_scale(self.ctx.h, self.h, Cm.h, float(s), int(divide)))
+        return Cm
+
+    def scale_(self, s: float, divide: bool = False) -> "Csr":
+        """In place: self *= s (or self /= s)."""
+        _check(lib().spg_csr_scale(self.ctx.h, self.h, self.h, float(s), int(divide)))
+        return self
+
+    def row_sums(self, d_out=None, stream=None):
+        """Row sums in CSR order (a locked row's accumulate()); a torch CUDA
+        tensor, or written into d_out asynchronously."""
+        if d_out is None:
+            import torch
+            out = torch.empty(self.n_rows, dtype=torch.float64, device="cuda")
+            _check(lib().spg_csr_row_sums(self.ctx.h, self.h, _ptr(out), None))
+            self.ctx.sync()
+            return out
+        _check(lib().spg_csr_row_sums(self.ctx.h, self.h, _ptr(d_out), stream))
+        return d_out
+
+    def row_sums_host(self, row0: int = 0, n: int | None = None) -> np.ndarray:
+        n = self.n_rows - row0 if n is None else n
+        out = np.empty(n, np.float64)
+        _check(lib().spg_csr_row_sums_host(self.ctx.h, self.h, row0, n, _ptr(out)))
+        return out
+
+    def lookup(self, d_rows, d_cols, d_vals=None, d_found=None, stream=None):
+        """Batched point lookups on device arrays (uint64 rows, uint32 cols):
+        writes the stored value (or 0.0) and a found flag (uint8) per query."""
+        n = int(d_rows.numel()) if hasattr(d_rows, "numel") else len(d_rows)
+        _check(lib().spg_csr_lookup(self.ctx.h, self.h, n, _ptr(d_rows), _ptr(d_cols), _ptr(d_vals), _ptr(d_found),
+                                    stream))
+
+    def partition(self, n_parts: int) -> np.ndarray:
+        """nnz-balanced row boundaries (n_parts + 1 entries)."""
+        b = np.empty(n_parts + 1, np.uint64)
+        _check(lib().spg_csr_partition(self.ctx.h, self.h, n_parts, _ptr(b)))
+        return b
 
 
 # ---------------------------------------------------------------- device draws

@@ -87,6 +87,7 @@ const char *spg_strerror(int status) {
         case SPG_ERR_CUDA: return "CUDA runtime error";
         case SPG_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
         case SPG_ERR_UNSUPPORTED: return "unsupported";
+        case SPG_ERR_DOMAIN: return "domain error";
         default: return "unknown status";
     }
 }

@@ -268,9 +268,6 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 // a key wider than 32 bits inside a tile); the outputs are then undefined.
 int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
                       uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s);
-// Device reduction: max over uint32 array (returns through *h_max, syncs).
-int reduce_max_u32(Ctx *c, const uint32_t *d, uint64_t n, uint32_t *h_max,
-                   cudaStream_t s);
 
 // CSR helpers used by several ops (spg_lock.cu).
 int csr_alloc(Csr *A, uint64_t capacity, cudaStream_t s);

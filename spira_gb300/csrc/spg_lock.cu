@@ -72,13 +72,30 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
         mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
         mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
     }
-    const bool wd = __any_sync(0xffffffffu, d), wg = __any_sync(0xffffffffu, g), we = __any_sync(0xffffffffu, e);
+    const unsigned flags = (__any_sync(0xffffffffu, d) ? 1u : 0u) | (__any_sync(0xffffffffu, g) ? 2u : 0u) |
+                           (__any_sync(0xffffffffu, e) ? 4u : 0u);
+    // one set of atomics per block: per-warp atomics on the same two words
+    // serialise at L2 and cost more than the pass itself
+    __shared__ unsigned s_mr[LB / 32], s_mc[LB / 32], s_fl[LB / 32];
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        atomicMax(stats, mr);
-        atomicMax(stats + 1, mc);
-        if (wd) stats[2] = 1u;
-        if (wg) stats[3] = 1u;
-        if (we) stats[4] = 1u;
+        s_mr[w] = mr;
+        s_mc[w] = mc;
+        s_fl[w] = flags;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned bm = 0, bc = 0, bf = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            bm = max(bm, s_mr[i]);
+            bc = max(bc, s_mc[i]);
+            bf |= s_fl[i];
+        }
+        atomicMax(stats, bm);
+        atomicMax(stats + 1, bc);
+        if (bf & 1u) stats[2] = 1u;
+        if (bf & 2u) stats[3] = 1u;
+        if (bf & 4u) stats[4] = 1u;
     }
 }
 
@@ -139,19 +156,83 @@ __global__ void lock_gather_delta(const uint64_t *__restrict__ keys, const uint3
     }
 }
 
-// off[r] = lower_bound(sorted_rows[0..u), r) for r in [0, n_rows].
-__global__ void offsets_from_sorted_rows(const uint32_t *__restrict__ srows, uint64_t u, uint64_t n_rows,
-                                         uint64_t *__restrict__ off) {
-    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r <= n_rows;
-         r += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t lo = 0, hi = u;
-        while (lo < hi) {
-            const uint64_t mid = (lo + hi) >> 1;
-            if ((uint64_t)srows[mid] < r) lo = mid + 1;
-            else hi = mid;
+// off[r] = lower_bound(sorted_rows[0..u), r) for r in [0, n_rows], from the
+// row boundaries: position i (i == u standing for row n_rows) is the first
+// position of rows srows[i - 1] + 1 .. srows[i], so it writes those offsets.
+// One pass over the rows, coalesced, no searches. Runs of up to GAP_LONG
+// empty rows are written by the thread at their boundary; longer ones are
+// listed in `gaps` (up to GAP_SLOTS of them) for offsets_fill_gaps to spread
+// over the grid, and written by their thread once the list is full. A
+// decreasing step (never in the sorted input) writes nothing, so every write
+// stays inside [0, n_rows].
+constexpr uint64_t GAP_LONG = 4096;
+constexpr unsigned GAP_SLOTS = 1024;
+
+struct RowGap {
+    uint64_t lo, hi, pos;
+};
+
+constexpr int OFF_T = 256, OFF_E = 8, OFF_TILE = OFF_T * OFF_E;  // positions per block step
+
+// Block steps over tiles of OFF_TILE positions: the tile's rows (and the one
+// before it) are staged in shared memory with coalesced loads, then thread t
+// checks positions t, t + OFF_T, ... against their predecessors, so a
+// position costs a few instructions and only row boundaries write.
+__global__ void __launch_bounds__(OFF_T)
+offsets_from_sorted_rows(const uint32_t *__restrict__ srows, uint64_t u, uint64_t n_rows,
+                         uint64_t *__restrict__ off, RowGap *__restrict__ gaps, unsigned *__restrict__ n_gaps) {
+    __shared__ uint64_t s_row[OFF_TILE + 1];  // s_row[j] = row at position tile + j - 1
+    for (uint64_t tile = blockIdx.x * (uint64_t)OFF_TILE; tile <= u; tile += (uint64_t)gridDim.x * OFF_TILE) {
+        for (int j = threadIdx.x; j <= OFF_TILE; j += OFF_T) {
+            const uint64_t p = tile + j - 1;  // tile == 0, j == 0: never read
+            s_row[j] = (tile + j >= 1 && p < u) ? min((uint64_t)srows[p], n_rows) : n_rows;
         }
-        off[r] = lo;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < OFF_E; ++k) {
+            const int j = threadIdx.x + k * OFF_T;
+            const uint64_t i = tile + j;
+            if (i > u) break;
+            const uint64_t cur = s_row[j + 1];
+            const uint64_t lo = i == 0 ? 0 : s_row[j] + 1;  // rows [lo, cur] start at position i
+            if (cur + 1 <= lo) continue;  // inside a row (or a decreasing step: nothing)
+            uint64_t hi = cur + 1;
+            if (hi - lo > GAP_LONG) {
+                const unsigned slot = atomicAdd(n_gaps, 1u);
+                if (slot < GAP_SLOTS) {
+                    gaps[slot] = {lo, hi, i};
+                    continue;  // listed: written by offsets_fill_gaps
+                }
+            }
+            for (uint64_t r = lo; r < hi; ++r) off[r] = i;
+        }
+        __syncthreads();
     }
+}
+
+// The listed long stretches of empty rows, each spread over the whole grid.
+__global__ void offsets_fill_gaps(const RowGap *__restrict__ gaps, const unsigned *__restrict__ n_gaps,
+                                  uint64_t *__restrict__ off) {
+    const unsigned n = min(*n_gaps, GAP_SLOTS);
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nt = (uint64_t)gridDim.x * blockDim.x;
+    for (unsigned g = 0; g < n; ++g) {
+        const RowGap G = gaps[g];
+        for (uint64_t r = G.lo + t; r < G.hi; r += nt) off[r] = G.pos;
+    }
+}
+
+// off[0..n_rows] from the non-decreasing rows srows[0..u) (stream-ordered).
+int launch_row_offsets(Ctx *c, const uint32_t *srows, uint64_t u, uint64_t n_rows, uint64_t *off, cudaStream_t s) {
+    DevBuf scratch;  // [counter (16 bytes)] [GAP_SLOTS gaps]
+    SPG_TRY(scratch.alloc(16 + GAP_SLOTS * sizeof(RowGap), s));
+    unsigned *n_gaps = scratch.as<unsigned>();
+    RowGap *gaps = reinterpret_cast<RowGap *>(scratch.as<char>() + 16);
+    SPG_CUDA_TRY(cudaMemsetAsync(n_gaps, 0, sizeof(unsigned), s));
+    offsets_from_sorted_rows<<<grid_for(u + 1, OFF_TILE, (unsigned)c->n_sms * 8), OFF_T, 0, s>>>(srows, u, n_rows, off,
+                                                                                            gaps, n_gaps);
+    offsets_fill_gaps<<<c->n_sms * 4, LB, 0, s>>>(gaps, n_gaps, off);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
 }
 
 // Step 3: insertion point / collision / contribution of every delta entry.
@@ -409,9 +490,7 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
     if (!f[1]) {  // the row-grouped sort reads rows and columns directly
         DevBuf s_off, keys2, idx2;
         SPG_TRY(s_off.alloc((n_rows + 1) * sizeof(uint64_t), s));
-        offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
-            rows, m, n_rows, s_off.as<uint64_t>());
-        SPG_LAUNCH_CHECK();
+        SPG_TRY(launch_row_offsets(c, rows, m, n_rows, s_off.as<uint64_t>(), s));
         SPG_TRY(keys2.alloc(m * sizeof(uint64_t), s));
         SPG_TRY(idx2.alloc(m * sizeof(uint32_t), s));
         bool done = false;
@@ -453,9 +532,7 @@ int sort_dedup(Ctx *c, const uint32_t *rows, const uint32_t *cols, const double 
 
 int row_offsets(Ctx *c, const uint32_t *srows, uint64_t u, uint64_t n_rows, DevBuf &doff, cudaStream_t s) {
     SPG_TRY(doff.alloc((n_rows + 1) * sizeof(uint64_t), s));
-    offsets_from_sorted_rows<<<grid_for(n_rows + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
-        srows, u, n_rows, doff.as<uint64_t>());
-    SPG_LAUNCH_CHECK();
+    SPG_TRY(launch_row_offsets(c, srows, u, n_rows, doff.as<uint64_t>(), s));
     return SPG_OK;
 }
 
@@ -479,14 +556,13 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         first_direct_copy<<<g, LB, 0, s>>>(cols, vals, m, out_cols.as<uint32_t>(), out_vals.as<double>(),
                                            zero.as<unsigned>());
         SPG_LAUNCH_CHECK();
+        // the offsets go out before the zero check comes back: one host sync
+        SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
+        SPG_TRY(launch_row_offsets(c, rows, m, n, new_off.as<uint64_t>(), s));
         unsigned hz = 1;
         SPG_CUDA_TRY(cudaMemcpyAsync(&hz, zero.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
         if (!hz) {
-            SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
-            offsets_from_sorted_rows<<<grid_for(n + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
-                rows, m, n, new_off.as<uint64_t>());
-            SPG_LAUNCH_CHECK();
             A->invalidate_derived();
             A->off = std::move(new_off);
             A->cols = std::move(out_cols);
@@ -495,9 +571,9 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
             A->capacity = m;  // build_csr: exact
             A->built = true;
             A->may_have_zeros = false;
-            SPG_CUDA_TRY(cudaStreamSynchronize(s));
             return SPG_OK;
         }
+        new_off.release();
         out_cols.release();
         out_vals.release();
     }
@@ -521,9 +597,7 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         SPG_TRY(out_vals.alloc(csr_alloc_elems(0) * sizeof(double), s));
     }
     SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
-    offsets_from_sorted_rows<<<grid_for(n + 1, LB, (unsigned)c->n_sms * 32), LB, 0, s>>>(
-        orow.as<uint32_t>(), nnz, n, new_off.as<uint64_t>());
-    SPG_LAUNCH_CHECK();
+    SPG_TRY(launch_row_offsets(c, orow.as<uint32_t>(), nnz, n, new_off.as<uint64_t>(), s));
     A->invalidate_derived();
     A->off = std::move(new_off);
     A->cols = std::move(out_cols);

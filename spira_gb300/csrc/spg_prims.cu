@@ -604,32 +604,4 @@ int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const 
     return SPG_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Max reduction (used for device-side index range checks)
-// ---------------------------------------------------------------------------
-namespace {
-__global__ void max_u32_kernel(const uint32_t *__restrict__ d, uint64_t n, unsigned *out) {
-    unsigned m = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        m = max(m, d[i]);
-#pragma unroll
-    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
-}
-}  // namespace
-
-int reduce_max_u32(Ctx *c, const uint32_t *d, uint64_t n, uint32_t *h_max, cudaStream_t s) {
-    DevBuf out;
-    SPG_TRY(out.alloc(sizeof(unsigned), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(out.ptr, 0, sizeof(unsigned), s));
-    if (n) {
-        max_u32_kernel<<<grid_for(n, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(d, n, out.as<unsigned>());
-        SPG_LAUNCH_CHECK();
-    }
-    SPG_CUDA_TRY(cudaMemcpyAsync(h_max, out.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
-    return SPG_OK;
-}
-
 }  // namespace spg

@@ -284,7 +284,13 @@ __global__ void seg_max_row(const uint64_t *__restrict__ off, uint64_t n, unsign
         m = max(m, (unsigned long long)(off[r + 1] - off[r]));
 #pragma unroll
     for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+    __shared__ unsigned long long s_m[32];  // one atomic per block, not per warp
+    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned w = 1; w < (blockDim.x >> 5); ++w) m = max(m, s_m[w]);
+        atomicMax(mx, m);
+    }
 }
 
 __global__ void seg_empty_rows(const uint32_t *__restrict__ empty, uint64_t n_empty, double *__restrict__ y) {

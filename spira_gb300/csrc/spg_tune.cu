@@ -51,6 +51,25 @@ __global__ void gather_probe(const double *__restrict__ x, uint32_t mask, double
     out[t] = a;
 }
 
+// FP64 FMA rate: 8 independent chains per thread (enough warps and chains to
+// cover the pipe's latency); a = a * m + c with |m| < 1 stays bounded. m and c
+// are arguments, so nothing folds at compile time.
+constexpr int FMA_CHAINS = 8;
+
+__global__ void __launch_bounds__(256) fma_probe(double m, double c, uint32_t iters, double *__restrict__ out) {
+    double a[FMA_CHAINS];
+#pragma unroll
+    for (int i = 0; i < FMA_CHAINS; ++i) a[i] = (double)(threadIdx.x + i);
+    for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < FMA_CHAINS; ++i) a[i] = fma(a[i], m, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < FMA_CHAINS; ++i) s += a[i];
+    out[blockIdx.x * (uint64_t)blockDim.x + threadIdx.x] = s;
+}
+
 // ---------------------------------------------------------------- features
 // acc layout (doubles): [0..31] histogram, 32 sum L, 33 sum L^2, 34 max L,
 // 35 empty rows, 36 sum of |col/n_cols - row/n_rows| over sampled nonzeros,
@@ -546,6 +565,38 @@ int spg_probe_gather_rate(spg_ctx *c, uint64_t n_x, uint64_t n_gathers, double *
     SPG_LAUNCH_CHECK();
     std::sort(ts.begin(), ts.end());
     *gathers_per_s = (double)(n_thr * GATHER_PER_THREAD) / (ts[ts.size() / 2] * 1e-3);
+    return SPG_OK;
+}
+
+int spg_probe_fp64_rate(spg_ctx *c, uint32_t iters, double *fma_per_s) {
+    if (!c || !fma_per_s) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_fp64_rate: null argument");
+    if (iters < 16 || iters > (1u << 20))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_fp64_rate: iters must be in [16, 2^20]");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const unsigned grid = (unsigned)(8 * c->n_sms);
+    DevBuf out;
+    SPG_TRY(out.alloc((uint64_t)grid * 256 * sizeof(double), s));
+    cudaEvent_t e0, e1;
+    SPG_CUDA_TRY(cudaEventCreate(&e0));
+    SPG_CUDA_TRY(cudaEventCreate(&e1));
+    std::vector<float> ts;
+    int rc = SPG_OK;
+    for (int r = 0; r < 7 && rc == SPG_OK; ++r) {
+        cudaEventRecord(e0, s);
+        fma_probe<<<grid, 256, 0, s>>>(0.999999, 1e-3, iters, out.as<double>());
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) rc = set_error(SPG_ERR_CUDA, "fp64 probe: event sync failed");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r >= 2) ts.push_back(ms);  // two warm-up runs
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SPG_TRY(rc);
+    SPG_LAUNCH_CHECK();
+    std::sort(ts.begin(), ts.end());
+    *fma_per_s = (double)grid * 256.0 * FMA_CHAINS * iters / (ts[ts.size() / 2] * 1e-3);
     return SPG_OK;
 }
 

@@ -314,6 +314,236 @@ TEST(Partition, BoundariesContract) {
     EXPECT_EQ(z[3], 6u);
 }
 
+// tests/serial/matrix_addition_tests.cpp:152-217
+TEST(MatrixAddition, ThrowsOnShapeMismatch) {
+    MA A(2, 3);
+    MA B(3, 2);
+    EXPECT_THROW(spira::serial::algorithms::MatrixAddition(A, B), std::invalid_argument);
+}
+
+TEST(MatrixAddition, AddsMatricesElementwise_Sparse) {
+    MA A(3, 4);
+    MA B(3, 4);
+    A.insert(0, 0, 1.0);
+    A.insert(0, 3, 2.0);
+    A.insert(2, 1, 3.0);
+    B.insert(0, 0, 10.0);
+    B.insert(1, 2, 20.0);
+    B.insert(2, 1, -3.0);
+    A.lock();
+    B.lock();
+    auto C = spira::serial::algorithms::MatrixAddition(A, B);
+    auto [r, c] = C.shape();
+    EXPECT_EQ(r, 3u);
+    EXPECT_EQ(c, 4u);
+    EXPECT_EQ(C.get(0, 0), 11.0);
+    EXPECT_EQ(C.get(0, 3), 2.0);
+    EXPECT_EQ(C.get(1, 2), 20.0);
+    EXPECT_EQ(C.get(2, 1), 0.0);
+    EXPECT_FALSE(C.contains(2, 1));  // the zero sum is dropped
+    EXPECT_EQ(C.get(2, 3), 0.0);
+    EXPECT_EQ(A.get(0, 0), 1.0);
+    EXPECT_EQ(B.get(0, 0), 10.0);
+    EXPECT_EQ(A.get(2, 1), 3.0);
+    EXPECT_EQ(B.get(2, 1), -3.0);
+}
+
+TEST(MatrixAddition, ZeroMatrix_AdditionKeepsOriginal) {
+    MA A(2, 2);
+    MA Z(2, 2);
+    A.insert(0, 1, 7.0);
+    A.insert(1, 0, 9.0);
+    A.lock();
+    Z.lock();
+    auto C = spira::serial::algorithms::MatrixAddition(A, Z);
+    EXPECT_EQ(C.get(0, 1), 7.0);
+    EXPECT_EQ(C.get(1, 0), 9.0);
+    EXPECT_EQ(C.get(0, 0), 0.0);
+    EXPECT_EQ(C.get(1, 1), 0.0);
+    EXPECT_EQ(C.nnz(), 2u);
+}
+
+// matrix_operators.hpp:18-62, 104-140: +, -, +=, -=, * s, / s
+TEST(MatrixOperators, AddSubScale) {
+    MS A(3, 3), B(3, 3);
+    A.insert(0, 0, 1.5);
+    A.insert(1, 2, -2.0);
+    B.insert(0, 0, 0.5);
+    B.insert(2, 1, 4.0);
+    A.lock();
+    B.lock();
+    auto S = A + B;
+    auto D = A - B;
+    EXPECT_EQ(S.get(0, 0), 2.0);
+    EXPECT_EQ(S.get(2, 1), 4.0);
+    EXPECT_EQ(D.get(0, 0), 1.0);
+    EXPECT_EQ(D.get(2, 1), -4.0);
+    EXPECT_EQ(D.get(1, 2), -2.0);
+    auto Z = A - A;
+    EXPECT_EQ(Z.nnz(), 0u);
+    auto T = A * 2.0;
+    EXPECT_EQ(T.get(1, 2), -4.0);
+    auto H = A / 4.0;
+    EXPECT_EQ(H.get(0, 0), 0.375);
+    EXPECT_THROW(A / 0.0, std::domain_error);
+    MS E(3, 4);
+    E.lock();
+    EXPECT_THROW(A + E, std::invalid_argument);
+    A += B;
+    EXPECT_EQ(A.get(0, 0), 2.0);
+    A -= B;
+    EXPECT_EQ(A.get(0, 0), 1.5);
+    EXPECT_FALSE(A.contains(2, 1));
+}
+
+// tests/serial/scalar_tests.cpp:30-117
+TEST(Scalers, MultiplicationScaler_ScalesExistingEntries) {
+    MA m(3, 4);
+    m.insert(0, 0, 1.5);
+    m.insert(0, 3, -2.0);
+    m.insert(2, 1, 4.0);
+    spira::serial::algorithms::multiplication_scaler(m, 3.0);
+    EXPECT_NEAR(m.get(0, 0), 4.5, 1e-12);
+    EXPECT_NEAR(m.get(0, 3), -6.0, 1e-12);
+    EXPECT_NEAR(m.get(2, 1), 12.0, 1e-12);
+    EXPECT_NEAR(m.get(1, 1), 0.0, 1e-12);
+    EXPECT_NEAR(m.get(2, 3), 0.0, 1e-12);
+}
+
+TEST(Scalers, DivisionScaler_ScalesExistingEntries) {
+    MA m(2, 3);
+    m.insert(0, 2, 10.0);
+    m.insert(1, 0, -6.0);
+    spira::serial::algorithms::division_scaler(m, 2.0);
+    EXPECT_NEAR(m.get(0, 2), 5.0, 1e-12);
+    EXPECT_NEAR(m.get(1, 0), -3.0, 1e-12);
+    EXPECT_NEAR(m.get(0, 0), 0.0, 1e-12);
+}
+
+TEST(Scalers, MultiplyThenDivide_ReturnsOriginal_ForNonZeroScaler) {
+    MA m(3, 3);
+    m.insert(0, 1, 1.25);
+    m.insert(2, 2, -9.0);
+    m.insert(1, 0, 0.5);
+    const double a01 = m.get(0, 1), a22 = m.get(2, 2), a10 = m.get(1, 0);
+    spira::serial::algorithms::multiplication_scaler(m, 7.0);
+    spira::serial::algorithms::division_scaler(m, 7.0);
+    EXPECT_NEAR(m.get(0, 1), a01, 1e-12);
+    EXPECT_NEAR(m.get(2, 2), a22, 1e-12);
+    EXPECT_NEAR(m.get(1, 0), a10, 1e-12);
+    EXPECT_NEAR(m.get(0, 0), 0.0, 1e-12);
+}
+
+TEST(Scalers, MultiplyByZero_MakesEntriesZero) {
+    MA m(2, 2);
+    m.insert(0, 0, 3.0);
+    m.insert(1, 1, -4.0);
+    spira::serial::algorithms::multiplication_scaler(m, 0.0);
+    EXPECT_NEAR(m.get(0, 0), 0.0, 1e-12);
+    EXPECT_NEAR(m.get(1, 1), 0.0, 1e-12);
+}
+
+TEST(Scalers, DivisionByZero_Behavior) {
+    MA m(1, 3);
+    m.insert(0, 1, 2.0);
+    EXPECT_THROW(spira::serial::algorithms::division_scaler(m, 0.0), std::domain_error);
+}
+
+// In place on a re-opened matrix: the committed values are scaled on the
+// device and survive the next lock; a staged insert at a committed position
+// is overridden by the scaled committed value (it was staged before it).
+TEST(Scalers, InPlaceAfterLock_ScalesCommittedValues) {
+    MS m(3, 3);
+    m.insert(0, 0, 2.0);
+    m.insert(1, 1, 3.0);
+    m.lock();
+    m.open();
+    m.insert(1, 1, 100.0);
+    m.insert(2, 2, 5.0);
+    spira::serial::algorithms::multiplication_scaler(m, 0.5);
+    m.lock();
+    EXPECT_EQ(m.get(0, 0), 1.0);
+    EXPECT_EQ(m.get(1, 1), 1.5);
+    EXPECT_EQ(m.get(2, 2), 5.0);
+    MS out(1, 1);
+    spira::serial::algorithms::multiplication_scaler(m, out, 4.0);
+    EXPECT_EQ(out.get(1, 1), 6.0);
+    EXPECT_EQ(out.nnz(), 3u);
+}
+
+// tests/serial/accumulate_algo_tests.cpp:26-160
+TEST(Accumulate, SingleRowAndWholeMatrix) {
+    using namespace spira::serial::algorithms;
+    MA empty(3, 5);
+    EXPECT_DOUBLE_EQ(accumulate(empty, 0), 0.0);
+    EXPECT_THROW(accumulate(empty, 3), std::out_of_range);
+    EXPECT_THROW(accumulate(empty, 100), std::out_of_range);
+    auto z = accumulate(empty);
+    EXPECT_EQ(z.size(), 3u);
+    MA mat(3, 5);
+    mat.insert(0, 0, 1.0);
+    mat.insert(0, 1, 2.0);
+    mat.insert(1, 0, 10.0);
+    mat.insert(2, 0, 100.0);
+    mat.insert(2, 1, 200.0);
+    mat.insert(2, 2, 300.0);
+    auto open_r = accumulate(mat);
+    EXPECT_DOUBLE_EQ(open_r[0], 3.0);
+    EXPECT_DOUBLE_EQ(open_r[1], 10.0);
+    EXPECT_DOUBLE_EQ(open_r[2], 600.0);
+    mat.lock();
+    auto locked_r = accumulate(mat);
+    for (int i = 0; i < 3; ++i) EXPECT_DOUBLE_EQ(open_r[i], locked_r[i]);
+    MA ow(1, 5);
+    ow.insert(0, 0, 10.0);
+    ow.insert(0, 0, 25.0);
+    EXPECT_DOUBLE_EQ(accumulate(ow, 0), 25.0);
+    ow.lock();
+    EXPECT_DOUBLE_EQ(accumulate(ow, 0), 25.0);
+    // open after a lock: staged entries shadow committed ones
+    ow.open();
+    ow.insert(0, 0, 1.0);
+    ow.insert(0, 4, 2.0);
+    EXPECT_DOUBLE_EQ(accumulate(ow, 0), 3.0);
+    MA canc(1, 5);
+    canc.insert(0, 0, -3.0);
+    canc.insert(0, 1, 5.0);
+    canc.insert(0, 2, -2.0);
+    EXPECT_DOUBLE_EQ(accumulate(canc, 0), 0.0);
+}
+
+// parallel/algorithms/matrix_addition.hpp, scalars.hpp, accumulate.hpp and
+// parallel_matrix::rebalance
+TEST(ParallelAlgorithms, AdditionScalersAccumulateRebalance) {
+    using PM = spira::parallel::parallel_matrix<SoA, uint32_t, double>;
+    PM A(100, 100, 4), B(100, 100, 4), C3(100, 100, 3);
+    for (uint32_t r = 0; r < 100; ++r) {
+        A.insert(r, r, 1.0 + r);
+        if (r < 10)
+            for (uint32_t c = 0; c < 50; ++c) B.insert(r, c, 0.5);
+    }
+    A.lock();
+    B.lock();
+    C3.lock();
+    EXPECT_THROW(spira::parallel::algorithms::MatrixAddition(A, C3), std::invalid_argument);
+    auto S = spira::parallel::algorithms::MatrixAddition(A, B);
+    EXPECT_EQ(S.get(3, 3), 4.5);
+    EXPECT_EQ(S.get(3, 4), 0.5);
+    EXPECT_EQ(S.get(50, 50), 51.0);
+    EXPECT_EQ(S.nnz(), 100u + 500u - 10u);
+    auto acc = spira::parallel::algorithms::accumulate(S);
+    EXPECT_DOUBLE_EQ(acc[0], 1.0 + 49 * 0.5 + 0.5);
+    EXPECT_DOUBLE_EQ(spira::parallel::algorithms::accumulate(S, 99), 100.0);
+    PM out(100, 100, 4);
+    spira::parallel::algorithms::multiplication_scaler(S, out, 2.0);
+    EXPECT_EQ(out.get(50, 50), 102.0);
+    EXPECT_THROW(spira::parallel::algorithms::division_scaler(S, out, 0.0), std::domain_error);
+    S.rebalance();  // nnz-balanced on the device: the 10 dense rows get a partition of their own
+    auto p0 = S.partition_at(0);
+    EXPECT_EQ(p0.row_start, 0u);
+    EXPECT_TRUE(p0.row_end <= 10u);
+}
+
 int main() {
     int n = 0;
     for (auto &c : registry()) {

@@ -146,6 +146,31 @@ def test_lock_row_grouped_sparse_rows(ctx):
     assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(rows, cols, vals)]))
 
 
+@pytest.mark.parametrize("dups", [False, True])
+def test_lock_long_empty_stretches(ctx, dups):
+    """Row offsets across long runs of empty rows: more stretches of > 4096
+    empty rows than the offsets pass lists for the whole grid (the rest are
+    written warp by warp), a leading and a trailing stretch; strictly
+    increasing inserts (direct path) and inserts with duplicates (sorted)."""
+    n = 6_000_000
+    hot = (7000 + 4999 * np.arange(1190, dtype=np.uint64)).astype(np.uint32)
+    rows = np.repeat(hot, 2)
+    cols = np.tile(np.array([3, 9], np.uint32), len(hot))
+    if dups:
+        cols[1::2] = 3
+    vals = gen.sym_unit(gen.hash3(12, 2, np.arange(len(rows), dtype=np.uint64)))
+    A = gpu_lock(ctx, n, n, [(rows, cols, vals)])
+    assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(rows, cols, vals)]))
+
+
+def test_lock_nothing_staged_on_many_rows(ctx):
+    n = 5_000_000
+    e = np.array([], np.uint32)
+    A = gpu_lock(ctx, n, n, [(e, e, np.array([]))])
+    H = A.download()
+    assert A.nnz == 0 and len(H.off) == n + 1 and not H.off.any()
+
+
 def test_lock_zipf_long_rows(ctx):
     r, c, v = gen.zipf_rows(100_000, seed=9)
     b = gen.relock_batch(100_000, 100_000, len(r), seed=10, zero_frac=0.05)

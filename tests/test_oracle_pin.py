@@ -150,3 +150,86 @@ def test_oracle_spgemm_transpose_parallel_match_spira():
                          check_capacity=not par)
         assert_csr_equal(oracle.transpose(A), oracle.ref_transpose(A, parallel=par, n_threads=3),
                          check_capacity=not par)
+
+
+def _ops_pair(n=2500, seed=11):
+    """A and B with shared positions, exact cancellations on some of them and
+    explicit zeros (as load_csr may install) in A."""
+    ra, ca, va = gen.uniform_rows(n, n, 6, seed=seed)
+    A = oracle.lock_epochs(n, n, [(ra, ca, va)])
+    rb, cb, vb = gen.uniform_rows(n, n, 4, seed=seed + 1)
+    # B also holds every third entry of A, negated on half of them (sum +-0)
+    k = np.arange(0, len(A.cols), 3)
+    rows_a = np.repeat(np.arange(n, dtype=np.uint32), np.diff(A.off).astype(np.int64))
+    sv = np.where(np.arange(len(k)) % 2 == 0, -A.vals[k], 0.5 * A.vals[k])
+    B = oracle.lock_epochs(n, n, [(np.concatenate([rb, rows_a[k]]), np.concatenate([cb, A.cols[k]]),
+                                   np.concatenate([vb, sv]))])
+    Az = oracle.Csr(A.n_rows, A.n_cols, A.off.copy(), A.cols.copy(), A.vals.copy(), A.capacity)
+    Az.vals[1::17] = 0.0
+    Az.vals[2::23] = -0.0
+    Az.vals[5::31] = np.nan
+    return Az, B
+
+
+@needs_ref
+def test_oracle_add_matches_spira():
+    A, B = _ops_pair()
+    got = oracle.add(A, B)
+    assert_csr_equal(got, oracle.ref_add(A, B))
+    assert_csr_equal(got, oracle.ref_add(A, B, parallel=True, n_threads=3), check_capacity=False)
+    assert_csr_equal(oracle.add(B, A), oracle.ref_add(B, A))
+    with pytest.raises(ValueError):
+        oracle.ref_add(A, oracle.lock_epochs(10, 10, []))
+
+
+@needs_ref
+@pytest.mark.parametrize("s,divide", [(2.5, False), (-3.0, False), (0.0, False), (1e-310, False), (np.nan, False),
+                                      (3.0, True), (1e300, True), (-0.125, True)])
+def test_oracle_scale_matches_spira(s, divide):
+    A, _ = _ops_pair(seed=21)
+    got = oracle.scale(A, s, divide)
+    assert_csr_equal(got, oracle.ref_scale(A, s, divide))
+
+
+@needs_ref
+def test_spira_in_place_scale_is_lost_at_lock():
+    """Spira's in-place scalers (serial/scalars.hpp:10-18, 37-49) insert the
+    scaled values through row::insert, which leaves the matrix's dirty flags
+    unset; the next lock() copies every clean row's old slice
+    (csr_build.hpp:190-215), so the values come back unscaled. Only the
+    capacity moves, by the merge rule over the buffered entries: kept while
+    2 nnz fits, else 1.5 x 2 nnz. Recorded here because libspg's in-place
+    scale installs the scaled values instead."""
+    A, _ = _ops_pair(seed=21)
+    m = len(A.cols)
+    for s, divide in ((2.5, False), (3.0, True)):
+        ip = oracle.ref_scale(A, s, divide, in_place=True)
+        assert_csr_equal(ip, A, check_capacity=False)
+        assert ip.capacity == (A.capacity if 2 * m <= A.capacity else 3 * m)
+
+
+@needs_ref
+def test_oracle_division_by_zero_is_a_domain_error():
+    A, _ = _ops_pair(n=50)
+    for z in (0.0, -0.0):
+        with pytest.raises(ArithmeticError):
+            oracle.ref_scale(A, z, divide=True)
+
+
+@needs_ref
+def test_oracle_row_sums_match_spira():
+    r, c, v = gen.zipf_rows(20_000, seed=23)
+    A = oracle.lock_epochs(20_000, 20_000, [(r, c, v)])
+    np.testing.assert_array_equal(oracle.row_sums(A).view(np.uint64), oracle.ref_row_sums(A).view(np.uint64))
+
+
+@needs_ref
+@pytest.mark.parametrize("T", [1, 2, 3, 7, 64, 5000])
+def test_oracle_partition_matches_spira(T):
+    r, c, v = gen.zipf_rows(3000, seed=24)
+    A = oracle.lock_epochs(3000, 3000, [(r, c, v)])
+    np.testing.assert_array_equal(oracle.partition(A, T), oracle.ref_partition(A, T))
+    E = oracle.lock_epochs(100, 100, [])  # nnz == 0: uniform split
+    np.testing.assert_array_equal(oracle.partition(E, T), oracle.ref_partition(E, T))
+    few = oracle.lock_epochs(100, 100, [(np.array([99], np.uint32), np.array([0], np.uint32), np.array([1.0]))])
+    np.testing.assert_array_equal(oracle.partition(few, T), oracle.ref_partition(few, T))

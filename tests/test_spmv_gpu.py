@@ -165,6 +165,13 @@ def test_gather_probe(ctx):
         ctx.probe_gather_rate(1 << 20, 8)
 
 
+def test_fp64_probe(ctx):
+    r = ctx.probe_fp64_rate(256)
+    assert 1e10 < r < 1e13
+    with pytest.raises(sg.InvalidArgument):
+        ctx.probe_fp64_rate(4)
+
+
 def test_spmv_laplacian_2a_full(ctx):
     """Config 2a at full size: 5-point Laplacian on 1414^2, re-lock, SpMV."""
     r, c, v = gen.laplacian_2d(1414)
