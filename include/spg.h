@@ -282,6 +282,23 @@ int spg_csr_lookup(spg_ctx *ctx, const spg_csr *A, uint64_t n, const uint64_t *d
  * parallel_matrix::rebalance installs, parallel_matrix.hpp:434-452). */
 int spg_csr_partition(spg_ctx *ctx, const spg_csr *A, uint64_t n_parts, uint64_t *bounds);
 
+/* ---- binary CSR files (no Spira counterpart) --------------------------------
+ * Little-endian; each section starts on an 8-byte boundary:
+ *   64-byte header: magic "SPGCSR\0\0", u64 version (1), n_rows, n_cols, nnz,
+ *                   flags (bit 0: values may hold explicit +-0), checksum, 0
+ *   u64 offsets[n_rows + 1]; u32 cols[nnz] zero-padded to 8 bytes; f64 vals[nnz]
+ * checksum = sum over the payload's 64-bit words w_i (i from 0 at the first
+ * offsets word) of splitmix64_finaliser(w_i ^ (i * 0x9E3779B97F4A7C15)),
+ * modulo 2^64 (computed on the device).
+ * spg_csr_save writes a locked A (SPG_ERR_LOGIC otherwise). spg_csr_load_file
+ * reshapes A to the file's shape after checking the header against the file
+ * size, the checksum and load_csr's CSR rules (matrix.hpp:524-575); any
+ * failure gives SPG_ERR_INVALID_ARGUMENT and leaves A unchanged.
+ * spg_csr_file_info reads and checks only the header (no device needed). */
+int spg_csr_save(spg_ctx *ctx, const spg_csr *A, const char *path);
+int spg_csr_load_file(spg_ctx *ctx, spg_csr *A, const char *path);
+int spg_csr_file_info(const char *path, uint64_t *n_rows, uint64_t *n_cols, uint64_t *nnz);
+
 /* ---- transpose / SpGEMM ----------------------------------------------------
  * spg_transpose: AT <- A^T (AT is reshaped to n_cols x n_rows, capacity ==
  * nnz); each output row lists its source rows in ascending order

@@ -133,6 +133,9 @@ _SIGS = [
     ("spg_csr_row_sums_host", _I, [_P, _P, _U64, _U64, _P]),
     ("spg_csr_lookup", _I, [_P, _P, _U64, _P, _P, _P, _P, _P]),
     ("spg_csr_partition", _I, [_P, _P, _U64, _P]),
+    ("spg_csr_save", _I, [_P, _P, C.c_char_p]),
+    ("spg_csr_load_file", _I, [_P, _P, C.c_char_p]),
+    ("spg_csr_file_info", _I, [C.c_char_p, C.POINTER(_U64), C.POINTER(_U64), C.POINTER(_U64)]),
     ("spg_transpose", _I, [_P, _P, _P]),
     ("spg_spgemm", _I, [_P, _P, _P, _P]),
     # spg_gen.h
@@ -398,6 +401,15 @@ class Csr:
         _check(lib().spg_csr_row_sums_host(self.ctx.h, self.h, row0, n, _ptr(out)))
         return out
 
+    def save(self, path) -> None:
+        """Writes the CSR to a binary file (spg_csr_save)."""
+        _check(lib().spg_csr_save(self.ctx.h, self.h, str(path).encode()))
+
+    def load_file(self, path) -> "Csr":
+        """Replaces this matrix with a saved file's CSR (checked)."""
+        _check(lib().spg_csr_load_file(self.ctx.h, self.h, str(path).encode()))
+        return self
+
     def lookup(self, d_rows, d_cols, d_vals=None, d_found=None, stream=None):
         """Batched point lookups on device arrays (uint64 rows, uint32 cols):
         writes the stored value (or 0.0) and a found flag (uint8) per query."""
@@ -414,6 +426,13 @@ class Csr:
 
 # ---------------------------------------------------------------- device draws
 GEN_BELOW_U32, GEN_SYM_F64, GEN_UNIT_F64 = 0, 1, 2
+
+
+def csr_file_info(path):
+    """(n_rows, n_cols, nnz) from a CSR file's header; needs no device."""
+    r, c, z = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    _check(lib().spg_csr_file_info(str(path).encode(), C.byref(r), C.byref(c), C.byref(z)))
+    return r.value, c.value, z.value
 
 
 def gen_draw(ctx: Context, seed: int, stream: int, n: int, kind: int, bound: int, d_out, counter0: int = 0):

@@ -181,22 +181,36 @@ constexpr int OFF_T = 256, OFF_E = 8, OFF_TILE = OFF_T * OFF_E;  // positions pe
 __global__ void __launch_bounds__(OFF_T)
 offsets_from_sorted_rows(const uint32_t *__restrict__ srows, uint64_t u, uint64_t n_rows,
                          uint64_t *__restrict__ off, RowGap *__restrict__ gaps, unsigned *__restrict__ n_gaps) {
-    __shared__ uint64_t s_row[OFF_TILE + 1];  // s_row[j] = row at position tile + j - 1
+    __shared__ uint32_t s_row[OFF_TILE + 1];  // s_row[j] = row at position tile + j - 1 (when < u)
     for (uint64_t tile = blockIdx.x * (uint64_t)OFF_TILE; tile <= u; tile += (uint64_t)gridDim.x * OFF_TILE) {
-        for (int j = threadIdx.x; j <= OFF_TILE; j += OFF_T) {
+        // all loads of a thread issued before any is stored (HBM needs many
+        // bytes in flight per SM)
+        uint32_t v[OFF_E + 1];
+#pragma unroll
+        for (int k = 0; k <= OFF_E; ++k) {
+            const int j = threadIdx.x + k * OFF_T;
             const uint64_t p = tile + j - 1;  // tile == 0, j == 0: never read
-            s_row[j] = (tile + j >= 1 && p < u) ? min((uint64_t)srows[p], n_rows) : n_rows;
+            v[k] = (j <= OFF_TILE && tile + j >= 1 && p < u) ? srows[p] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k <= OFF_E; ++k) {
+            const int j = threadIdx.x + k * OFF_T;
+            if (j <= OFF_TILE) s_row[j] = v[k];
         }
         __syncthreads();
+        const int lim = (int)min((uint64_t)OFF_TILE, u + 1 - tile);  // positions tile .. u of this tile
 #pragma unroll
         for (int k = 0; k < OFF_E; ++k) {
             const int j = threadIdx.x + k * OFF_T;
+            if (j >= lim) break;
             const uint64_t i = tile + j;
-            if (i > u) break;
-            const uint64_t cur = s_row[j + 1];
-            const uint64_t lo = i == 0 ? 0 : s_row[j] + 1;  // rows [lo, cur] start at position i
-            if (cur + 1 <= lo) continue;  // inside a row (or a decreasing step: nothing)
-            uint64_t hi = cur + 1;
+            const bool at_end = i == u;
+            // inside a row: same row as the position before (32-bit fast path)
+            if (i != 0 && !at_end && s_row[j + 1] == s_row[j]) continue;
+            const uint64_t cur = at_end ? n_rows : min((uint64_t)s_row[j + 1], n_rows);
+            const uint64_t lo = i == 0 ? 0 : (uint64_t)s_row[j] + 1;  // rows [lo, cur] start at position i
+            if (cur + 1 <= lo) continue;  // a decreasing step (never in sorted input): nothing
+            const uint64_t hi = cur + 1;
             if (hi - lo > GAP_LONG) {
                 const unsigned slot = atomicAdd(n_gaps, 1u);
                 if (slot < GAP_SLOTS) {
@@ -423,25 +437,101 @@ struct Delta {
 
 // First lock (build_csr, csr_build.hpp:32-98): the CSR is the last write of
 // every key with zeros dropped. flag[i] = 1 iff sorted entry i is kept.
-__global__ void first_keep_flags(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx,
-                                 const double *__restrict__ vals, uint64_t m, uint64_t *__restrict__ flag) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        flag[i] = ((i + 1 == m || keys[i] != keys[i + 1]) && !is_zero(vals[idx[i]])) ? 1 : 0;
+// First lock, general path: the sorted entries are compacted in two passes
+// over tiles of KTILE entries, without a per-entry position array. Entry i
+// is kept when it is the last of its key run (the last write) and its value
+// is not +-0. Pass 1 counts the kept entries of every tile; after a scan of
+// the counts, pass 2 recomputes the flags, ranks them inside the tile
+// (entries k * KT + t, k-major: ballots per warp, warp totals in shared
+// memory) and writes row, column and value at tile prefix + rank.
+constexpr int KT = 256, KI = 8, KTILE = KT * KI;
+
+__device__ __forceinline__ unsigned lane_lt_mask() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
 
-__global__ void first_gather(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx,
-                             const uint64_t *__restrict__ pos, uint64_t m, int cbits, const double *__restrict__ vals,
-                             uint32_t *__restrict__ orow, uint32_t *__restrict__ ocol, double *__restrict__ oval) {
+__device__ __forceinline__ void keep_flags_of_tile(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx,
+                                                   const double *__restrict__ vals, uint64_t m, uint64_t base,
+                                                   bool (&f)[KI], uint64_t (&key)[KI], double (&val)[KI]) {
+    uint32_t ix[KI];
+    uint64_t nxt[KI];
+#pragma unroll
+    for (int k = 0; k < KI; ++k) {  // loads of all items first
+        const uint64_t i = base + (uint64_t)k * KT + threadIdx.x;
+        key[k] = i < m ? keys[i] : 0;
+        nxt[k] = i + 1 < m ? keys[i + 1] : ~0ull;
+        ix[k] = i < m ? idx[i] : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < KI; ++k) {
+        const uint64_t i = base + (uint64_t)k * KT + threadIdx.x;
+        const bool last = i < m && (i + 1 == m || key[k] != nxt[k]);
+        val[k] = last ? vals[ix[k]] : 0.0;
+        f[k] = last && !is_zero(val[k]);
+    }
+}
+
+__global__ void __launch_bounds__(KT)
+first_keep_count(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx, const double *__restrict__ vals,
+                 uint64_t m, uint64_t *__restrict__ tile_counts) {
+    bool f[KI];
+    uint64_t key[KI];
+    double val[KI];
+    keep_flags_of_tile(keys, idx, vals, m, blockIdx.x * (uint64_t)KTILE, f, key, val);
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < KI; ++k) c += f[k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    __shared__ unsigned s_c[KT / 32];
+    if ((threadIdx.x & 31) == 0) s_c[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < KT / 32; ++w) t += s_c[w];
+        tile_counts[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(KT)
+first_keep_gather(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ idx, const double *__restrict__ vals,
+                  uint64_t m, int cbits, const uint64_t *__restrict__ tile_prefix, uint32_t *__restrict__ orow,
+                  uint32_t *__restrict__ ocol, double *__restrict__ oval) {
+    bool f[KI];
+    uint64_t key[KI];
+    double val[KI];
+    keep_flags_of_tile(keys, idx, vals, m, blockIdx.x * (uint64_t)KTILE, f, key, val);
+    __shared__ unsigned s_w[KI][KT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned rank[KI];
+#pragma unroll
+    for (int k = 0; k < KI; ++k) {
+        const unsigned b = __ballot_sync(0xffffffffu, f[k]);
+        rank[k] = __popc(b & lane_lt_mask());
+        if (lane == 0) s_w[k][warp] = __popc(b);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // exclusive prefix over (k, warp): the tile's entry order
+        unsigned run = 0;
+        for (int k = 0; k < KI; ++k)
+            for (int w = 0; w < KT / 32; ++w) {
+                const unsigned v = s_w[k][w];
+                s_w[k][w] = run;
+                run += v;
+            }
+    }
+    __syncthreads();
+    const uint64_t base = tile_prefix[blockIdx.x];
     const uint64_t cmask = cbits ? ((1ull << cbits) - 1) : 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t j = pos[i];
-        if (pos[i + 1] == j) continue;
-        const uint64_t k = keys[i];
-        orow[j] = (uint32_t)(k >> cbits);
-        ocol[j] = (uint32_t)(k & cmask);
-        oval[j] = vals[idx[i]];
+#pragma unroll
+    for (int k = 0; k < KI; ++k) {
+        if (!f[k]) continue;
+        const uint64_t j = base + s_w[k][warp] + rank[k];
+        orow[j] = (uint32_t)(key[k] >> cbits);
+        ocol[j] = (uint32_t)(key[k] & cmask);
+        oval[j] = val[k];
     }
 }
 
@@ -580,17 +670,20 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
     if (m) {
         const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
         SPG_TRY(sort_keys(c, rows, cols, m, n, A->n_cols, keys, idx, pre, s));
-        SPG_TRY(pos.alloc((m + 1) * sizeof(uint64_t), s));
-        first_keep_flags<<<g, LB, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), vals, m, pos.as<uint64_t>());
+        const uint64_t tiles = (m + KTILE - 1) / KTILE;
+        SPG_TRY(pos.alloc((tiles + 1) * sizeof(uint64_t), s));  // kept entries per tile, then their prefix
+        first_keep_count<<<(unsigned)tiles, KT, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), vals, m,
+                                                        pos.as<uint64_t>());
         SPG_LAUNCH_CHECK();
-        SPG_TRY(exclusive_scan_u64(c, pos.as<uint64_t>(), m, pos.as<uint64_t>() + m, s));
-        SPG_CUDA_TRY(cudaMemcpyAsync(&nnz, pos.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+        SPG_TRY(exclusive_scan_u64(c, pos.as<uint64_t>(), tiles, pos.as<uint64_t>() + tiles, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(&nnz, pos.as<uint64_t>() + tiles, 8, cudaMemcpyDeviceToHost, s));
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
         SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
         SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
         SPG_TRY(orow.alloc((nnz ? nnz : 1) * sizeof(uint32_t), s));
-        first_gather<<<g, LB, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), pos.as<uint64_t>(), m, cbits, vals,
-                                      orow.as<uint32_t>(), out_cols.as<uint32_t>(), out_vals.as<double>());
+        first_keep_gather<<<(unsigned)tiles, KT, 0, s>>>(keys.as<uint64_t>(), idx.as<uint32_t>(), vals, m, cbits,
+                                                         pos.as<uint64_t>(), orow.as<uint32_t>(),
+                                                         out_cols.as<uint32_t>(), out_vals.as<double>());
         SPG_LAUNCH_CHECK();
     } else {
         SPG_TRY(out_cols.alloc(csr_alloc_elems(0) * sizeof(uint32_t), s));
