@@ -195,16 +195,149 @@ __global__ void compact_entries(const uint32_t *__restrict__ cols, const double 
     }
 }
 
-// Row sums in CSR order (one thread per row: the sum is one left-to-right
-// chain, as the CPU loop adds it).
-__global__ void row_sums_kernel(const uint64_t *__restrict__ off, const double *__restrict__ vals, uint64_t n_rows,
-                                double *__restrict__ out) {
+// Row sums in CSR order: each sum is one left-to-right chain of __dadd_rn,
+// as the CPU loop adds it, so a row is never split and a lane owns a row.
+// A warp FP64 instruction costs the FP64 pipe the same whether one lane or
+// 32 are active, so lanes must carry rows of similar length: rows of at most
+// RS_SHORT entries are summed where they lie (thread per row), longer rows
+// are bucketed by length (bucket b holds lengths in (32 << b, 64 << b]) and
+// summed bucket by bucket, a lane per row, each loading RS_BATCH values
+// ahead of its adds.
+constexpr int RS_SHORT = 32, RS_BUCKETS = 10, RS_BATCH = 8;
+
+__device__ __forceinline__ int rs_bucket(uint64_t len) {  // len > RS_SHORT
+    const int b = 63 - __clzll((long long)(len - 1)) - 5;  // (32, 64] -> 0, (64, 128] -> 1, ...
+    return b < RS_BUCKETS - 1 ? b : RS_BUCKETS - 1;
+}
+
+__device__ __forceinline__ double row_chain(const double *__restrict__ vals, uint64_t k, uint64_t e) {
+    double acc = 0.0;
+    for (; k + RS_BATCH <= e; k += RS_BATCH) {
+        double v[RS_BATCH];
+#pragma unroll
+        for (int j = 0; j < RS_BATCH; ++j) v[j] = vals[k + j];
+#pragma unroll
+        for (int j = 0; j < RS_BATCH; ++j) acc = __dadd_rn(acc, v[j]);
+    }
+    for (; k < e; ++k) acc = __dadd_rn(acc, vals[k]);
+    return acc;
+}
+
+// The same chain for long rows, software-pipelined: four batches of
+// RS_BATCH values are in flight while one is added, so a lane's chain runs
+// at the FP64 latency instead of waiting on memory every batch.
+__device__ __forceinline__ void rs_load(double (&r)[RS_BATCH], const double *__restrict__ vals, uint64_t p,
+                                        uint64_t e) {
+#pragma unroll
+    for (int j = 0; j < RS_BATCH; ++j) r[j] = p + j < e ? vals[p + j] : 0.0;
+}
+
+__device__ __forceinline__ void rs_add(double &acc, const double (&r)[RS_BATCH], uint64_t p, uint64_t e) {
+#pragma unroll
+    for (int j = 0; j < RS_BATCH; ++j)
+        if (p + j < e) acc = __dadd_rn(acc, r[j]);
+}
+
+__device__ __forceinline__ double row_chain_long(const double *__restrict__ vals, uint64_t k, uint64_t e) {
+    constexpr uint64_t B = RS_BATCH;
+    double acc = 0.0, r0[RS_BATCH], r1[RS_BATCH], r2[RS_BATCH], r3[RS_BATCH];
+    rs_load(r0, vals, k, e);
+    rs_load(r1, vals, k + B, e);
+    rs_load(r2, vals, k + 2 * B, e);
+    rs_load(r3, vals, k + 3 * B, e);
+    for (; k < e; k += 4 * B) {
+        rs_add(acc, r0, k, e);
+        rs_load(r0, vals, k + 4 * B, e);
+        rs_add(acc, r1, k + B, e);
+        rs_load(r1, vals, k + 5 * B, e);
+        rs_add(acc, r2, k + 2 * B, e);
+        rs_load(r2, vals, k + 6 * B, e);
+        rs_add(acc, r3, k + 3 * B, e);
+        rs_load(r3, vals, k + 7 * B, e);
+    }
+    return acc;
+}
+
+// Pass 1: short rows summed; long rows counted per bucket (fill == false)
+// or placed in their bucket's list (fill == true; cursor[b] starts at the
+// bucket's first slot).
+template <bool FILL>
+__global__ void __launch_bounds__(OB)
+row_sums_split(const uint64_t *__restrict__ off, const double *__restrict__ vals, uint64_t n_rows,
+               double *__restrict__ out, unsigned long long *__restrict__ cnt, uint32_t *__restrict__ list) {
+    __shared__ unsigned s_cnt[RS_BUCKETS];
+    if (!FILL) {
+        for (int i = threadIdx.x; i < RS_BUCKETS; i += OB) s_cnt[i] = 0;
+        __syncthreads();
+    }
     for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n_rows;
          r += (uint64_t)gridDim.x * blockDim.x) {
-        double acc = 0.0;
-        for (uint64_t k = off[r], e = off[r + 1]; k < e; ++k) acc = __dadd_rn(acc, vals[k]);
-        out[r] = acc;
+        const uint64_t b = off[r], e = off[r + 1];
+        if (e - b <= RS_SHORT) {
+            if (!FILL) out[r] = row_chain(vals, b, e);
+        } else if (FILL) {
+            list[atomicAdd(&cnt[rs_bucket(e - b)], 1ull)] = (uint32_t)r;
+        } else {
+            atomicAdd(&s_cnt[rs_bucket(e - b)], 1u);
+        }
     }
+    if (!FILL) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < RS_BUCKETS; i += OB)
+            if (s_cnt[i]) atomicAdd(&cnt[i], (unsigned long long)s_cnt[i]);
+    }
+}
+
+// cnt[0..B) counts -> base[]: the buckets laid out longest first, base[b]
+// = first slot of bucket b, base[B] = total; cnt becomes the fill cursors.
+__global__ void row_sums_buckets(unsigned long long *__restrict__ cnt, unsigned long long *__restrict__ base) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        unsigned long long run = 0;
+        for (int i = RS_BUCKETS - 1; i >= 0; --i) {
+            base[i] = run;
+            run += cnt[i];
+            cnt[i] = base[i];
+        }
+        base[RS_BUCKETS] = run;
+    }
+}
+
+// Pass 2: the long rows, longest first, a lane per row. A warp FP64
+// instruction occupies its scheduler's FP64 unit for 64 cycles, so a row's
+// chain advances one value per 64 cycles at best, and only if its warp is
+// the sole FP64 user of that scheduler: the launch is one block of RS_LW
+// warps per SM (a warp per scheduler), and list entry i goes to warp
+// i % W, lane (i / W) % 32, so the heaviest rows land in different warps
+// and each warp's lanes carry rows of falling length.
+constexpr int RS_LW = 4;
+
+__global__ void __launch_bounds__(RS_LW * 32)
+row_sums_long(const uint64_t *__restrict__ off, const double *__restrict__ vals, const uint32_t *__restrict__ list,
+              const unsigned long long *__restrict__ base, double *__restrict__ out) {
+    const uint64_t W = (uint64_t)gridDim.x * RS_LW;
+    const uint64_t w = blockIdx.x * (uint64_t)RS_LW + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const uint64_t total = base[RS_BUCKETS];
+    for (uint64_t i = w + W * lane; i < total; i += W * 32) {
+        const uint32_t r = list[i];
+        out[r] = row_chain_long(vals, off[r], off[r + 1]);
+    }
+}
+
+int row_sums_impl(Ctx *c, const uint64_t *off, const double *vals, uint64_t n_rows, uint64_t nnz, double *out,
+                  cudaStream_t s) {
+    const unsigned cap = (unsigned)c->n_sms * 16;
+    const uint64_t max_long = nnz / (RS_SHORT + 1) + 1;
+    DevBuf meta, list;
+    SPG_TRY(meta.alloc((2 * RS_BUCKETS + 1) * sizeof(unsigned long long), s));
+    SPG_TRY(list.alloc(max_long * sizeof(uint32_t), s));
+    unsigned long long *cnt = meta.as<unsigned long long>(), *base = cnt + RS_BUCKETS;
+    SPG_CUDA_TRY(cudaMemsetAsync(cnt, 0, RS_BUCKETS * sizeof(unsigned long long), s));
+    row_sums_split<false><<<grid_for(n_rows, OB, cap), OB, 0, s>>>(off, vals, n_rows, out, cnt, nullptr);
+    row_sums_buckets<<<1, 32, 0, s>>>(cnt, base);
+    row_sums_split<true><<<grid_for(n_rows, OB, cap), OB, 0, s>>>(off, vals, n_rows, out, cnt, list.as<uint32_t>());
+    row_sums_long<<<(unsigned)c->n_sms, RS_LW * 32, 0, s>>>(off, vals, list.as<uint32_t>(), base, out);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
 }
 
 // Point lookups: found[i] = 1 and vals_out[i] = A(r, c) when stored; queries
@@ -434,10 +567,7 @@ int spg_csr_row_sums(spg_ctx *c, const spg_csr *A, double *d_out, void *stream) 
     if (!A->built) return set_error(SPG_ERR_LOGIC, "spg_csr_row_sums: matrix must be locked");
     if (!A->n_rows) return SPG_OK;
     SPG_CUDA_TRY(cudaSetDevice(c->device));
-    row_sums_kernel<<<grid_for(A->n_rows, OB, (unsigned)c->n_sms * 16), OB, 0, pick_stream(c, stream)>>>(
-        A->d_off(), A->d_vals(), A->n_rows, d_out);
-    SPG_LAUNCH_CHECK();
-    return SPG_OK;
+    return row_sums_impl(c, A->d_off(), A->d_vals(), A->n_rows, A->nnz, d_out, pick_stream(c, stream));
 }
 
 int spg_csr_row_sums_host(spg_ctx *c, const spg_csr *A, uint64_t row0, uint64_t n, double *out) {
@@ -451,9 +581,7 @@ int spg_csr_row_sums_host(spg_ctx *c, const spg_csr *A, uint64_t row0, uint64_t 
     cudaStream_t s = c->stream;
     DevBuf d;
     SPG_TRY(d.alloc(n * sizeof(double), s));
-    row_sums_kernel<<<grid_for(n, OB, (unsigned)c->n_sms * 16), OB, 0, s>>>(A->d_off() + row0, A->d_vals(), n,
-                                                                             d.as<double>());
-    SPG_LAUNCH_CHECK();
+    SPG_TRY(row_sums_impl(c, A->d_off() + row0, A->d_vals(), n, A->nnz, d.as<double>(), s));
     SPG_CUDA_TRY(cudaMemcpyAsync(out, d.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
     return SPG_OK;
