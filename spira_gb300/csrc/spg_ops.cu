@@ -132,22 +132,45 @@ __global__ void add_offsets(const uint64_t *__restrict__ aoff, const uint64_t *_
 }
 
 // Writes X's kept entries into C. sx = X's scanned keep flags (nx + 1
-// entries), sy = Y's; X = A sums on a collision.
+// entries), sy = Y's; X = A sums on a collision. A thread handles SI entries
+// per step with their loads issued together.
 template <bool X_IS_A>
-__global__ void add_scatter(const uint32_t *__restrict__ xcols, const double *__restrict__ xvals, uint64_t nx,
-                            const double *__restrict__ yvals, const uint64_t *__restrict__ sx,
-                            const uint64_t *__restrict__ sy, const uint64_t *__restrict__ partner,
-                            uint32_t *__restrict__ ccols, double *__restrict__ cvals) {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nx; e += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t s0 = sx[e];
-        if (sx[e + 1] == s0) continue;  // dropped
-        const uint64_t pp = partner[e];
-        const uint64_t p = pp & ~COLLIDE;
-        const uint64_t pos = s0 + sy[p];
-        double v = xvals[e];
-        if (X_IS_A && (pp & COLLIDE)) v = __dadd_rn(v, yvals[p]);
-        ccols[pos] = xcols[e];
-        cvals[pos] = v;
+__global__ void __launch_bounds__(OB)
+add_scatter(const uint32_t *__restrict__ xcols, const double *__restrict__ xvals, uint64_t nx,
+            const double *__restrict__ yvals, const uint64_t *__restrict__ sx, const uint64_t *__restrict__ sy,
+            const uint64_t *__restrict__ partner, uint32_t *__restrict__ ccols, double *__restrict__ cvals) {
+    constexpr int SI = 4;
+    for (uint64_t e0 = blockIdx.x * (uint64_t)(OB * SI); e0 < nx; e0 += (uint64_t)gridDim.x * OB * SI) {
+        uint64_t s0[SI], s1[SI], pp[SI];
+#pragma unroll
+        for (int q = 0; q < SI; ++q) {
+            const uint64_t e = e0 + threadIdx.x + (uint64_t)q * OB;
+            s0[q] = e < nx ? sx[e] : 0;
+            s1[q] = e < nx ? sx[e + 1] : 0;
+            pp[q] = e < nx ? partner[e] : 0;
+        }
+        uint64_t pos[SI];
+        double v[SI], yv[SI];
+        uint32_t c[SI];
+#pragma unroll
+        for (int q = 0; q < SI; ++q) {
+            const uint64_t e = e0 + threadIdx.x + (uint64_t)q * OB;
+            const bool kept = e < nx && s1[q] != s0[q];
+            const uint64_t p = pp[q] & ~COLLIDE;
+            pos[q] = kept ? s0[q] + sy[p] : 0;
+            c[q] = kept ? xcols[e] : 0u;
+            v[q] = kept ? xvals[e] : 0.0;
+            yv[q] = (kept && X_IS_A && (pp[q] & COLLIDE)) ? yvals[p] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < SI; ++q) {
+            const uint64_t e = e0 + threadIdx.x + (uint64_t)q * OB;
+            if (e >= nx || s1[q] == s0[q]) continue;  // dropped
+            double val = v[q];
+            if (X_IS_A && (pp[q] & COLLIDE)) val = __dadd_rn(val, yv[q]);
+            ccols[pos[q]] = c[q];
+            cvals[pos[q]] = val;
+        }
     }
 }
 
@@ -446,11 +469,11 @@ int add_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
     SPG_TRY(cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     if (na)
-        add_scatter<true><<<grid_for(na, OB, cap), OB, 0, s>>>(A->d_cols(), A->d_vals(), na, B->d_vals(),
+        add_scatter<true><<<grid_for(na, OB * 4, cap), OB, 0, s>>>(A->d_cols(), A->d_vals(), na, B->d_vals(),
                                                                ka.as<uint64_t>(), kb.as<uint64_t>(), pa.as<uint64_t>(),
                                                                cols.as<uint32_t>(), vals.as<double>());
     if (nb)
-        add_scatter<false><<<grid_for(nb, OB, cap), OB, 0, s>>>(B->d_cols(), B->d_vals(), nb, A->d_vals(),
+        add_scatter<false><<<grid_for(nb, OB * 4, cap), OB, 0, s>>>(B->d_cols(), B->d_vals(), nb, A->d_vals(),
                                                                 kb.as<uint64_t>(), ka.as<uint64_t>(),
                                                                 pb.as<uint64_t>(), cols.as<uint32_t>(),
                                                                 vals.as<double>());

@@ -91,31 +91,35 @@ __global__ void scan_tile_reduce(const T *__restrict__ d, uint64_t n, T *__restr
 }
 
 // Scan each tile (blocked arrangement: thread t owns items t*ITEMS..), adding
-// the tile's exclusive prefix. Loads go through shared memory to stay coalesced.
+// the tile's exclusive prefix. Loads go through shared memory to stay
+// coalesced; the shared tile is padded by one element every 16 so the
+// blocked reads and writes (thread stride ITEMS) do not pile onto a few banks.
+__device__ __forceinline__ int scan_pad(int j) { return j + (j >> 4); }
+
 template <typename T>
 __global__ void scan_tile_apply(T *__restrict__ d, uint64_t n, const T *__restrict__ tile_prefix,
                                 T *__restrict__ d_total) {
-    __shared__ T tile[SCAN_TILE];
+    __shared__ T tile[SCAN_TILE + SCAN_TILE / 16];
     const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
         int j = i * SCAN_BLOCK + threadIdx.x;
         uint64_t k = base + j;
-        tile[j] = (k < n) ? d[k] : T(0);
+        tile[scan_pad(j)] = (k < n) ? d[k] : T(0);
     }
     __syncthreads();
     T v[SCAN_ITEMS];
     T s = 0;
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-        v[i] = tile[threadIdx.x * SCAN_ITEMS + i];
+        v[i] = tile[scan_pad(threadIdx.x * SCAN_ITEMS + i)];
         s += v[i];
     }
     T total;
     T pre = block_exclusive_scan(s, total) + (tile_prefix ? tile_prefix[blockIdx.x] : T(0));
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-        tile[threadIdx.x * SCAN_ITEMS + i] = pre;
+        tile[scan_pad(threadIdx.x * SCAN_ITEMS + i)] = pre;
         pre += v[i];
     }
     __syncthreads();
@@ -123,7 +127,7 @@ __global__ void scan_tile_apply(T *__restrict__ d, uint64_t n, const T *__restri
     for (int i = 0; i < SCAN_ITEMS; ++i) {
         int j = i * SCAN_BLOCK + threadIdx.x;
         uint64_t k = base + j;
-        if (k < n) d[k] = tile[j];
+        if (k < n) d[k] = tile[scan_pad(j)];
     }
     if (d_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_BLOCK - 1) {
         // last thread of last tile: its running prefix after all items
