@@ -78,6 +78,29 @@ def test_transpose_shapes(ctx, shape):
     assert_csr_equal(T.transpose().download(), H, check_capacity=False)  # double transpose
 
 
+@pytest.mark.parametrize("longest", [16, 32, 33])
+def test_transpose_row_length_tiers(ctx, longest):
+    """Output rows of every length up to `longest`: up to 16 entries are
+    sorted in a thread's registers, 17..32 across a warp, and one longer row
+    sends every row through the per-tile sort."""
+    n_rows, n_cols = 10_000, 700
+    rows, cols = [], []
+    for col in range(n_cols):
+        cnt = col % (longest + 1)
+        pick = np.unique(gen.below(gen.hash3(50 + col, 1, np.arange(4 * cnt + 4, dtype=np.uint64)), n_rows))
+        pick = pick[gen.below(gen.hash3(60 + col, 2, np.arange(len(pick), dtype=np.uint64)), 1 << 30).argsort()]
+        pick = pick[:cnt]
+        rows.append(pick.astype(np.uint32))
+        cols.append(np.full(len(pick), col, np.uint32))
+    r, c = np.concatenate(rows), np.concatenate(cols)
+    v = gen.sym_unit(gen.hash3(70, 3, np.arange(len(r), dtype=np.uint64)))
+    A = locked(ctx, n_rows, n_cols, r, c, v)
+    H = A.download()
+    T = A.transpose()
+    assert max(np.diff(T.download().off)) == longest
+    assert_csr_equal(T.download(), oracle.transpose(H))
+
+
 def test_transpose_zipf_long_rows(ctx):
     r, c, v = gen.zipf_rows(200_000, seed=12)
     A = locked(ctx, 200_000, 200_000, r, c, v)
