@@ -44,6 +44,15 @@ def test_null_arguments_are_status_codes():
     assert L.spg_ctx_create(0, None) == 1
     assert L.spg_csr_info_get(None, None) == 1
     assert L.spg_spmv(None, None, None, None, 0, None) == 1
+    assert L.spg_csr_add(None, None, None, None) == 1
+    assert L.spg_csr_scale(None, None, None, 2.0, 0) == 1
+    assert L.spg_csr_row_sums(None, None, None, None) == 1
+    assert L.spg_csr_lookup(None, None, 0, None, None, None, None, None) == 1
+    assert L.spg_csr_partition(None, None, 4, None) == 1
+    assert L.spg_csr_save(None, None, b"x") == 1
+    assert L.spg_csr_load_file(None, None, b"x") == 1
+    assert L.spg_csr_file_info(None, None, None, None) == 1
+    assert L.spg_strerror(8) == b"domain error"
 
 
 def test_no_gpu_is_an_error_not_a_fallback():
