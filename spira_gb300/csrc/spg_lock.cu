@@ -349,8 +349,21 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
         }
     }
     __syncthreads();
-    // consecutive threads on consecutive entries (coalesced)
-    for (uint64_t k = k0 + threadIdx.x; k < k1; k += LB) {
+    // consecutive threads on consecutive entries (coalesced); a thread's
+    // loads for all its entries are issued before any is used
+    constexpr int MI = MO_CHUNK / LB;
+    uint32_t cs[MI];
+    double vs[MI];
+#pragma unroll
+    for (int q = 0; q < MI; ++q) {
+        const uint64_t k = k0 + threadIdx.x + (uint64_t)q * LB;
+        cs[q] = k < k1 ? cols[k] : 0u;
+        vs[q] = k < k1 ? vals[k] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < MI; ++q) {
+        const uint64_t k = k0 + threadIdx.x + (uint64_t)q * LB;
+        if (k >= k1) break;
         uint64_t p, ds, de, nb;
         if (local) {
             const int lo = s_row[k - k0];
@@ -365,7 +378,7 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
             de = doff[r + 1];
             nb = new_off[r];
         }
-        const uint32_t c = cols[k];
+        const uint32_t c = cs[q];
         uint64_t dst = nb + p;
         if (ds != de) {
             uint64_t lo = ds, hi = de;
@@ -378,7 +391,7 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
             dst += (uint64_t)(P[lo] - P[ds]);
         }
         out_cols[dst] = c;
-        out_vals[dst] = vals[k];
+        out_vals[dst] = vs[q];
     }
 }
 
