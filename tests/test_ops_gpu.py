@@ -193,3 +193,39 @@ def test_partition_matches_oracle(ctx, T):
     E = sg.Csr(ctx, 1000, 1000)
     E.lock(np.array([], np.uint32), np.array([], np.uint32), np.array([]))
     np.testing.assert_array_equal(E.partition(T), oracle.partition(Eh, T))
+
+
+def test_degenerate_shapes(ctx, tmp_path):
+    """Zero rows, zero columns and empty matrices through every operation."""
+    import torch
+    for n_rows, n_cols in ((0, 0), (0, 5), (5, 0), (3, 3)):
+        A = sg.Csr(ctx, n_rows, n_cols)
+        A.lock(np.array([], np.uint32), np.array([], np.uint32), np.array([]))
+        H = A.download()
+        assert_csr_equal(A.add(A).download(), oracle.add(H, H))
+        assert_csr_equal(A.scaled(3.0).download(), oracle.scale(H, 3.0))
+        A.scale_(2.0)
+        assert A.nnz == 0
+        assert len(A.row_sums_host()) == n_rows
+        np.testing.assert_array_equal(A.partition(4), oracle.partition(H, 4))
+        p = tmp_path / f"e{n_rows}x{n_cols}.spgcsr"
+        A.save(p)
+        B = sg.Csr(ctx, 1, 1).load_file(p)
+        assert (B.n_rows, B.n_cols, B.nnz) == (n_rows, n_cols, 0)
+        q = torch.zeros(1, dtype=torch.int64, device="cuda")
+        A.lookup(q[:0], q[:0].to(torch.int32), None, torch.zeros(0, dtype=torch.uint8, device="cuda"))
+
+
+def test_lookup_and_partition_before_the_first_lock(ctx):
+    import torch
+    A = sg.Csr(ctx, 100, 100)
+    d_r = torch.arange(10, dtype=torch.int64, device="cuda")
+    d_c = torch.arange(10, dtype=torch.int32, device="cuda")
+    d_v = torch.full((10,), 7.0, dtype=torch.float64, device="cuda")
+    d_f = torch.ones(10, dtype=torch.uint8, device="cuda")
+    A.lookup(d_r, d_c, d_v, d_f)
+    ctx.sync()
+    assert not d_f.any() and not d_v.any()
+    np.testing.assert_array_equal(A.partition(4), [0, 25, 50, 75, 100])
+    with pytest.raises(sg.LogicError):
+        A.row_sums_host()
