@@ -223,18 +223,33 @@ def run_ours(args):
         d = np.abs(y - y_ref) / np.where(sc > 0, sc, 1.0)
         max_err = max(max_err, float(d.max()))
 
-    # end to end through the C ABI with host (pinned) buffers
+    # end to end through the C ABI with host (pinned) buffers: each step
+    # uploads both x, runs both SpMVs and reads both y back; the two
+    # matrices' calls go out asynchronously on two streams, so one matrix's
+    # transfers overlap the other's (the host link is the bound)
     xs = [torch.from_numpy(m["x"]).pin_memory() for m in mats]
     ys = [torch.empty(m["n_rows"], dtype=torch.float64).pin_memory() for m in mats]
+    e2e_streams = [torch.cuda.Stream() for _ in mats]
     e2e_steps = max(10, min(args.steps, 200))
+
+    # the larger x first: its SpMV waits for all of it (random columns),
+    # while the banded Laplacian's blocks start on the first pieces of theirs
+    order = sorted(range(len(mats)), key=lambda i: -mats[i]["n_cols"])
+
+    def e2e_step():
+        for i in order:
+            mats[i]["A"].spmv_host_async(xs[i].numpy(), ys[i].numpy(), variant=mats[i]["selected"],
+                                         stream=e2e_streams[i].cuda_stream)
+        for st in e2e_streams:
+            st.synchronize()
+
     for _ in range(3):
-        for m, xh, yh in zip(mats, xs, ys):
-            m["A"].spmv_host(xh.numpy(), yh.numpy(), variant=m["selected"])
+        e2e_step()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for m, xh, yh in zip(mats, xs, ys):
-            m["A"].spmv_host(xh.numpy(), yh.numpy(), variant=m["selected"])
+        e2e_step()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    ctx.sync()  # reports a device-side timeout, if any
 
     peak, peak_kind = peaks()
     ops = None if args.no_ops else run_ops(ctx, peak)
@@ -304,7 +319,7 @@ def run_ours(args):
                 "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": int(sum(8 * m["n_cols"] for m in mats)),
                 "d2h_bytes_per_step": int(sum(8 * m["n_rows"] for m in mats)),
-                "path": "spg_spmv_host (C ABI) from pinned host x to pinned host y"},
+                "path": "spg_spmv_host_async (C ABI) from pinned host x to pinned host y, the two matrices on two streams"},
         "gpu_launches": gpu_launches,
         "clocks": clocks,
         "cpu_baseline": cpu,

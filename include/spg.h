@@ -144,6 +144,14 @@ int spg_spmv(spg_ctx *ctx, const spg_csr *A, const double *d_x, double *d_y,
  * SPG_ERR_INVALID_ARGUMENT (serial/spmv.hpp:150-155). */
 int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
                   uint64_t x_len, double *y, uint64_t y_len, int variant);
+/* The same from pinned host x and y (SPG_ERR_INVALID_ARGUMENT otherwise),
+ * enqueued on `stream` and returning at once: the copies and kernels of
+ * different matrices can then overlap (one matrix's upload with another's
+ * SpMV or download). y is complete once `stream` is; spg_ctx_sync reports a
+ * device-side timeout. Calls on the same matrix must be ordered (one stream):
+ * each matrix stages x and y in its own device buffers. */
+int spg_spmv_host_async(spg_ctx *ctx, const spg_csr *A, const double *x, uint64_t x_len, double *y,
+                        uint64_t y_len, int variant, void *stream);
 /* SpMV that allocates no device memory at all. No counterpart in Spira.
  * For callers that cannot call cudaMalloc (or let this library call it):
  * code whose device memory is all owned by another allocator or a fixed

@@ -105,6 +105,7 @@ _SIGS = [
     ("spg_lock_device", _I, [_P, _P, _P, _P, _P, _U64]),
     ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
     ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
+    ("spg_spmv_host_async", _I, [_P, _P, _P, _U64, _P, _U64, _I, _P]),
     ("spg_spmv_noalloc", _I, [_P, _P, _P, _P, _P]),
     ("spg_spmv_noalloc_max", _U64, []),
     ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
@@ -330,6 +331,12 @@ class Csr:
         if y is None:
             y = np.empty(self.n_rows, np.float64)
         _check(lib().spg_spmv_host(self.ctx.h, self.h, _ptr(x), len(x), _ptr(y), len(y), variant))
+        return y
+
+    def spmv_host_async(self, x, y, variant: int = SPMV_AUTO, stream=None):
+        """y = A x from pinned host buffers (numpy views of pinned torch
+        tensors), enqueued on `stream`; y is ready once the stream is."""
+        _check(lib().spg_spmv_host_async(self.ctx.h, self.h, _ptr(x), len(x), _ptr(y), len(y), variant, stream))
         return y
 
     def selected_spmv(self) -> int:

@@ -399,9 +399,12 @@ int spg_spmv(spg_ctx *c, const spg_csr *Ac, const double *d_x, double *d_y, int 
     return spmv_launch(c, A, d_x, d_y, variant, pick_stream(c, stream));
 }
 
-int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,
-                  int variant) {
-    if (!c || !Ac) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: null handle");
+// Host-buffer SpMV; `async` (pinned x and y only) enqueues everything on
+// `ls` and returns without waiting.
+static int spmv_host_impl(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,
+                          int variant, bool async, void *user_stream) {
+    const char *who = async ? "spg_spmv_host_async" : "spg_spmv_host";
+    if (!c || !Ac) return set_error(SPG_ERR_INVALID_ARGUMENT, "%s: null handle", who);
     SPG_CHECK_LIVE(Ac);
     // Checks in the order of serial/spmv.hpp:150-158.
     if (x_len != Ac->n_cols)
@@ -411,17 +414,30 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
         return set_error(SPG_ERR_INVALID_ARGUMENT,
                          "The size of the output vector y does not match the number of rows of the matrix");
     if (!Ac->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
-    if ((x_len && !x) || (y_len && !y)) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: null vector");
+    if ((x_len && !x) || (y_len && !y)) return set_error(SPG_ERR_INVALID_ARGUMENT, "%s: null vector", who);
     spg_csr *A = const_cast<spg_csr *>(Ac);
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
+    const bool pinned = host_pinned(x) && host_pinned(y);
+    if (async && !pinned)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_async: x and y must be pinned host memory");
+    const cudaStream_t ls = async ? pick_stream(c, user_stream) : s;  // where the SpMV is enqueued
     if (variant == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &variant));
     if (variant < 0 || variant >= SPG_SPMV_N_VARIANTS)
-        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host: unknown variant %d", variant);
-    if (c->xbuf.bytes < x_len * sizeof(double)) SPG_TRY(c->xbuf.alloc(x_len * sizeof(double), s));
-    if (c->ybuf.bytes < y_len * sizeof(double)) SPG_TRY(c->ybuf.alloc(y_len * sizeof(double), s));
-    const double *dx = c->xbuf.as<double>();
-    double *dy = c->ybuf.as<double>();
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "%s: unknown variant %d", who, variant);
+    // pinned buffers stage through the matrix's own device vectors (recorded
+    // graphs stay valid across calls, matrices can overlap); pageable ones
+    // through the context's
+    DevBuf &bx = pinned ? A->stage_x : c->xbuf, &by = pinned ? A->stage_y : c->ybuf;
+    if (bx.bytes < x_len * sizeof(double)) SPG_TRY(bx.alloc(x_len * sizeof(double), s));
+    if (by.bytes < y_len * sizeof(double)) SPG_TRY(by.alloc(y_len * sizeof(double), s));
+    if (ls != s) {  // the buffers were (re)allocated in s's order
+        cudaEvent_t ready = c->host_events[Ctx::N_HOST_EVENTS - 3];
+        SPG_CUDA_TRY(cudaEventRecord(ready, s));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(ls, ready, 0));
+    }
+    const double *dx = bx.as<double>();
+    double *dy = by.as<double>();
     // Large matrices: compute y in row blocks and copy each block back on a
     // second stream while the next block computes (the host link, ~200 GB/s,
     // otherwise idles during the SpMV).
@@ -442,9 +458,12 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
     }
     const int nb = rows.empty() ? 0 : (int)rows.size() - 1;
     if (nb < 2) {
-        if (x_len) SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
-        SPG_TRY(spmv_launch(c, A, dx, dy, variant, s));
-        if (y_len) SPG_CUDA_TRY(cudaMemcpyAsync(y, dy, y_len * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (x_len)
+            SPG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(dx), x, x_len * sizeof(double), cudaMemcpyHostToDevice,
+                                         ls));
+        SPG_TRY(spmv_launch(c, A, dx, dy, variant, ls));
+        if (y_len) SPG_CUDA_TRY(cudaMemcpyAsync(y, dy, y_len * sizeof(double), cudaMemcpyDeviceToHost, ls));
+        if (async) return SPG_OK;
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
         return c->take_status();
     }
@@ -465,12 +484,13 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
             for (int j = 0; j < nb; ++j) {
                 const uint64_t c0 = std::min(x_len, xc * j), c1 = std::min(x_len, xc * (j + 1));
                 if (c1 > c0)
-                    SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.as<double>() + c0, x + c0, (c1 - c0) * sizeof(double),
+                    SPG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(dx) + c0, x + c0, (c1 - c0) * sizeof(double),
                                                  cudaMemcpyHostToDevice, c->upload_stream));
                 SPG_CUDA_TRY(cudaEventRecord(c->upload_events[j], c->upload_stream));
             }
         } else if (x_len) {
-            SPG_CUDA_TRY(cudaMemcpyAsync(c->xbuf.ptr, x, x_len * sizeof(double), cudaMemcpyHostToDevice, s));
+            SPG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(dx), x, x_len * sizeof(double), cudaMemcpyHostToDevice,
+                                         s));
         }
         // stage i makes rows [rows[i-1], rows[i]) final (row-parallel: stage i
         // computes block i, so its rows are [rows[i], rows[i+1]))
@@ -509,7 +529,7 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
     // and replayed while the same buffers come back: one launch instead of a
     // few dozen API calls, whose host time otherwise exceeds the transfers of
     // a matrix this size.
-    if (host_pinned(x) && host_pinned(y)) {
+    if (pinned) {
         if (!(A->host_graph && A->host_gx == x && A->host_gy == y && A->host_gvariant == variant &&
               A->host_gdx == dx && A->host_gdy == dy)) {
             A->drop_host_graph();
@@ -532,14 +552,32 @@ int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len
             }
         }
         if (A->host_graph) {
-            SPG_CUDA_TRY(cudaGraphLaunch(A->host_graph, s));
+            SPG_CUDA_TRY(cudaGraphLaunch(A->host_graph, ls));
+            if (async) return SPG_OK;
             SPG_CUDA_TRY(cudaStreamSynchronize(s));
             return c->take_status();
         }
     }
+    // not recorded: the sequence runs on the context's stream (an
+    // asynchronous call then waits for it here)
+    if (ls != s) {
+        cudaEvent_t before = c->host_events[Ctx::N_HOST_EVENTS - 3];
+        SPG_CUDA_TRY(cudaEventRecord(before, ls));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(s, before, 0));
+    }
     SPG_TRY(enqueue());
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
     return c->take_status();
+}
+
+int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,
+                  int variant) {
+    return spmv_host_impl(c, Ac, x, x_len, y, y_len, variant, false, nullptr);
+}
+
+int spg_spmv_host_async(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,
+                        int variant, void *stream) {
+    return spmv_host_impl(c, Ac, x, x_len, y, y_len, variant, true, stream);
 }
 
 int spg_spmv_launches(spg_ctx *c, const spg_csr *Ac, int variant, int *n) {

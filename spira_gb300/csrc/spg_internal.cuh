@@ -165,6 +165,9 @@ struct Csr {
     double *host_gy = nullptr;
     const void *host_gdx = nullptr, *host_gdy = nullptr;
     int host_gvariant = -1;
+    // Device staging of x and y for host-buffer SpMVs from pinned memory (the
+    // matrix's own, so SpMVs of different matrices can be in flight at once).
+    DevBuf stage_x, stage_y;
     void drop_host_graph() {
         if (host_graph) cudaGraphExecDestroy(host_graph);
         host_graph = nullptr;

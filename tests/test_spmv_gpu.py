@@ -156,6 +156,33 @@ def test_host_spmv_pipelined_blocks_match_device_path(ctx):
     np.testing.assert_array_equal(yp.numpy(), yd.cpu().numpy())
 
 
+def test_host_spmv_async_two_matrices_two_streams(ctx):
+    """Asynchronous host-buffer SpMVs of two matrices in flight at once on
+    two streams give the same bits as the synchronous call; unpinned
+    buffers are refused."""
+    import torch
+    mats = []
+    for n, seed in ((700_000, 81), (300_000, 82)):
+        r, c, v = gen.zipf_rows(n, seed=seed) if n == 300_000 else gen.laplacian_2d(837)
+        n = 837 * 837 if n == 700_000 else n
+        A = build(ctx, n, n, [(r, c, v)])
+        x = gen.dense_x(n, seed + 1)
+        mats.append((A, torch.from_numpy(x).pin_memory(), torch.empty(n, dtype=torch.float64).pin_memory(),
+                     A.spmv_host(x)))
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    for rep in range(3):  # record, then replay
+        for (A, xp, yp, want), st in zip(mats, streams):
+            yp.zero_()
+            A.spmv_host_async(xp.numpy(), yp.numpy(), stream=st.cuda_stream)
+        for st in streams:
+            st.synchronize()
+        for A, xp, yp, want in mats:
+            np.testing.assert_array_equal(yp.numpy(), want)
+    A, xp, yp, want = mats[0]
+    with pytest.raises(sg.InvalidArgument):
+        A.spmv_host_async(xp.numpy().copy(), yp.numpy())
+
+
 def test_gather_probe(ctx):
     r = ctx.probe_gather_rate(1 << 20, 1 << 22)
     assert 1e9 < r < 1e13
