@@ -152,6 +152,15 @@ int spg_spmv_host(spg_ctx *ctx, const spg_csr *A, const double *x,
  * each matrix stages x and y in its own device buffers. */
 int spg_spmv_host_async(spg_ctx *ctx, const spg_csr *A, const double *x, uint64_t x_len, double *y,
                         uint64_t y_len, int variant, void *stream);
+/* n (<= 4) distinct matrices' SpMVs from pinned host buffers xs[i] (n_cols
+ * of mats[i]) into ys[i] (n_rows), as one recorded graph enqueued on `stream`
+ * (returns at once; y complete once the stream is). variants may be NULL
+ * (SPG_SPMV_AUTO for all). The uploads are ordered — matrices whose SpMV
+ * reads x anywhere first, largest x first — so that matrix's x does not share
+ * the host link with the others while the rest upload, compute and download
+ * during its SpMV. No Spira counterpart (one spmv call per matrix there). */
+int spg_spmv_host_multi(spg_ctx *ctx, uint32_t n, const spg_csr *const *mats, const double *const *xs,
+                        double *const *ys, const int *variants, void *stream);
 /* SpMV that allocates no device memory at all. No counterpart in Spira.
  * For callers that cannot call cudaMalloc (or let this library call it):
  * code whose device memory is all owned by another allocator or a fixed

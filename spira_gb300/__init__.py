@@ -106,6 +106,7 @@ _SIGS = [
     ("spg_spmv", _I, [_P, _P, _P, _P, _I, _P]),
     ("spg_spmv_host", _I, [_P, _P, _P, _U64, _P, _U64, _I]),
     ("spg_spmv_host_async", _I, [_P, _P, _P, _U64, _P, _U64, _I, _P]),
+    ("spg_spmv_host_multi", _I, [_P, _U32, _P, _P, _P, _P, _P]),
     ("spg_spmv_noalloc", _I, [_P, _P, _P, _P, _P]),
     ("spg_spmv_noalloc_max", _U64, []),
     ("spg_spmv_selected", _I, [_P, _P, C.POINTER(_I)]),
@@ -433,6 +434,17 @@ class Csr:
 
 # ---------------------------------------------------------------- device draws
 GEN_BELOW_U32, GEN_SYM_F64, GEN_UNIT_F64 = 0, 1, 2
+
+
+def spmv_host_multi(ctx: Context, mats, xs, ys, variants=None, stream=None):
+    """SpMVs of several matrices from pinned host buffers (numpy views of
+    pinned torch tensors) in one call, enqueued on `stream`."""
+    n = len(mats)
+    hm = (C.c_void_p * n)(*[A.h for A in mats])
+    hx = (C.c_void_p * n)(*[_ptr(x) for x in xs])
+    hy = (C.c_void_p * n)(*[_ptr(y) for y in ys])
+    hv = (C.c_int * n)(*variants) if variants is not None else None
+    _check(lib().spg_spmv_host_multi(ctx.h, n, hm, hx, hy, hv, stream))
 
 
 def csr_file_info(path):

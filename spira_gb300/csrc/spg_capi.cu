@@ -171,6 +171,13 @@ int spg_ctx_destroy(spg_ctx *c) {
         if (c->host_events[i]) cudaEventDestroy(c->host_events[i]);
         if (c->upload_events[i]) cudaEventDestroy(c->upload_events[i]);
     }
+    c->drop_multi();
+    for (int l = 0; l < Ctx::MULTI_MAX; ++l) {
+        for (cudaStream_t &st : c->multi_stream[l])
+            if (st) cudaStreamSynchronize(st), cudaStreamDestroy(st);
+        for (cudaEvent_t &ev : c->multi_event[l])
+            if (ev) cudaEventDestroy(ev);
+    }
     cudaStreamDestroy(c->upload_stream);
     cudaStreamDestroy(c->copy_stream);
     cudaStreamDestroy(c->stream);
@@ -568,6 +575,188 @@ static int spmv_host_impl(spg_ctx *c, const spg_csr *Ac, const double *x, uint64
     SPG_TRY(enqueue());
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
     return c->take_status();
+}
+
+// Several matrices' host-buffer SpMVs as one recorded graph. Each matrix
+// gets a lane (compute, upload and download streams). The uploads are
+// chained in priority order — matrices whose SpMV reads x anywhere (so waits
+// for all of it), largest x first, then the row-parallel ones, whose blocks
+// start on the first pieces of theirs — so the first matrix's x is not slowed
+// by the others sharing the host link, and the other matrices' transfers and
+// kernels proceed while it computes.
+struct MultiPlan {
+    spg_csr *A;
+    const double *x;
+    double *y;
+    const double *dx;
+    double *dy;
+    int variant;
+    bool row_parallel;
+    std::vector<uint64_t> rows;  // row blocks (nb + 1 bounds), empty: one block
+    uint64_t xc;                 // columns per x piece (row-parallel)
+};
+
+static int multi_lane_resources(Ctx *c, int n) {
+    for (int l = 0; l < n; ++l) {
+        for (cudaStream_t &st : c->multi_stream[l])
+            if (!st) SPG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (cudaEvent_t &ev : c->multi_event[l])
+            if (!ev) SPG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    return SPG_OK;
+}
+
+static int multi_enqueue(Ctx *c, std::vector<MultiPlan> &P, const std::vector<int> &order, cudaStream_t s) {
+    constexpr int NE = Ctx::N_HOST_EVENTS;
+    cudaEvent_t fork = c->host_events[NE - 1];
+    SPG_CUDA_TRY(cudaEventRecord(fork, s));
+    cudaEvent_t gate = nullptr;  // the previous lane's last upload
+    for (int l = 0; l < (int)order.size(); ++l) {
+        MultiPlan &p = P[order[l]];
+        cudaStream_t comp = c->multi_stream[l][0], up = c->multi_stream[l][1], copy = c->multi_stream[l][2];
+        cudaEvent_t *ev = c->multi_event[l];  // [0, NE): block done; [NE, 2 NE): x piece up
+        const uint64_t x_len = p.A->n_cols, y_len = p.A->n_rows;
+        for (cudaStream_t st : {comp, up, copy}) SPG_CUDA_TRY(cudaStreamWaitEvent(st, fork, 0));
+        if (gate) SPG_CUDA_TRY(cudaStreamWaitEvent(up, gate, 0));
+        const int nb = p.rows.empty() ? 1 : (int)p.rows.size() - 1;
+        const int pieces = p.row_parallel && nb > 1 ? nb : 1;
+        for (int j = 0; j < pieces; ++j) {
+            const uint64_t c0 = pieces == 1 ? 0 : std::min(x_len, p.xc * j);
+            const uint64_t c1 = pieces == 1 ? x_len : std::min(x_len, p.xc * (j + 1));
+            if (c1 > c0)
+                SPG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(p.dx) + c0, p.x + c0, (c1 - c0) * sizeof(double),
+                                             cudaMemcpyHostToDevice, up));
+            SPG_CUDA_TRY(cudaEventRecord(ev[NE + j], up));
+        }
+        gate = ev[NE + pieces - 1];
+        if (p.rows.empty()) {  // one block: whole x, one launch, whole y
+            SPG_CUDA_TRY(cudaStreamWaitEvent(comp, gate, 0));
+            SPG_TRY(spmv_launch(c, p.A, p.dx, p.dy, p.variant, comp));
+            SPG_CUDA_TRY(cudaEventRecord(ev[0], comp));
+            SPG_CUDA_TRY(cudaStreamWaitEvent(copy, ev[0], 0));
+            if (y_len) SPG_CUDA_TRY(cudaMemcpyAsync(p.y, p.dy, y_len * sizeof(double), cudaMemcpyDeviceToHost, copy));
+        } else {
+            const int stages = p.row_parallel ? nb : nb + 1;
+            if (!p.row_parallel) SPG_CUDA_TRY(cudaStreamWaitEvent(comp, gate, 0));
+            for (int i = 0; i < stages; ++i) {
+                uint64_t r0, r1;
+                if (p.row_parallel) {
+                    r0 = p.rows[i];
+                    r1 = p.rows[i + 1];
+                    if (x_len) {
+                        const int64_t reach = p.A->host_reach[i];
+                        const int piece = reach < 0 ? 0 : (int)std::min<uint64_t>(nb - 1, (uint64_t)reach / p.xc);
+                        SPG_CUDA_TRY(cudaStreamWaitEvent(comp, ev[NE + piece], 0));
+                    }
+                    SPG_TRY(spmv_launch_rows(c, p.A, p.dx, p.dy, p.variant, r0, r1, comp));
+                } else {
+                    SPG_TRY(spmv_adaptive_stage(c, p.A, p.dx, p.dy, p.variant, i, comp));
+                    if (i == 0) continue;
+                    r0 = p.rows[i - 1];
+                    r1 = p.rows[i];
+                }
+                if (r1 <= r0) continue;
+                SPG_CUDA_TRY(cudaEventRecord(ev[i], comp));
+                SPG_CUDA_TRY(cudaStreamWaitEvent(copy, ev[i], 0));
+                SPG_CUDA_TRY(cudaMemcpyAsync(p.y + r0, p.dy + r0, (r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                             copy));
+            }
+        }
+        // join the lane back to s
+        for (cudaStream_t st : {comp, up, copy}) {
+            SPG_CUDA_TRY(cudaEventRecord(ev[NE - 1], st));
+            SPG_CUDA_TRY(cudaStreamWaitEvent(s, ev[NE - 1], 0));
+        }
+    }
+    return SPG_OK;
+}
+
+int spg_spmv_host_multi(spg_ctx *c, uint32_t n, const spg_csr *const *mats, const double *const *xs,
+                        double *const *ys, const int *variants, void *stream) {
+    if (!c || (n && (!mats || !xs || !ys))) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: null argument");
+    if (n > (uint32_t)Ctx::MULTI_MAX)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: at most %d matrices", Ctx::MULTI_MAX);
+    if (!n) return SPG_OK;
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    std::vector<MultiPlan> P(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        spg_csr *A = const_cast<spg_csr *>(mats[i]);
+        if (!A) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: null matrix %u", i);
+        SPG_CHECK_LIVE(A);
+        if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
+        for (uint32_t j = 0; j < i; ++j)
+            if (mats[j] == mats[i]) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: matrix %u repeated", i);
+        if ((A->n_cols && !xs[i]) || (A->n_rows && !ys[i]) || !host_pinned(xs[i]) || !host_pinned(ys[i]))
+            return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: x and y must be pinned host memory");
+        int v = variants ? variants[i] : SPG_SPMV_AUTO;
+        if (v == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &v));
+        if (v < 0 || v >= SPG_SPMV_N_VARIANTS)
+            return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: unknown variant %d", v);
+        if (A->stage_x.bytes < A->n_cols * sizeof(double)) SPG_TRY(A->stage_x.alloc(A->n_cols * sizeof(double), s));
+        if (A->stage_y.bytes < A->n_rows * sizeof(double)) SPG_TRY(A->stage_y.alloc(A->n_rows * sizeof(double), s));
+        MultiPlan &p = P[i];
+        p.A = A;
+        p.x = xs[i];
+        p.y = ys[i];
+        p.dx = A->stage_x.as<double>();
+        p.dy = A->stage_y.as<double>();
+        p.variant = v;
+        p.row_parallel = v == SPG_SPMV_SCALAR || (v >= SPG_SPMV_VECTOR2 && v <= SPG_SPMV_VECTOR32);
+        const bool adaptive = v == SPG_SPMV_ADAPTIVE || v == SPG_SPMV_ADAPTIVE16 || v == SPG_SPMV_INTERLEAVED;
+        constexpr uint64_t PIPELINE_MIN_NNZ = 4u << 20;
+        constexpr int NB = 4;
+        if (A->nnz >= PIPELINE_MIN_NNZ && A->n_rows && (p.row_parallel || adaptive)) {
+            if (p.row_parallel) {
+                p.rows.resize(NB + 1);
+                for (int b = 0; b <= NB; ++b) p.rows[b] = A->n_rows * (uint64_t)b / NB;
+            } else {
+                SPG_TRY(spmv_adaptive_blocks(c, A, v, NB, &p.rows, s));
+            }
+            if (p.rows.size() < 3) p.rows.clear();
+        }
+        const int nb = p.rows.empty() ? 1 : (int)p.rows.size() - 1;
+        p.xc = (A->n_cols + nb - 1) / (uint64_t)nb;
+        if (p.row_parallel && nb > 1 && A->n_cols) SPG_TRY(spmv_row_block_reach(c, A, nb, s));
+    }
+    // priority: matrices that wait for all of x (largest x first), then the row-parallel ones
+    std::vector<int> order(n);
+    for (uint32_t i = 0; i < n; ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const bool wa = !(P[a].row_parallel && !P[a].rows.empty()), wb = !(P[b].row_parallel && !P[b].rows.empty());
+        if (wa != wb) return wa;
+        return P[a].A->n_cols > P[b].A->n_cols;
+    });
+    std::vector<uintptr_t> key;
+    for (int i : order) {
+        const MultiPlan &p = P[i];
+        for (uintptr_t k : {(uintptr_t)p.A, (uintptr_t)p.A->epoch, (uintptr_t)p.x, (uintptr_t)p.y,
+                            (uintptr_t)p.dx, (uintptr_t)p.dy, (uintptr_t)p.variant})
+            key.push_back(k);
+    }
+    if (!(c->multi_graph && c->multi_key == key)) {
+        c->drop_multi();
+        SPG_TRY(multi_lane_resources(c, (int)n));
+        cudaGraph_t g = nullptr;
+        SPG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = multi_enqueue(c, P, order, s);
+        cudaError_t ec = cudaStreamEndCapture(s, &g);
+        cudaGraphExec_t ex = nullptr;
+        if (rc == SPG_OK && ec == cudaSuccess) ec = cudaGraphInstantiate(&ex, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (rc != SPG_OK) return rc;
+        if (ec != cudaSuccess) return set_error(SPG_ERR_CUDA, "spg_spmv_host_multi: graph: %s", cudaGetErrorString(ec));
+        c->multi_graph = ex;
+        c->multi_key = key;
+    }
+    const cudaStream_t ls = pick_stream(c, stream);
+    if (ls != s) {  // staging was (re)allocated in s's order
+        cudaEvent_t ready = c->host_events[Ctx::N_HOST_EVENTS - 3];
+        SPG_CUDA_TRY(cudaEventRecord(ready, s));
+        SPG_CUDA_TRY(cudaStreamWaitEvent(ls, ready, 0));
+    }
+    SPG_CUDA_TRY(cudaGraphLaunch(c->multi_graph, ls));
+    return SPG_OK;
 }
 
 int spg_spmv_host(spg_ctx *c, const spg_csr *Ac, const double *x, uint64_t x_len, double *y, uint64_t y_len,

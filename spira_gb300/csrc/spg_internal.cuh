@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <string>
 #include <utility>
+#include <atomic>
 #include <vector>
 
 #include "../../include/spg.h"
@@ -131,6 +132,19 @@ struct Ctx {
     static constexpr int N_HOST_EVENTS = 8;
     cudaEvent_t host_events[N_HOST_EVENTS] = {};
     cudaEvent_t upload_events[N_HOST_EVENTS] = {};
+    // Host SpMVs of several matrices in one call (spg_host_multi.cu): per
+    // matrix lane a compute, an upload and a download stream and events,
+    // created at first use; the recorded graph and what it was recorded for.
+    static constexpr int MULTI_MAX = 4;
+    cudaStream_t multi_stream[MULTI_MAX][3] = {};
+    cudaEvent_t multi_event[MULTI_MAX][2 * N_HOST_EVENTS] = {};
+    cudaGraphExec_t multi_graph = nullptr;
+    std::vector<uintptr_t> multi_key;
+    void drop_multi() {
+        if (multi_graph) cudaGraphExecDestroy(multi_graph);
+        multi_graph = nullptr;
+        multi_key.clear();
+    }
     // SpMV variant choice: policy and the loaded selector (spg_tune.cu).
     int spmv_policy = SPG_POLICY_SELECTOR;
     DevBuf model;  // FP32 selector blob
@@ -177,7 +191,15 @@ struct Csr {
         host_gvariant = -1;
     }
     ~Csr() { drop_host_graph(); }
+    // Renewed whenever the CSR changes, unique across all matrices of the
+    // process (keys graphs recorded over the matrix).
+    uint64_t epoch = 0;
+    static uint64_t next_epoch() {
+        static std::atomic<uint64_t> counter{0};
+        return ++counter;
+    }
     void invalidate_derived() {
+        epoch = next_epoch();
         stats_valid = false;
         selected_spmv = -1;
         plan_stream = SpmvPlan{};

@@ -183,6 +183,49 @@ def test_host_spmv_async_two_matrices_two_streams(ctx):
         A.spmv_host_async(xp.numpy().copy(), yp.numpy())
 
 
+def test_host_spmv_multi(ctx):
+    """Several matrices' host-buffer SpMVs in one call (one recorded graph):
+    the same bits as one call each, re-recorded after a re-lock; unpinned
+    buffers, repeated matrices and more than four are refused."""
+    import torch
+    mats, xs, ys, want = [], [], [], []
+    specs = [("zipf", 300_000, 91), ("lap", 837, 92), ("rand", 50_000, 93)]
+    for kind, n, seed in specs:
+        if kind == "zipf":
+            r, c, v = gen.zipf_rows(n, seed=seed)
+        elif kind == "lap":
+            r, c, v = gen.laplacian_2d(n)
+            n = n * n
+        else:
+            r, c, v = gen.random_rows(n, n, 12, seed=seed)
+        A = build(ctx, n, n, [(r, c, v)])
+        x = gen.dense_x(n, seed + 1)
+        mats.append(A)
+        xs.append(torch.from_numpy(x).pin_memory())
+        ys.append(torch.empty(n, dtype=torch.float64).pin_memory())
+        want.append(A.spmv_host(x))
+    st = torch.cuda.Stream()
+    for rep in range(3):
+        for y in ys:
+            y.zero_()
+        sg.spmv_host_multi(ctx, mats, [x.numpy() for x in xs], [y.numpy() for y in ys], stream=st.cuda_stream)
+        st.synchronize()
+        for y, w in zip(ys, want):
+            np.testing.assert_array_equal(y.numpy(), w)
+    mats[1].lock(np.array([3], np.uint32), np.array([4], np.uint32), np.array([2.0]))
+    want[1] = mats[1].spmv_host(xs[1].numpy().copy())
+    sg.spmv_host_multi(ctx, mats, [x.numpy() for x in xs], [y.numpy() for y in ys])
+    ctx.sync()
+    for y, w in zip(ys, want):
+        np.testing.assert_array_equal(y.numpy(), w)
+    with pytest.raises(sg.InvalidArgument):
+        sg.spmv_host_multi(ctx, mats[:1], [xs[0].numpy().copy()], [ys[0].numpy()])
+    with pytest.raises(sg.InvalidArgument):
+        sg.spmv_host_multi(ctx, [mats[0], mats[0]], [xs[0].numpy()] * 2, [ys[0].numpy()] * 2)
+    with pytest.raises(sg.InvalidArgument):
+        sg.spmv_host_multi(ctx, mats * 2, [x.numpy() for x in xs] * 2, [y.numpy() for y in ys] * 2)
+
+
 def test_gather_probe(ctx):
     r = ctx.probe_gather_rate(1 << 20, 1 << 22)
     assert 1e9 < r < 1e13
