@@ -1,5 +1,5 @@
 """SpMV on the GPU, every variant, against the oracle and Spira's golden
-outputs. FP64 tolerance (written here, from the benchmark spec's bound): per row
+outputs. FP64 tolerance (written here, the project's stated FP64 bound): per row
 |y - y_ref| <= 1e-12 * sum_k |a_rk x_k|; the compensated oracle gives y_ref
 to ~2 ulp, and Spira's own SIMD path is held to the same bound."""
 from __future__ import annotations
