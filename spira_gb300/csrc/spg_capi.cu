@@ -450,7 +450,8 @@ static int spmv_host_impl(spg_ctx *c, const spg_csr *Ac, const double *x, uint64
     // otherwise idles during the SpMV).
     constexpr uint64_t PIPELINE_MIN_NNZ = 4u << 20;
     constexpr int NB = 4;  // the last block's copy and the one-block fix-up look-ahead stay exposed;
-                           // 8 blocks measured slower (per-block launch and tail costs)
+                           // 2 and 8 blocks measured slower (per-block launch and tail costs)
+    static_assert(NB + 1 <= Ctx::N_HOST_EVENTS - 3, "a stage event per block, plus fork, join and ready");
     const bool row_parallel = variant == SPG_SPMV_SCALAR || (variant >= SPG_SPMV_VECTOR2 && variant <= SPG_SPMV_VECTOR32);
     const bool adaptive =
         variant == SPG_SPMV_ADAPTIVE || variant == SPG_SPMV_ADAPTIVE16 || variant == SPG_SPMV_INTERLEAVED;
@@ -706,6 +707,7 @@ int spg_spmv_host_multi(spg_ctx *c, uint32_t n, const spg_csr *const *mats, cons
         const bool adaptive = v == SPG_SPMV_ADAPTIVE || v == SPG_SPMV_ADAPTIVE16 || v == SPG_SPMV_INTERLEAVED;
         constexpr uint64_t PIPELINE_MIN_NNZ = 4u << 20;
         constexpr int NB = 4;
+        static_assert(NB + 1 <= Ctx::N_HOST_EVENTS - 1, "a stage event per block, plus the join event");
         if (A->nnz >= PIPELINE_MIN_NNZ && A->n_rows && (p.row_parallel || adaptive)) {
             if (p.row_parallel) {
                 p.rows.resize(NB + 1);
