@@ -218,6 +218,8 @@ struct Csr {
         off.release();
         cols.release();
         vals.release();
+        stage_x.release();  // every device buffer goes while the context's stream exists
+        stage_y.release();
         built = false;
         nnz = capacity = 0;
         ctx = nullptr;
