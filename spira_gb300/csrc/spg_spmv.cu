@@ -41,7 +41,19 @@ spmv_scalar(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
     if (r >= n_rows) return;
     const uint64_t b = off[r], e = off[r + 1];
     double acc = 0.0;
-    for (uint64_t k = b; k < e; ++k) acc = fma(ldx(x, cols[k]), vals[k], acc);
+    uint64_t k = b;
+    // four entries' loads and gathers issued before their FMAs (the chain
+    // itself stays in CSR order)
+    for (; k + 4 <= e; k += 4) {
+        const uint32_t c0 = cols[k], c1 = cols[k + 1], c2 = cols[k + 2], c3 = cols[k + 3];
+        const double v0 = vals[k], v1 = vals[k + 1], v2 = vals[k + 2], v3 = vals[k + 3];
+        const double x0 = ldx(x, c0), x1 = ldx(x, c1), x2 = ldx(x, c2), x3 = ldx(x, c3);
+        acc = fma(x0, v0, acc);
+        acc = fma(x1, v1, acc);
+        acc = fma(x2, v2, acc);
+        acc = fma(x3, v3, acc);
+    }
+    for (; k < e; ++k) acc = fma(ldx(x, cols[k]), vals[k], acc);
     y[r] = acc;
 }
 
