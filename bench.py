@@ -46,6 +46,36 @@ def spmv_bytes(n_rows, n_cols, nnz):
     return 12 * nnz + 8 * (n_rows + 1) + 8 * n_cols + 8 * n_rows
 
 
+class Replicas:
+    """One process per GPU under torchrun: every rank runs the same workload
+    on its own GPU (the path does not shard: replicas only), timed regions are
+    bracketed by barriers and the slowest rank's time is the job's. Scalars
+    travel over gloo; there is no data-path collective."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        if self.world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -123,7 +153,8 @@ def run_ours(args):
 
     import spira_gb300 as sg
 
-    dev = 0
+    rep = Replicas()
+    dev = rep.local
     torch.cuda.set_device(dev)
     ctx = sg.Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -172,13 +203,15 @@ def run_ours(args):
             for _ in range(warmup):
                 step(variant_of)
             torch.cuda.synchronize()
+            rep.barrier()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             for _ in range(steps):
                 step(variant_of)
             e1.record(stream)
             torch.cuda.synchronize()
-            total_ms = float(e0.elapsed_time(e1))
+            rep.barrier()
+            total_ms = rep.max(float(e0.elapsed_time(e1)))
             k = min(steps, 200)
             ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 * len(mats))] for _ in range(k)]
             for s in range(k):
@@ -211,7 +244,7 @@ def run_ours(args):
     ms_auto, per_auto = timed(lambda m: m["autotuned"], max(args.steps // 4, 10), args.warmup)
     ms_b2b = [b2b(m) for m in mats]
     clocks = clk.stop()
-    batched = None if args.no_batched else run_batched(ctx, stream)
+    batched = None if (args.no_batched or rep.rank != 0) else run_batched(ctx, stream)
 
     # parity check of the measured configuration against the compensated oracle
     import oracle
@@ -245,18 +278,20 @@ def run_ours(args):
 
     for _ in range(3):
         e2e_step()
+    rep.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    e2e_ms = rep.max((time.perf_counter() - t0) * 1e3 / e2e_steps)
+    rep.barrier()
     ctx.sync()  # reports a device-side timeout, if any
 
     peak, peak_kind = peaks()
-    ops = None if args.no_ops else run_ops(ctx, peak)
+    ops = None if (args.no_ops or rep.rank != 0) else run_ops(ctx, peak)
     dom = int(np.argmax(per_sel))
     dm = mats[dom]
     achieved = dm["bytes"] / (per_sel[dom] * 1e-3) / 1e9
-    gpu_launches = args.steps * sum(m["A"].spmv_launches(m["selected"]) for m in mats)
+    gpu_launches = rep.world * args.steps * sum(m["A"].spmv_launches(m["selected"]) for m in mats)
     # The second ceiling of a random-column matrix: L2 -> SM transfers. Every x
     # read moves its own 32-byte sector and the 12 B/nnz matrix stream crosses
     # the same path; the probe's random reads (one sector each) measure the rate.
@@ -266,17 +301,20 @@ def run_ours(args):
     cap = NCU_TRAFFIC.get((dm["name"], sg.SPMV_NAMES[dm["selected"]]))
     traffic = round(cap[0] * dm["nnz"] / cap[1]) if cap else None
 
+    if rep.rank != 0:  # the other replicas only contribute their timings
+        return
     cpu = cpu_baseline(host, [m["x"] for m in mats], total_bytes)
+    W = rep.world  # every replica moves the step's bytes
     line = {
         "metric": METRIC,
-        "value": round(total_bytes / (ms_sel * 1e-3) / 1e9, 2),
+        "value": round(W * total_bytes / (ms_sel * 1e-3) / 1e9, 2),
         "unit": "GB/s",
-        "n_gpus": 1,
+        "n_gpus": W,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": round(ms_sel, 5),
         "higher_is_better": True,
-        "scaling": "replicas",
+        "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded generators: 2D Laplacian 1414^2 and Zipf(1.8) 4M rows)",
@@ -293,9 +331,9 @@ def run_ours(args):
             "bytes_per_step": total_bytes,
             "streams": "the two SpMVs of a step on two streams, joined per step",
             "l2": "no flush: each step streams 1.03 GB (> 129 MB L2)"},
-        "plain": {"variant": "scalar (one thread per row)", "value": round(total_bytes / (ms_plain * 1e-3) / 1e9, 2),
+        "plain": {"variant": "scalar (one thread per row)", "value": round(W * total_bytes / (ms_plain * 1e-3) / 1e9, 2),
                   "ms_per_step": round(ms_plain, 5)},
-        "autotuned": {"value": round(total_bytes / (ms_auto * 1e-3) / 1e9, 2), "ms_per_step": round(ms_auto, 5),
+        "autotuned": {"value": round(W * total_bytes / (ms_auto * 1e-3) / 1e9, 2), "ms_per_step": round(ms_auto, 5),
                       "variants": [sg.SPMV_NAMES[m["autotuned"]] for m in mats],
                       "learned_over_autotuned_time": round(ms_sel / ms_auto, 4),
                       "autotune_ms_per_variant": {m["name"]: {sg.SPMV_NAMES[v]: round(float(t), 4)
@@ -315,7 +353,7 @@ def run_ours(args):
                                         "frac_of_ceiling": round(floor_ms / per_sel[dom], 4)}},
         "parity": {"max_err_vs_compensated_oracle": max_err, "tolerance": 1e-12,
                    "bound": "|y-y_ref| <= tol * sum|a x| per row"},
-        "e2e": {"value": round(total_bytes / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
+        "e2e": {"value": round(W * total_bytes / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
                 "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": int(sum(8 * m["n_cols"] for m in mats)),
                 "d2h_bytes_per_step": int(sum(8 * m["n_rows"] for m in mats)),
@@ -650,7 +688,7 @@ def run_reference(args):
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
-        "scaling": "replicas", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "bytes_per_step": total_bytes},
         "cpu_baseline": {"value": v, "unit": "GB/s", "cores": nthr, "kind": kind, "sample": sample},
         "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -843,11 +881,8 @@ def main():
         if rank == 0:
             run_reference(args)
         return
-    if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
-        # replicas only: the path does not shard within one job; each rank would
-        # run an independent replica. This pool runs one GPU per job.
-        if rank != 0:
-            return
+    # N > 1 (torchrun): every rank runs an independent replica on its GPU
+    # (replicas only: the path does not shard), rank 0 prints the job's line
     run_ours(args)
 
 
