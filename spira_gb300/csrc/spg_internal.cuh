@@ -163,7 +163,7 @@ struct Csr {
     DevBuf off;   // uint64_t[n_rows + 1]
     DevBuf cols;  // uint32_t[capacity]
     DevBuf vals;  // double[capacity]
-    // Row-length statistics for the selector (computed lazily).
+    // The longest row, computed lazily by csr_max_row.
     bool stats_valid = false;
     uint64_t max_row = 0;
     int selected_spmv = -1;
@@ -298,7 +298,6 @@ int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const 
 
 // CSR helpers used by several ops (spg_lock.cu).
 int csr_alloc(Csr *A, uint64_t capacity, cudaStream_t s);
-int csr_row_stats(Ctx *c, Csr *A, cudaStream_t s);
 
 // SpMV dispatch (spg_spmv.cu).
 int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant,
@@ -323,6 +322,9 @@ int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, ui
                      cudaStream_t s);
 // A->host_reach for nb equal row blocks (cached until the next lock).
 int spmv_row_block_reach(Ctx *c, Csr *A, int nb, cudaStream_t s);
+// Fills A->max_row (the longest row) once per CSR; `known` false while `s`
+// is being captured (the count needs a synchronisation).
+int csr_max_row(Ctx *c, Csr *A, cudaStream_t s, bool *known);
 // The cached plan slot of one of those variants.
 inline SpmvPlan &adaptive_plan_of(Csr *A, int variant) {
     return variant == SPG_SPMV_INTERLEAVED ? A->plan_inter : A->plan_adaptive;

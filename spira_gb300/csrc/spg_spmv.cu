@@ -37,8 +37,7 @@ __global__ void __launch_bounds__(BLOCK)
 spmv_scalar(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
             const double *__restrict__ vals, const double *__restrict__ x,
             double *__restrict__ y, uint64_t n_rows) {
-    const uint64_t r = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
-    if (r >= n_rows) return;
+  for (uint64_t r = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; r < n_rows; r += (uint64_t)gridDim.x * BLOCK) {
     const uint64_t b = off[r], e = off[r + 1];
     double acc = 0.0;
     uint64_t k = b;
@@ -55,6 +54,7 @@ spmv_scalar(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
     }
     for (; k < e; ++k) acc = fma(ldx(x, cols[k]), vals[k], acc);
     y[r] = acc;
+  }
 }
 
 // Dot over [b, e) by NL cooperating lanes (lane in [0, NL)), lane-strided,
@@ -470,7 +470,68 @@ __global__ void row_block_reach(const uint64_t *__restrict__ off, const uint32_t
 }
 }  // namespace
 
+namespace {
+__global__ void max_row_len(const uint64_t *__restrict__ off, uint64_t n, unsigned long long *__restrict__ mx) {
+    unsigned long long m = 0;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x)
+        m = max(m, (unsigned long long)(off[r + 1] - off[r]));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ unsigned long long s_m[BLOCK / 32];
+    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < BLOCK / 32; ++w) m = max(m, s_m[w]);
+        atomicMax(mx, m);
+    }
+}
+
+// Rows no longer than this count as balanced for SCALAR.
+constexpr uint64_t SCALAR_BALANCED_ROW = 64;
+}  // namespace
+
+// The matrix's longest row, computed once per CSR (needs a synchronisation,
+// so not while `s` is being captured: then `known` stays false).
+int csr_max_row(Ctx *c, Csr *A, cudaStream_t s, bool *known) {
+    *known = A->stats_valid;
+    if (A->stats_valid) return SPG_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SPG_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return SPG_OK;
+    DevBuf mx;
+    SPG_TRY(mx.alloc(sizeof(unsigned long long), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned long long), s));
+    if (A->n_rows) {
+        max_row_len<<<grid_for(A->n_rows, BLOCK, (unsigned)c->n_sms * 8), BLOCK, 0, s>>>(
+            A->d_off(), A->n_rows, mx.as<unsigned long long>());
+        SPG_LAUNCH_CHECK();
+    }
+    unsigned long long h = 0;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&h, mx.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    A->max_row = h;
+    A->stats_valid = true;
+    *known = true;
+    return SPG_OK;
+}
+
+// SCALAR's grid: on matrices whose rows are all short (balanced work per
+// thread) one wave of blocks striding over the rows, which saves the block
+// ramp and tail of a one-block-per-256-rows grid (2D Laplacian: 34.8 -> 33.6
+// us); on others (a long row holds up its block) a block per 256 rows.
+static unsigned scalar_grid(Ctx *c, Csr *A, uint64_t n, cudaStream_t s) {
+    bool known = false;
+    if (csr_max_row(c, A, s, &known) != SPG_OK) {
+        cudaGetLastError();
+        known = false;
+    }
+    const bool balanced = known && A->max_row <= SCALAR_BALANCED_ROW;
+    return grid_for(n, BLOCK, balanced ? (unsigned)c->n_sms * 8 : (1u << 30));
+}
+
 int spmv_row_block_reach(Ctx *c, Csr *A, int nb, cudaStream_t s) {
+    bool known = false;
+    SPG_TRY(csr_max_row(c, A, s, &known));  // before any capture of the row blocks
     if ((int)A->host_reach.size() == nb) return SPG_OK;
     DevBuf d;
     SPG_TRY(d.alloc(nb * sizeof(long long), s));
@@ -498,7 +559,7 @@ int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, ui
     double *yb = y + r0;
     switch (variant) {
         case SPG_SPMV_SCALAR:
-            spmv_scalar<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(off, cols, vals, x, yb, n);
+            spmv_scalar<<<scalar_grid(c, A, n, s), BLOCK, 0, s>>>(off, cols, vals, x, yb, n);
             break;
 #define SPG_VEC_CASE(ID, G)                                                                  \
     case ID:                                                                                 \
@@ -525,7 +586,7 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStr
     const double *vals = A->d_vals();
     switch (variant) {
         case SPG_SPMV_SCALAR:
-            spmv_scalar<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(off, cols, vals, x, y, n);
+            spmv_scalar<<<scalar_grid(c, A, n, s), BLOCK, 0, s>>>(off, cols, vals, x, y, n);
             break;
 #define SPG_VEC_CASE(ID, G)                                                                   \
     case ID:                                                                                  \

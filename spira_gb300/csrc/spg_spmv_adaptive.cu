@@ -278,21 +278,6 @@ __global__ void seg_fixup(const Rec *__restrict__ recs, uint64_t q0, uint64_t q1
     y[nzrow ? nzrow[row] : row] = s;
 }
 
-__global__ void seg_max_row(const uint64_t *__restrict__ off, uint64_t n, unsigned long long *__restrict__ mx) {
-    unsigned long long m = 0;
-    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x)
-        m = max(m, (unsigned long long)(off[r + 1] - off[r]));
-#pragma unroll
-    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ unsigned long long s_m[32];  // one atomic per block, not per warp
-    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (unsigned w = 1; w < (blockDim.x >> 5); ++w) m = max(m, s_m[w]);
-        atomicMax(mx, m);
-    }
-}
-
 __global__ void seg_empty_rows(const uint32_t *__restrict__ empty, uint64_t n_empty, double *__restrict__ y) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_empty) y[empty[i]] = 0.0;
@@ -424,19 +409,9 @@ int spmv_adaptive_blocks(Ctx *c, Csr *A, int variant, int nb, std::vector<uint64
     }
     // Blocks must be long enough that a row starting in block b ends by the
     // end of block b + 1 (the fix-up of block b reads ahead one block).
-    uint64_t max_row = 0;
-    if (A->n_rows) {
-        DevBuf mx;
-        SPG_TRY(mx.alloc(sizeof(unsigned long long), s));
-        SPG_CUDA_TRY(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned long long), s));
-        seg_max_row<<<grid_for(A->n_rows, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(
-            A->d_off(), A->n_rows, mx.as<unsigned long long>());
-        SPG_LAUNCH_CHECK();
-        unsigned long long h = 0;
-        SPG_CUDA_TRY(cudaMemcpyAsync(&h, mx.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
-        max_row = h;
-    }
+    bool known = false;
+    SPG_TRY(csr_max_row(c, A, s, &known));
+    const uint64_t max_row = known ? A->max_row : A->nnz;  // no row is longer than nnz
     const uint64_t chunk_nnz = 32ull * (variant == SPG_SPMV_ADAPTIVE ? 32 : 16);
     while (nb > 1 && (nch / nb) * chunk_nnz < max_row + 2 * chunk_nnz) --nb;
     if (nb < 1) nb = 1;
