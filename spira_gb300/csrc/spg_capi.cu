@@ -432,6 +432,7 @@ static int spmv_host_impl(spg_ctx *c, const spg_csr *Ac, const double *x, uint64
     if (variant == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &variant));
     if (variant < 0 || variant >= SPG_SPMV_N_VARIANTS)
         return set_error(SPG_ERR_INVALID_ARGUMENT, "%s: unknown variant %d", who, variant);
+    SPG_TRY(spmv_prepare(c, A, variant, s));  // plans synchronise: not inside the recorded graph
     // pinned buffers stage through the matrix's own device vectors (recorded
     // graphs stay valid across calls, matrices can overlap); pageable ones
     // through the context's
@@ -694,6 +695,7 @@ int spg_spmv_host_multi(spg_ctx *c, uint32_t n, const spg_csr *const *mats, cons
         if (v == SPG_SPMV_AUTO) SPG_TRY(spmv_resolve_auto(c, A, &v));
         if (v < 0 || v >= SPG_SPMV_N_VARIANTS)
             return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spmv_host_multi: unknown variant %d", v);
+        SPG_TRY(spmv_prepare(c, A, v, s));  // before the graph is recorded
         if (A->stage_x.bytes < A->n_cols * sizeof(double)) SPG_TRY(A->stage_x.alloc(A->n_cols * sizeof(double), s));
         if (A->stage_y.bytes < A->n_rows * sizeof(double)) SPG_TRY(A->stage_y.alloc(A->n_rows * sizeof(double), s));
         MultiPlan &p = P[i];

@@ -325,6 +325,10 @@ int spmv_row_block_reach(Ctx *c, Csr *A, int nb, cudaStream_t s);
 // Fills A->max_row (the longest row) once per CSR; `known` false while `s`
 // is being captured (the count needs a synchronisation).
 int csr_max_row(Ctx *c, Csr *A, cudaStream_t s, bool *known);
+// Builds whatever plan `variant` needs, so that a later spmv_launch only
+// enqueues work (plans synchronise: callers that record a CUDA graph call it
+// before the recording).
+int spmv_prepare(Ctx *c, Csr *A, int variant, cudaStream_t s);
 // The cached plan slot of one of those variants.
 inline SpmvPlan &adaptive_plan_of(Csr *A, int variant) {
     return variant == SPG_SPMV_INTERLEAVED ? A->plan_inter : A->plan_adaptive;

@@ -578,6 +578,21 @@ int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, ui
     return SPG_OK;
 }
 
+int spmv_prepare(Ctx *c, Csr *A, int variant, cudaStream_t s) {
+    switch (variant) {
+        case SPG_SPMV_STREAM:
+            return build_stream_plan(c, A, s);
+        case SPG_SPMV_MERGE:
+            return build_merge_plan(c, A, s);
+        case SPG_SPMV_ADAPTIVE:
+        case SPG_SPMV_ADAPTIVE16:
+        case SPG_SPMV_INTERLEAVED:
+            return build_adaptive_plan(c, A, variant, s);
+        default:
+            return SPG_OK;
+    }
+}
+
 int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s) {
     const uint64_t n = A->n_rows;
     if (n == 0) return SPG_OK;

@@ -279,3 +279,23 @@ def test_spmv_device_pointers_and_stream(ctx):
     s.synchronize()
     y_ref, scale = oracle.spmv_compensated(A.download(), x)
     assert spmv_rel_err(yd.cpu().numpy(), y_ref, scale) <= SPMV_TOL
+
+
+def test_host_spmv_multi_builds_plans_before_recording(ctx):
+    """Plan-based variants named explicitly on matrices that never ran them:
+    their plans are built before the graph is recorded (a plan build
+    synchronises, which a recording stream cannot)."""
+    import torch
+    specs = [(sg.SPMV_MERGE, 20_000, 41), (sg.SPMV_STREAM, 30_000, 42), (sg.SPMV_INTERLEAVED, 25_000, 43)]
+    mats, xs, ys, want = [], [], [], []
+    for v, n, seed in specs:
+        r, c, vals = gen.random_rows(n, n, 9, seed=seed)
+        mats.append(build(ctx, n, n, [(r, c, vals)]))
+        x = gen.dense_x(n, seed)
+        xs.append(torch.from_numpy(x).pin_memory())
+        ys.append(torch.empty(n, dtype=torch.float64).pin_memory())
+    sg.spmv_host_multi(ctx, mats, [x.numpy() for x in xs], [y.numpy() for y in ys],
+                       variants=[v for v, _, _ in specs])
+    ctx.sync()
+    for A, (v, _, _), x, y in zip(mats, specs, xs, ys):
+        np.testing.assert_array_equal(y.numpy(), A.spmv_host(x.numpy().copy(), variant=v))
