@@ -85,10 +85,15 @@ __global__ void seg_row_maps(const uint64_t *__restrict__ ne_scan, uint64_t n, u
 
 // ---------------------------------------------------------------- SpMV
 // ITEMS nonzeros per lane, handled in sub-batches of SUB (loads, gathers, FMAs)
-// to keep registers low enough for 4 CTAs of 256 threads per SM. INTER: cols
-// and vals are the lane-interleaved copies (ITEMS == 16).
-template <int ITEMS, int SUB, bool INTER>
-__global__ void __launch_bounds__(256, 4)
+// to keep registers low enough for MINB CTAs of 256 threads per SM. INTER: cols
+// and vals are the lane-interleaved copies (ITEMS == 16). The sub-batch size
+// does not change the FMA order. INTERLEAVED runs SUB = 2 at 32 registers, 8
+// CTAs (64 warps) per SM: on the random-column Zipf matrix its gathers are
+// latency-bound, and more warps with 2 gathers each in flight beat fewer with
+// 8 (4M rows: 0.268 ms against 0.289-0.299 with SUB = 8 at 4 CTAs, 0.276 with
+// SUB = 4 at 5 CTAs).
+template <int ITEMS, int SUB, bool INTER, int MINB = 4>
+__global__ void __launch_bounds__(256, MINB)
 spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, const double *__restrict__ x,
          double *__restrict__ y, uint64_t nnz, const unsigned *__restrict__ bitmap,
          const uint32_t *__restrict__ chunk_base, const uint32_t *__restrict__ nzrow, Rec *__restrict__ recs,
@@ -96,6 +101,7 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
     const uint64_t w = c0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= c1) return;
+    static_assert(SUB % 4 == 0 || (INTER && SUB == 2), "column loads come in 16-byte pieces (interleaved: halves)");
     const uint64_t p0 = w * (32ull * ITEMS) + (uint64_t)lane * ITEMS;
     unsigned word = 0;
     if (p0 < nnz) {
@@ -132,14 +138,21 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
                     v[u] = t.x;
                     v[u + 1] = t.y;
                 }
+                if constexpr (SUB >= 4) {
 #pragma unroll
-                for (int u = 0; u < SUB; u += 4) {
-                    const uint4 t = __ldcs(reinterpret_cast<const uint4 *>(
-                        cols + cb + 128u * (unsigned)((SUB * h + u) >> 2) + 4u * (unsigned)lane));
-                    c[u] = t.x;
-                    c[u + 1] = t.y;
-                    c[u + 2] = t.z;
-                    c[u + 3] = t.w;
+                    for (int u = 0; u < SUB; u += 4) {
+                        const uint4 t = __ldcs(reinterpret_cast<const uint4 *>(
+                            cols + cb + 128u * (unsigned)((SUB * h + u) >> 2) + 4u * (unsigned)lane));
+                        c[u] = t.x;
+                        c[u + 1] = t.y;
+                        c[u + 2] = t.z;
+                        c[u + 3] = t.w;
+                    }
+                } else {  // SUB == 2: one half of the lane's 16-byte piece of columns
+                    const uint2 t = __ldcs(reinterpret_cast<const uint2 *>(
+                        cols + cb + 128u * (unsigned)((SUB * h) >> 2) + 4u * (unsigned)lane + ((SUB * h) & 3u)));
+                    c[0] = t.x;
+                    c[1] = t.y;
                 }
             } else {
 #pragma unroll
@@ -359,7 +372,7 @@ int launch_seg(const SpmvPlan &P, const Csr *A, const double *x, double *y, int 
     const uint32_t *nzrow = P.count1 ? P.extra1.as<uint32_t>() : nullptr;
     const unsigned grid = grid_for((c1 - c0) * 32, 256);
     if (variant == SPG_SPMV_INTERLEAVED)
-        spmv_seg<16, 8, true><<<grid, 256, 0, s>>>(P.extra3.as<uint32_t>(), P.extra4.as<double>(), x, y, A->nnz,
+        spmv_seg<16, 2, true, 8><<<grid, 256, 0, s>>>(P.extra3.as<uint32_t>(), P.extra4.as<double>(), x, y, A->nnz,
                                                 P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
                                                 P.aux.as<Rec>(), c0, c1);
     else if (variant == SPG_SPMV_ADAPTIVE16)
