@@ -580,6 +580,10 @@ int spmv_launch_rows(Ctx *c, Csr *A, const double *x, double *y, int variant, ui
 
 int spmv_prepare(Ctx *c, Csr *A, int variant, cudaStream_t s) {
     switch (variant) {
+        case SPG_SPMV_SCALAR: {  // the longest row picks SCALAR's grid
+            bool known = false;
+            return csr_max_row(c, A, s, &known);
+        }
         case SPG_SPMV_STREAM:
             return build_stream_plan(c, A, s);
         case SPG_SPMV_MERGE:
