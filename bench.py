@@ -292,12 +292,13 @@ def run_ours(args):
     dm = mats[dom]
     achieved = dm["bytes"] / (per_sel[dom] * 1e-3) / 1e9
     gpu_launches = rep.world * args.steps * sum(m["A"].spmv_launches(m["selected"]) for m in mats)
-    # The second ceiling of a random-column matrix: L2 -> SM transfers. Every x
-    # read moves its own 32-byte sector and the 12 B/nnz matrix stream crosses
-    # the same path; the probe's random reads (one sector each) measure the rate.
+    # The second ceiling of a random-column matrix: requests from L1 to L2.
+    # Every x read is its own request (one 32-byte sector); the 12 B/nnz matrix
+    # stream arrives in coalesced 128-byte requests. The probe's random reads
+    # (one request each) measure the rate.
     gather_rate = ctx.probe_gather_rate(1 << 22, 1 << 26)
-    l2_sm_bytes = 32 * dm["nnz"] + 12 * dm["nnz"]
-    floor_ms = l2_sm_bytes / (32 * gather_rate) * 1e3
+    l1_l2_requests = dm["nnz"] * (1 + 12 / 128)
+    floor_ms = l1_l2_requests / gather_rate * 1e3
     cap = NCU_TRAFFIC.get((dm["name"], sg.SPMV_NAMES[dm["selected"]]))
     traffic = round(cap[0] * dm["nnz"] / cap[1]) if cap else None
 
@@ -346,9 +347,9 @@ def run_ours(args):
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "algorithmic_bytes": dm["bytes"],
                      "gather_ceiling": {"random_8B_gathers_per_s": round(gather_rate, -6),
-                                        "l2_to_sm_gbs": round(32 * gather_rate / 1e9, 1),
                                         "probe": "spg_probe_gather_rate(2^22 doubles, 2^26 reads)",
-                                        "l2_to_sm_bytes_per_launch": l2_sm_bytes,
+                                        "l1_to_l2_requests_per_launch": round(l1_l2_requests),
+                                        "model": "one request per x read + matrix stream / 128 B",
                                         "floor_ms": round(floor_ms, 5),
                                         "frac_of_ceiling": round(floor_ms / per_sel[dom], 4)}},
         "parity": {"max_err_vs_compensated_oracle": max_err, "tolerance": 1e-12,

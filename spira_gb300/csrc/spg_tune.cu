@@ -44,11 +44,14 @@ __device__ __forceinline__ uint32_t mix32(uint32_t a) {
 __global__ void gather_probe(const double *__restrict__ x, uint32_t mask, double *__restrict__ out, uint64_t n_thr) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= n_thr) return;
-    double a = 0.0;
+    // the values are combined with integer XOR: the probe times gathers alone,
+    // with no FP64 work beside them (an FP64 add per gather measured the same)
+    unsigned long long a = 0;
 #pragma unroll
     for (uint32_t j = 0; j < GATHER_PER_THREAD; ++j)
-        a += __ldg(x + (mix32((uint32_t)t * (uint32_t)GATHER_PER_THREAD + j) & mask));
-    out[t] = a;
+        a ^= (unsigned long long)__double_as_longlong(
+            __ldg(x + (mix32((uint32_t)t * (uint32_t)GATHER_PER_THREAD + j) & mask)));
+    out[t] = __longlong_as_double((long long)a);
 }
 
 // FP64 FMA rate: 8 independent chains per thread (enough warps and chains to
