@@ -37,8 +37,9 @@ ZIPF_N = 4_000_000
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel from one ncu
-# capture (profiles/spmv_interleaved_zipf4m.md): (bytes, nonzeros of the
-# captured matrix); scaled to the bench matrix by its nonzero count.
+# capture of dram__bytes_read.sum + dram__bytes_write.sum on the first-lock
+# 4M-row Zipf matrix: (bytes, nonzeros of the captured matrix); scaled to the
+# bench matrix by its nonzero count.
 NCU_TRAFFIC = {("zipf4m", "interleaved"): (817.1e6, 63_247_590)}
 
 
