@@ -47,6 +47,28 @@ def spmv_bytes(n_rows, n_cols, nnz):
     return 12 * nnz + 8 * (n_rows + 1) + 8 * n_cols + 8 * n_rows
 
 
+def workload_config(meta):
+    """The `config` both arms print: the same matrices (name, shape, nonzeros
+    after the re-lock) and the same bytes per step. meta: [(name, n_rows,
+    n_cols, nnz)]."""
+    mats = [{"name": nm, "n_rows": int(r), "n_cols": int(c), "nnz": int(z), "bytes_per_spmv": spmv_bytes(r, c, z)}
+            for nm, r, c, z in meta]
+    return {"workload": WORKLOAD, "matrices": mats, "bytes_per_step": int(sum(m["bytes_per_spmv"] for m in mats)),
+            "l2": "no flush: each step streams 1.03 GB (> 129 MB L2)"}
+
+
+# What the CPU arm runs where Spira's own sources are absent (kind "port"):
+# the oracle's C restatement of parallel::algorithms::spmv
+# (parallel/algorithms/spmv.hpp:125-161) over parallel_matrix's t*n/T row
+# partitions, each row in sparse_dot_double's SIMD order (4 accumulators x
+# lanes, tree reduce, tail) written as scalar fma() loops.
+CPU_PORT_BUILD = ("oracle/spira_oracle.c: gcc -O2 -ffp-contract=off, scalar fma() loops in the SIMD dot's "
+                  "order (NEON shape on aarch64: 2 lanes x 4 accumulators, fused tail; AVX-512 shape on x86-64), "
+                  "pthreads over t*n/T row partitions")
+CPU_REF_BUILD = ("Spira compiled from its sources (oracle/Makefile `ref`: -std=gnu++23 -O3, per-file SIMD flags), "
+                 "parallel::algorithms::spmv on parallel_matrix<soa_tag, uint32_t, double>")
+
+
 class Replicas:
     """One process per GPU under torchrun: every rank runs the same workload
     on its own GPU (the path does not shard: replicas only), timed regions are
@@ -320,9 +342,10 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded generators: 2D Laplacian 1414^2 and Zipf(1.8) 4M rows)",
-        "config": {"workload": WORKLOAD, "matrices": [
-            {"name": m["name"], "n_rows": m["n_rows"], "n_cols": m["n_cols"], "nnz": m["nnz"],
-             "bytes_per_spmv": m["bytes"], "variant": sg.SPMV_NAMES[m["selected"]],
+        "config": workload_config([(m["name"], m["n_rows"], m["n_cols"], m["nnz"]) for m in mats]),
+        "execution": "the two SpMVs of a step on two streams, joined per step",
+        "per_matrix": [
+            {"name": m["name"], "variant": sg.SPMV_NAMES[m["selected"]],
              "ms_selected": round(float(per_sel[i]), 5), "ms_plain": round(float(per_plain[i]), 5),
              "gbs_selected": round(m["bytes"] / (per_sel[i] * 1e-3) / 1e9, 1),
              "gbs_plain": round(m["bytes"] / (per_plain[i] * 1e-3) / 1e9, 1),
@@ -330,9 +353,6 @@ def run_ours(args):
              "gbs_100_back_to_back": round(m["bytes"] / (ms_b2b[i] * 1e-3) / 1e9, 1),
              "frac_100_back_to_back": round(m["bytes"] / (ms_b2b[i] * 1e-3) / 1e9 / peak, 4)}
             for i, m in enumerate(mats)],
-            "bytes_per_step": total_bytes,
-            "streams": "the two SpMVs of a step on two streams, joined per step",
-            "l2": "no flush: each step streams 1.03 GB (> 129 MB L2)"},
         "plain": {"variant": "scalar (one thread per row)", "value": round(W * total_bytes / (ms_plain * 1e-3) / 1e9, 2),
                   "ms_per_step": round(ms_plain, 5)},
         "autotuned": {"value": round(W * total_bytes / (ms_auto * 1e-3) / 1e9, 2), "ms_per_step": round(ms_auto, 5),
@@ -667,7 +687,8 @@ def cpu_baseline(host, xs, total_bytes, budget_s=12.0):
     dt = sum(t for t, _ in per)
     return {"value": round(total_bytes / dt / 1e9, 3), "unit": "GB/s", "cores": nthr, "kind": kind,
             "sample": f"full SpMVs of both matrices ({', '.join(str(r) for _, r in per)} reps), "
-                      f"{nthr} threads, parallel_matrix partitions t*n/T"}
+                      f"{nthr} threads, parallel_matrix partitions t*n/T",
+            "build": CPU_REF_BUILD if kind == "reference" else CPU_PORT_BUILD}
 
 
 def run_reference(args):
@@ -675,10 +696,11 @@ def run_reference(args):
     on the same matrices (built by the oracle's restatement of lock())."""
     import oracle
     nthr = os.cpu_count() or 1
-    host, xs = [], []
+    host, xs, meta = [], [], []
     for name, nr, nc, epochs, x in make_inputs(lambda n, seed: oracle.zipf_rows_host(n, seed=seed)):
         host.append(oracle.lock_epochs(nr, nc, epochs))
         xs.append(x)
+        meta.append((name, nr, nc, len(host[-1].cols)))
     total_bytes = sum(spmv_bytes(h.n_rows, h.n_cols, len(h.cols)) for h in host)
     kind = "reference" if oracle.ref_available() else "port"
     _cpu_spmv_seconds(host, xs, nthr, kind, budget_s=1.0)  # warm-up
@@ -691,8 +713,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bytes_per_step": total_bytes},
-        "cpu_baseline": {"value": v, "unit": "GB/s", "cores": nthr, "kind": kind, "sample": sample},
+        "config": workload_config(meta),
+        "cpu_baseline": {"value": v, "unit": "GB/s", "cores": nthr, "kind": kind, "sample": sample,
+                         "build": CPU_REF_BUILD if kind == "reference" else CPU_PORT_BUILD},
         "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 

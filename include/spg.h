@@ -91,6 +91,12 @@ int spg_ctx_stream(spg_ctx *ctx, void **stream);
 /* Waits for the context stream; SPG_ERR_DEVICE_TIMEOUT if a kernel's bounded
  * wait gave up since the last check (the context stays usable). */
 int spg_ctx_sync(spg_ctx *ctx);
+/* Bytes of the context's device memory pool (the device's default
+ * stream-ordered pool, from which every device buffer of libspg comes) that
+ * live buffers hold, and that the pool holds from the driver (freed buffers
+ * stay cached in it). Either pointer may be NULL. No Spira counterpart
+ * (Spira's memory is host memory). */
+int spg_ctx_pool_used(spg_ctx *ctx, uint64_t *used_bytes, uint64_t *reserved_bytes);
 
 /* ---- CSR handles ---------------------------------------------------------
  * spg_csr_create: an unbuilt n_rows x n_cols matrix (matrix.hpp:197-209). */
@@ -169,9 +175,12 @@ int spg_spmv_host_multi(spg_ctx *ctx, uint32_t n, const spg_csr *const *mats, co
  * scratch (tile starts and carry-outs) in a fixed array of about 2 MiB
  * compiled into libspg.so, which every device that loads the library keeps
  * until the process exits. Limit: rows + nonzeros <= spg_spmv_noalloc_max()
- * (117 440 512); larger matrices get SPG_ERR_INVALID_ARGUMENT. The first call
- * on a device looks up the array's device address (this may also load the
- * library's GPU code), so make that first call before any stream capture.
+ * (117 440 512); larger matrices get SPG_ERR_INVALID_ARGUMENT. Every
+ * spg_ctx_create looks up the array's device address for its device (this
+ * may also load the library's GPU code; a context created after
+ * cudaDeviceReset gets the new address), and a call finding none looks it up
+ * itself: create the context, or make that first call, before any stream
+ * capture.
  * Every call shares the one array: calls that overlap on the GPU (different
  * streams, or several host threads) race, and the caller must serialize
  * them. Each call rewrites all the scratch it reads. Device x, y; asynchronous
@@ -210,6 +219,13 @@ int spg_spmv_autotune(spg_ctx *ctx, const spg_csr *A, int reps, float *times_ms,
  * on matrices with randomly spread columns, where every nonzero's x read hits
  * its own L2 sector. */
 int spg_probe_gather_rate(spg_ctx *ctx, uint64_t n_x, uint64_t n_gathers, double *gathers_per_s);
+/* The same random reads with their shape as parameters, to show whether the
+ * rate above is the device's ceiling: blocks_per_sm x SMs blocks of 256
+ * threads (fewer may be resident; *resident_blocks_per_sm, may be NULL, says
+ * how many) walk n_gathers / per_thread items of per_thread independent reads
+ * (1, 2, 4, ..., 64 in flight per thread). No Spira counterpart. */
+int spg_probe_gather_rate_cfg(spg_ctx *ctx, uint64_t n_x, uint64_t n_gathers, int per_thread, int blocks_per_sm,
+                              double *gathers_per_s, int *resident_blocks_per_sm);
 /* Device probe, no Spira counterpart: the FP64 fused multiply-add rate (FMAs
  * per second, median of 5 timed runs after 2 warm-up runs) of a launch of 8
  * CTAs of 256 threads per SM, each thread running 8 independent FMA chains of

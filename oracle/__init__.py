@@ -19,7 +19,12 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "liboracle.so"
 REF_SO = HERE / "_ref" / "libspira_ref.so"
-REF_SRC = Path(os.environ.get("SPIRA_REF", "/root/reference"))
+# The Spira source tree to compile the reference from: $SPIRA_REF, no default.
+
+
+def ref_src() -> Path | None:
+    p = os.environ.get("SPIRA_REF")
+    return Path(p) if p else None
 
 Csr = namedtuple("Csr", "n_rows n_cols off cols vals capacity")
 
@@ -32,10 +37,13 @@ class _OrcCsr(C.Structure):
 def build(ref: bool | None = None) -> None:
     """Compile liboracle.so; and Spira itself when its sources are here."""
     subprocess.run(["make", "-s", "-C", str(HERE), "liboracle"], check=True)
+    src = ref_src()
     if ref is None:
-        ref = (REF_SRC / "include" / "spira" / "spira.hpp").exists()
+        ref = src is not None and (src / "include" / "spira" / "spira.hpp").exists()
     if ref:
-        subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
+        if src is None:
+            raise RuntimeError("SPIRA_REF must name the Spira source tree to build the reference")
+        subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={src}"], check=True)
 
 
 _orc = None

@@ -92,6 +92,7 @@ _SIGS = [
     ("spg_ctx_destroy", _I, [_P]),
     ("spg_ctx_stream", _I, [_P, C.POINTER(_P)]),
     ("spg_ctx_sync", _I, [_P]),
+    ("spg_ctx_pool_used", _I, [_P, C.POINTER(_U64), C.POINTER(_U64)]),
     ("spg_csr_create", _I, [_P, _U64, _U64, C.POINTER(_P)]),
     ("spg_csr_destroy", _I, [_P]),
     ("spg_csr_info_get", _I, [_P, C.POINTER(_Info)]),
@@ -115,6 +116,7 @@ _SIGS = [
     ("spg_spmv_features", _I, [_P, _P, _P]),
     ("spg_spmv_autotune", _I, [_P, _P, _I, _P, C.POINTER(_I)]),
     ("spg_probe_gather_rate", _I, [_P, _U64, _U64, C.POINTER(C.c_double)]),
+    ("spg_probe_gather_rate_cfg", _I, [_P, _U64, _U64, _I, _I, C.POINTER(C.c_double), C.POINTER(_I)]),
     ("spg_probe_fp64_rate", _I, [_P, C.c_uint32, C.POINTER(C.c_double)]),
     ("spg_selector_load", _I, [_P, _P, _U64, _I]),
     ("spg_mlp_param_count", _U64, [_I]),
@@ -215,6 +217,13 @@ class Context:
     def sync(self):
         _check(lib().spg_ctx_sync(self.h))
 
+    def pool_used(self):
+        """(bytes live buffers hold, bytes the pool holds) of the context's
+        device memory pool."""
+        u, r = C.c_uint64(), C.c_uint64()
+        _check(lib().spg_ctx_pool_used(self.h, C.byref(u), C.byref(r)))
+        return u.value, r.value
+
     def set_spmv_policy(self, policy: int):
         _check(lib().spg_set_spmv_policy(self.h, policy))
 
@@ -232,6 +241,28 @@ class Context:
         r = C.c_double()
         _check(lib().spg_probe_gather_rate(self.h, n_x, n_gathers, C.byref(r)))
         return r.value
+
+    def probe_gather_rate_cfg(self, per_thread: int, blocks_per_sm: int, n_x: int = 1 << 22,
+                              n_gathers: int = 1 << 26):
+        """(gathers per second, resident blocks per SM) of the random-read
+        probe with per_thread reads in flight per thread and blocks_per_sm
+        blocks of 256 threads per SM."""
+        r, b = C.c_double(), C.c_int()
+        _check(lib().spg_probe_gather_rate_cfg(self.h, n_x, n_gathers, per_thread, blocks_per_sm, C.byref(r),
+                                               C.byref(b)))
+        return r.value, b.value
+
+    def gather_ceiling_sweep(self, n_x: int = 1 << 22, n_gathers: int = 1 << 26):
+        """The random-read probe over reads in flight per thread (2..64) and
+        blocks per SM (2..16): every point and the maximum."""
+        pts = []
+        for per in (2, 4, 8, 16, 32, 64):
+            for bps in (2, 4, 8, 16):
+                rate, res = self.probe_gather_rate_cfg(per, bps, n_x, n_gathers)
+                pts.append({"per_thread": per, "blocks_per_sm": bps, "resident_blocks_per_sm": res,
+                            "gathers_per_s": rate})
+        best = max(pts, key=lambda p: p["gathers_per_s"])
+        return best, pts
 
     def probe_fp64_rate(self, iters: int = 4096) -> float:
         """FP64 fused multiply-adds per second over every SM: the ceiling of

@@ -146,6 +146,7 @@ int spg_ctx_create(int device, spg_ctx **out) {
         delete c;
         return set_error(SPG_ERR_CUDA, "spg_ctx_create: %s", cudaGetErrorString(e));
     }
+    noalloc_refresh(device);
     selector_load_default(c);
     *out = c;
     return SPG_OK;
@@ -188,6 +189,22 @@ int spg_ctx_destroy(spg_ctx *c) {
 int spg_ctx_stream(spg_ctx *c, void **stream) {
     if (!c || !stream) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_stream: null argument");
     *stream = c->stream;
+    return SPG_OK;
+}
+
+int spg_ctx_pool_used(spg_ctx *c, uint64_t *used_bytes, uint64_t *reserved_bytes) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_pool_used: null context");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (used_bytes) {
+        uint64_t v = 0;  // the attribute is a 64-bit unsigned count
+        SPG_CUDA_TRY(cudaMemPoolGetAttribute(c->pool, cudaMemPoolAttrUsedMemCurrent, &v));
+        *used_bytes = v;
+    }
+    if (reserved_bytes) {
+        uint64_t v = 0;  // the attribute is a 64-bit unsigned count
+        SPG_CUDA_TRY(cudaMemPoolGetAttribute(c->pool, cudaMemPoolAttrReservedMemCurrent, &v));
+        *reserved_bytes = v;
+    }
     return SPG_OK;
 }
 

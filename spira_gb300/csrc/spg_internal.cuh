@@ -305,6 +305,9 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant,
 int spmv_resolve_auto(Ctx *c, Csr *A, int *variant);
 // Loads spg_selector.bin from beside libspg.so (or $SPG_SELECTOR_MODEL) if any.
 int selector_load_default(Ctx *c);
+// Looks up the device address of spg_spmv_noalloc's scratch array for the
+// current device again (spg_spmv.cu); spg_ctx_create calls it.
+void noalloc_refresh(int device);
 // SPG_SPMV_ADAPTIVE, SPG_SPMV_ADAPTIVE16 and SPG_SPMV_INTERLEAVED
 // (spg_spmv_adaptive.cu); each builds and caches its plan on first use.
 int spmv_adaptive(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStream_t s);

@@ -665,27 +665,49 @@ constexpr size_t NOALLOC_BYTES = NOALLOC_STARTS_BYTES + NOALLOC_MAX_TILES * size
 static __device__ __align__(256) unsigned char g_spmv_noalloc_scratch[NOALLOC_BYTES];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
-void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+// Per device, the array's device address. Host threads with their own
+// contexts may look it up at the same time, hence atomics (they all store the
+// same value).
+std::atomic<void *> g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of the scratch array for the current device; looked up once
-// per device. The host-side symbol is only a stand-in and must never be
-// handed to a kernel.
-int noalloc_scratch(int device, void **out) {
-    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
-        return set_error(SPG_ERR_UNSUPPORTED, "spg_spmv_noalloc: device %d beyond %d", device, NOALLOC_MAX_DEVICES);
-    if (!g_noalloc_addr[device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return set_error(SPG_ERR_CUDA, "spg_spmv_noalloc: cudaGetSymbolAddress failed: %s",
-                             cudaGetErrorString(e));
-        g_noalloc_addr[device] = p;
-    }
-    *out = g_noalloc_addr[device];
+int noalloc_lookup(int device, void **out) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return set_error(SPG_ERR_CUDA, "spg_spmv_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+    g_noalloc_addr[device].store(p, std::memory_order_release);
+    *out = p;
     return SPG_OK;
 }
 
+// Device address of the scratch array for `device` (the current device). The
+// host-side symbol is only a stand-in and must never be handed to a kernel.
+int noalloc_scratch(int device, void **out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return set_error(SPG_ERR_UNSUPPORTED, "spg_spmv_noalloc: device %d beyond %d", device, NOALLOC_MAX_DEVICES);
+    void *p = g_noalloc_addr[device].load(std::memory_order_acquire);
+    if (p) {
+        *out = p;
+        return SPG_OK;
+    }
+    return noalloc_lookup(device, out);
+}
+
 }  // namespace
+
+// Called by spg_ctx_create with `device` current: the address is looked up
+// again for every new context, so a context created after cudaDeviceReset
+// (which ends the CUDA context the cached address belonged to) sees the new
+// one. Failures are left to the first spg_spmv_noalloc call to report.
+void noalloc_refresh(int device) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return;
+    void *p = nullptr;
+    if (noalloc_lookup(device, &p) != SPG_OK) {
+        g_noalloc_addr[device].store(nullptr, std::memory_order_release);
+        clear_error();
+    }
+}
+
 }  // namespace spg
 
 extern "C" uint64_t spg_spmv_noalloc_max(void) { return spg::NOALLOC_MAX_TILES * (uint64_t)spg::MG_TILE; }

@@ -54,6 +54,25 @@ __global__ void gather_probe(const double *__restrict__ x, uint32_t mask, double
     out[t] = __longlong_as_double((long long)a);
 }
 
+// The same reads with the number in flight and the occupancy as parameters:
+// a grid of blocks_per_sm x SMs blocks of 256 threads walks n_iter work items
+// of PER independent gathers each (grid-stride), so each thread has PER reads
+// in flight and an SM at most blocks x 256 x PER. Sweeping both shows whether
+// the rate above is a hardware ceiling or a latency limit of one shape.
+template <int PER>
+__global__ void __launch_bounds__(256) gather_probe_cfg(const double *__restrict__ x, uint32_t mask,
+                                                        double *__restrict__ out, uint64_t n_iter) {
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long a = 0;
+    for (uint64_t it = t0; it < n_iter; it += nt) {
+#pragma unroll
+        for (uint32_t j = 0; j < (uint32_t)PER; ++j)
+            a ^= (unsigned long long)__double_as_longlong(__ldg(x + (mix32((uint32_t)it * (uint32_t)PER + j) & mask)));
+    }
+    out[t0] = __longlong_as_double((long long)a);
+}
+
 // FP64 FMA rate: 8 independent chains per thread (enough warps and chains to
 // cover the pipe's latency); a = a * m + c with |m| < 1 stays bounded. m and c
 // are arguments, so nothing folds at compile time.
@@ -568,6 +587,67 @@ int spg_probe_gather_rate(spg_ctx *c, uint64_t n_x, uint64_t n_gathers, double *
     SPG_LAUNCH_CHECK();
     std::sort(ts.begin(), ts.end());
     *gathers_per_s = (double)(n_thr * GATHER_PER_THREAD) / (ts[ts.size() / 2] * 1e-3);
+    return SPG_OK;
+}
+
+int spg_probe_gather_rate_cfg(spg_ctx *c, uint64_t n_x, uint64_t n_gathers, int per_thread, int blocks_per_sm,
+                              double *gathers_per_s, int *resident_blocks_per_sm) {
+    if (!c || !gathers_per_s) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate_cfg: null argument");
+    if (n_x == 0 || (n_x & (n_x - 1)) || n_x > (1ull << 32))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate_cfg: n_x must be a power of two <= 2^32");
+    if (blocks_per_sm < 1 || blocks_per_sm > 64)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate_cfg: blocks_per_sm must be in [1, 64]");
+    const void *fn = nullptr;
+    switch (per_thread) {
+        case 1: fn = (const void *)gather_probe_cfg<1>; break;
+        case 2: fn = (const void *)gather_probe_cfg<2>; break;
+        case 4: fn = (const void *)gather_probe_cfg<4>; break;
+        case 8: fn = (const void *)gather_probe_cfg<8>; break;
+        case 16: fn = (const void *)gather_probe_cfg<16>; break;
+        case 32: fn = (const void *)gather_probe_cfg<32>; break;
+        case 64: fn = (const void *)gather_probe_cfg<64>; break;
+        default:
+            return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate_cfg: per_thread must be 1, 2, ..., 64");
+    }
+    const uint64_t n_iter = n_gathers / (uint64_t)per_thread;
+    if (n_iter == 0 || n_iter > (1ull << 32))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_probe_gather_rate_cfg: n_gathers out of range");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    int resident = 0;
+    SPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn, 256, 0));
+    if (resident_blocks_per_sm) *resident_blocks_per_sm = std::min(resident, blocks_per_sm);
+    cudaStream_t s = c->stream;
+    const unsigned grid = (unsigned)(blocks_per_sm * c->n_sms);
+    DevBuf x, out;
+    SPG_TRY(x.alloc(n_x * sizeof(double), s));
+    SPG_TRY(out.alloc((uint64_t)grid * 256 * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(x.ptr, 0, n_x * sizeof(double), s));
+    const double *xp = x.as<double>();
+    uint32_t mask = (uint32_t)(n_x - 1);
+    double *op = out.as<double>();
+    void *args[] = {(void *)&xp, (void *)&mask, (void *)&op, (void *)&n_iter};
+    cudaEvent_t e0, e1;
+    SPG_CUDA_TRY(cudaEventCreate(&e0));
+    SPG_CUDA_TRY(cudaEventCreate(&e1));
+    std::vector<float> ts;
+    int rc = SPG_OK;
+    for (int r = 0; r < 7 && rc == SPG_OK; ++r) {
+        cudaEventRecord(e0, s);
+        if (cudaLaunchKernel(fn, dim3(grid), dim3(256), args, 0, s) != cudaSuccess)
+            rc = set_error(SPG_ERR_CUDA, "gather probe: launch failed");
+        cudaEventRecord(e1, s);
+        if (rc == SPG_OK && cudaEventSynchronize(e1) != cudaSuccess)
+            rc = set_error(SPG_ERR_CUDA, "gather probe: event sync failed");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r >= 2) ts.push_back(ms);  // two warm-up runs
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SPG_TRY(rc);
+    SPG_LAUNCH_CHECK();
+    std::sort(ts.begin(), ts.end());
+    *gathers_per_s = (double)(n_iter * (uint64_t)per_thread) / (ts[ts.size() / 2] * 1e-3);
     return SPG_OK;
 }
 
