@@ -268,6 +268,7 @@ def run_ours(args):
     ms_b2b = [b2b(m) for m in mats]
     clocks = clk.stop()
     batched = None if (args.no_batched or rep.rank != 0) else run_batched(ctx, stream)
+    selector = None if (args.no_selector or rep.rank != 0) else run_selector(ctx)
 
     # parity check of the measured configuration against the compensated oracle
     import oracle
@@ -318,8 +319,11 @@ def run_ours(args):
     # The second ceiling of a random-column matrix: requests from L1 to L2.
     # Every x read is its own request (one 32-byte sector); the 12 B/nnz matrix
     # stream arrives in coalesced 128-byte requests. The probe's random reads
-    # (one request each) measure the rate.
-    gather_rate = ctx.probe_gather_rate(1 << 22, 1 << 26)
+    # (one request each), swept over reads in flight per thread and blocks per
+    # SM, measure the rate; its maximum is the ceiling.
+    g_best, g_pts = ctx.gather_ceiling_sweep(1 << 22, 1 << 26)
+    gather_rate = g_best["gathers_per_s"]
+    g_rates = [p["gathers_per_s"] for p in g_pts]
     l1_l2_requests = dm["nnz"] * (1 + 12 / 128)
     floor_ms = l1_l2_requests / gather_rate * 1e3
     cap = NCU_TRAFFIC.get((dm["name"], sg.SPMV_NAMES[dm["selected"]]))
@@ -362,13 +366,19 @@ def run_ours(args):
                                                              for v, t in enumerate(m["autotune_ms"])}
                                                   for m in mats}},
         "batched": batched,
+        "selector": selector,
         "ops": ops,
         "roofline": {"bound": "hbm", "kernel": f"spmv[{dm['name']}:{sg.SPMV_NAMES[dm['selected']]}]",
                      "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "algorithmic_bytes": dm["bytes"],
                      "gather_ceiling": {"random_8B_gathers_per_s": round(gather_rate, -6),
-                                        "probe": "spg_probe_gather_rate(2^22 doubles, 2^26 reads)",
+                                        "probe": "spg_probe_gather_rate_cfg(2^22 doubles, 2^26 reads): maximum "
+                                                 "over 2..64 reads in flight per thread x 2..16 blocks of 256 "
+                                                 "per SM",
+                                        "sweep_min_max": [round(min(g_rates), -6), round(max(g_rates), -6)],
+                                        "best_shape": {k: g_best[k] for k in ("per_thread", "blocks_per_sm",
+                                                                              "resident_blocks_per_sm")},
                                         "l1_to_l2_requests_per_launch": round(l1_l2_requests),
                                         "model": "one request per x read + matrix stream / 128 B",
                                         "floor_ms": round(floor_ms, 5),
@@ -457,6 +467,46 @@ def run_batched(ctx, stream, n_mats=4096, seed=2024):
     return out
 
 
+# The shipped selectors were trained on corpus matrices 0 .. n-1 drawn with
+# seed 7 (SpMV: n = 20 000, SpGEMM: n = 4 000; the last 10 % of each held out
+# during training). The bench scores them on matrices from index n on, which
+# neither training nor its held-out check has seen.
+SELECTOR_HELD_OUT = {"spmv": (20_000, 3), "spgemm": (4_000, 2)}  # first index, autotune reps
+
+
+def run_selector(ctx, budget_s=75.0):
+    """Held-out regret of the shipped learned selectors against exhaustive
+    autotuning (every candidate timed) and against the fixed default
+    (ADAPTIVE16 for SpMV, ROWMERGE for SpGEMM: the method without the
+    selector), on a time-capped slice of the corpus the selectors never saw."""
+    import spira_gb300 as sg
+    from spira_gb300 import selector as S
+    out = {}
+    models = {"spmv": sg._PKG / "spg_selector.bin", "spgemm": sg._PKG / "spg_spgemm_selector.bin"}
+    share = {"spmv": 0.55, "spgemm": 0.45}
+    for op, (first, reps) in SELECTOR_HELD_OUT.items():
+        path = models[op]
+        if not path.exists():
+            out[op] = {"unavailable": f"no shipped model ({path.name})"}
+            continue
+        blob = np.fromfile(path, dtype=np.float32)
+        t0 = time.time()
+        X, T, _ = S.collect(ctx, range(first, first + 100_000), seed=7, reps=reps, op=op,
+                            time_cap_s=budget_s * share[op])
+        secs = time.time() - t0
+        choice = S.predict(ctx, blob, X, op=op).argmin(axis=1)
+        default = S.DEFAULT_SPMV if op == "spmv" else S.DEFAULT_SPGEMM
+        ev = S.evaluate(T, choice, default)
+        names = sg.SPMV_NAMES if op == "spmv" else sg.SPGEMM_NAMES
+        ev.update({"corpus_indices": [first, first + len(X)], "seed": 7, "seconds": round(secs, 1),
+                   "candidates": len(names), "default": names[default],
+                   "exhaustive_best_histogram": {names[k]: int(c) for k, c in
+                                                 enumerate(np.bincount(T.argmin(axis=1), minlength=len(names)))
+                                                 if c}})
+        out[op] = ev  # (predict installed the shipped model, which the context had loaded anyway)
+    return out
+
+
 def lock_bytes(n_rows, staged, nnz_old, nnz_new):
     """Algorithmic bytes of one lock(): read the staged triples (u32 row, u32
     column, f64 value) and the old CSR, write the new CSR."""
@@ -469,19 +519,27 @@ def csr_bytes(n_rows, nnz):
 
 
 def run_ops(ctx, peak):
-    """lock() (first build and 1 % re-lock merge), transpose and SpGEMM on the
-    GPU at their full configuration sizes, against the oracle's C port of the
-    same steps on one host core. GPU times are wall-clock around the C-ABI
-    call with the stream synchronised on both sides (the calls synchronise
-    internally: their output sizes are data-dependent), median of 3."""
+    """lock() (first build and 1 % re-lock merge), transpose and SpGEMM (every
+    variant and the selected one) on the GPU at their full configuration
+    sizes. Each GPU figure is the median of 3 calls, twice: wall time around
+    the C-ABI call with the stream synchronised on both sides (the calls
+    synchronise internally: their output sizes are data-dependent), and
+    device time (spg_ctx_timer: the stream's work between those internal
+    synchronisations, host round trips excluded). CPU: the oracle's C port of
+    Spira's parallel paths on all host cores (parallel_matrix partitions
+    t*n/T: per-partition lock, row-partitioned Gustavson SpGEMM, transpose by
+    output partitions each scanning all of A), and of the serial path on one
+    core."""
     import torch
 
     import oracle
     import spira_gb300 as sg
     from spira_gb300 import gen, gen_device
 
+    nthr = os.cpu_count() or 1
+
     def wall(fn, reps=3, setup=None):
-        ts = []
+        ts, ds = [], []
         for _ in range(reps):
             if setup:
                 setup()
@@ -490,23 +548,35 @@ def run_ops(ctx, peak):
             fn()
             ctx.sync()
             ts.append(time.perf_counter() - t0)
-        return float(np.median(ts)) * 1e3
+        for _ in range(reps):
+            if setup:
+                setup()
+            ctx.sync()
+            ds.append(ctx.device_ms(fn))
+        return float(np.median(ts)) * 1e3, float(np.median(ds))
 
     def cpu(fn):
         t0 = time.perf_counter()
         out = fn()
         return (time.perf_counter() - t0) * 1e3, out
 
-    def rec(name, gpu_ms, by, cpu_ms, **kw):
-        d = {"case": name, "gpu_ms": round(gpu_ms, 3), "bytes": int(by),
-             "gbs": round(by / (gpu_ms * 1e-3) / 1e9, 1), "frac_of_hbm": round(by / (gpu_ms * 1e-3) / 1e9 / peak, 4)}
+    def rec(name, gpu, by, cpu_ms, cpu_serial_ms=None, **kw):
+        gpu_ms, dev_ms = gpu
+        d = {"case": name, "gpu_ms": round(gpu_ms, 3), "gpu_device_ms": round(dev_ms, 3), "bytes": int(by),
+             "gbs": round(by / (gpu_ms * 1e-3) / 1e9, 1), "frac_of_hbm": round(by / (gpu_ms * 1e-3) / 1e9 / peak, 4),
+             "device_gbs": round(by / (dev_ms * 1e-3) / 1e9, 1),
+             "device_frac_of_hbm": round(by / (dev_ms * 1e-3) / 1e9 / peak, 4)}
         if cpu_ms is not None:
-            d.update({"cpu_ms": round(cpu_ms, 1), "cpu_kind": "port", "cpu_cores": 1,
+            d.update({"cpu_ms": round(cpu_ms, 1), "cpu_kind": "port", "cpu_cores": nthr,
                       "speedup_vs_cpu": round(cpu_ms / gpu_ms, 1)})
+        if cpu_serial_ms is not None:
+            d.update({"cpu_serial_ms": round(cpu_serial_ms, 1), "cpu_serial_cores": 1,
+                      "speedup_vs_cpu_serial": round(cpu_serial_ms / gpu_ms, 1)})
         d.update(kw)
         return d
 
-    out = {"lock": [], "transpose": [], "spgemm": []}
+    out = {"lock": [], "transpose": [], "spgemm": [],
+           "cpu": f"oracle C port of Spira's parallel paths, {nthr} threads (serial path on 1 core beside it)"}
     dev = "cuda:0"
 
     def to_dev(r, c, v):
@@ -540,22 +610,23 @@ def run_ops(ctx, peak):
         t_relock = wall(lambda: A.lock(*delta), setup=lambda: A.copy_from(pristine))
         nnz1 = A.nnz
         t_e2e = None
-        cpu_first = cpu_relock = None
+        cpu_first = cpu_relock = ser_first = ser_relock = None
         if host_first:
             def do_host():
                 B = sg.Csr(ctx, n, n)
                 B.lock(*first)
                 B.close()
-            t_e2e = wall(do_host)
-            cpu_first, _ = cpu(lambda: oracle.lock_epochs(n, n, [first]))
-            cpu_both, _ = cpu(lambda: oracle.lock_epochs(n, n, [first, delta]))
-            cpu_relock = max(cpu_both - cpu_first, 0.0)
-        out["lock"].append(rec(f"{name}_first", t_first, lock_bytes(n, m, 0, nnz0), cpu_first, staged=int(m),
-                               nnz=int(nnz0), staging="device",
+            t_e2e = wall(do_host)[0]
+            ser_first, _ = cpu(lambda: oracle.lock_epochs(n, n, [first]))
+            ser_both, _ = cpu(lambda: oracle.lock_epochs(n, n, [first, delta]))
+            ser_relock = max(ser_both - ser_first, 0.0)
+            secs, _ = oracle.lock_parallel_time(n, n, [first, delta], nthr)
+            cpu_first, cpu_relock = secs[0] * 1e3, secs[1] * 1e3
+        out["lock"].append(rec(f"{name}_first", t_first, lock_bytes(n, m, 0, nnz0), cpu_first, ser_first,
+                               staged=int(m), nnz=int(nnz0), staging="device",
                                **({"e2e_ms_host_staging": round(t_e2e, 3)} if t_e2e else {})))
         out["lock"].append(rec(f"{name}_relock", t_relock, lock_bytes(n, len(delta[0]), nnz0, nnz1), cpu_relock,
-                               staged=int(len(delta[0])), nnz=int(nnz1), staging="host",
-                               **({"cpu_note": "port: lock of both epochs minus the first"} if cpu_relock else {})))
+                               ser_relock, staged=int(len(delta[0])), nnz=int(nnz1), staging="host"))
         A.close()
         pristine.close()
         del d_first
@@ -571,28 +642,52 @@ def run_ops(ctx, peak):
         res = {}
 
         def do_t():
+            if "T" in res:
+                res["T"].close()
             res["T"] = A.transpose()
 
         t_t = wall(do_t)
-        cpu_t, T_ref = cpu(lambda: oracle.transpose(H))
+        ser_t, T_ref = cpu(lambda: oracle.transpose(H))
+        cpu_t, _ = cpu(lambda: oracle.transpose_parallel(H, nthr))
         T = res["T"]
         same_t = oracle.csr_digest(T.download()) == oracle.csr_digest(T_ref)
-        out["transpose"].append(rec(name, t_t, 2 * csr_bytes(n, A.nnz), cpu_t, nnz=int(A.nnz), bit_exact=same_t))
+        out["transpose"].append(rec(name, t_t, 2 * csr_bytes(n, A.nnz), cpu_t, ser_t, nnz=int(A.nnz),
+                                    bit_exact=same_t))
         T.close()
+        res.clear()
+        ser_g, C_ref = cpu(lambda: oracle.spgemm(H, H))
+        cpu_g, _ = cpu(lambda: oracle.spgemm_parallel(H, H, nthr))
+        ref_digest = oracle.csr_digest(C_ref)
+        prods = int(oracle.spgemm_products(H, H))
+        by = 2 * csr_bytes(n, A.nnz) + csr_bytes(n, len(C_ref.cols))
+        per_variant = {}
+        for vname, vid in sg.SPGEMM_VARIANTS.items():
+            def do_g():
+                if "C" in res:
+                    res["C"].close()
+                res["C"] = A.spgemm(A, vid)
 
-        def do_g():
+            tv = wall(do_g)
+            per_variant[vname] = {"gpu_ms": round(tv[0], 3), "gpu_device_ms": round(tv[1], 3),
+                                  "bit_exact": oracle.csr_digest(res["C"].download()) == ref_digest}
+            res["C"].close()
+            res.clear()
+        sel = A.spgemm_selected(A)
+
+        def do_auto():
             if "C" in res:
                 res["C"].close()
             res["C"] = A.spgemm(A)
 
-        t_g = wall(do_g)
-        cpu_g, C_ref = cpu(lambda: oracle.spgemm(H, H))
+        t_g = wall(do_auto)
         Cm = res["C"]
-        prods = int(oracle.spgemm_products(H, H))
-        same_g = oracle.csr_digest(Cm.download()) == oracle.csr_digest(C_ref)
-        by = 2 * csr_bytes(n, A.nnz) + csr_bytes(n, Cm.nnz)
-        out["spgemm"].append(rec(name, t_g, by, cpu_g, nnz_a=int(A.nnz), nnz_c=int(Cm.nnz), products=prods,
-                                 gproducts_per_s=round(prods / (t_g * 1e-3) / 1e9, 2), bit_exact=same_g))
+        same_g = oracle.csr_digest(Cm.download()) == ref_digest
+        best = min(per_variant, key=lambda k: per_variant[k]["gpu_ms"])
+        out["spgemm"].append(rec(name, t_g, by, cpu_g, ser_g, nnz_a=int(A.nnz), nnz_c=int(Cm.nnz), products=prods,
+                                 gproducts_per_s=round(prods / (t_g[0] * 1e-3) / 1e9, 2), bit_exact=same_g,
+                                 selected=sg.SPGEMM_NAMES[sel], fastest=best,
+                                 selected_over_fastest=round(t_g[0] / per_variant[best]["gpu_ms"], 4),
+                                 variants=per_variant))
         Cm.close()
         A.close()
 
@@ -622,7 +717,7 @@ def run_ops(ctx, peak):
         cpu_add, C_ref = cpu(lambda: oracle.add(HA, HB))
         Cm = res["C"]
         by = csr_bytes(n, A.nnz) + csr_bytes(n, B.nnz) + csr_bytes(n, Cm.nnz)
-        out["elementwise"].append(rec(f"add_{name}", t_add, by, cpu_add, nnz_a=int(A.nnz), nnz_b=int(B.nnz),
+        out["elementwise"].append(rec(f"add_{name}", t_add, by, None, cpu_add, nnz_a=int(A.nnz), nnz_b=int(B.nnz),
                                       nnz_c=int(Cm.nnz),
                                       bit_exact=oracle.csr_digest(Cm.download()) == oracle.csr_digest(C_ref)))
         Cm.close()
@@ -635,15 +730,15 @@ def run_ops(ctx, peak):
 
         t_sc = wall(do_scale)
         cpu_sc, S_ref = cpu(lambda: oracle.scale(HA, 2.5))
-        out["elementwise"].append(rec(f"scale_copy_{name}", t_sc, 2 * csr_bytes(n, A.nnz), cpu_sc, nnz=int(A.nnz),
+        out["elementwise"].append(rec(f"scale_copy_{name}", t_sc, 2 * csr_bytes(n, A.nnz), None, cpu_sc, nnz=int(A.nnz),
                                       bit_exact=oracle.csr_digest(res["S"].download()) == oracle.csr_digest(S_ref)))
         res["S"].close()
-        t_ip = wall(lambda: A.scale_(-1.0))  # exact: three sign flips
+        t_ip = wall(lambda: A.scale_(-1.0))  # exact: six sign flips, A as before
         out["elementwise"].append(rec(f"scale_in_place_{name}", t_ip, 16 * A.nnz, None, nnz=int(A.nnz)))
         sums = torch.empty(n, dtype=torch.float64, device=dev)
         t_rs = wall(lambda: A.row_sums(sums))
         cpu_rs, rs_ref = cpu(lambda: oracle.row_sums(A.download()))
-        out["elementwise"].append(rec(f"row_sums_{name}", t_rs, 8 * A.nnz + 8 * (n + 1) + 8 * n, cpu_rs,
+        out["elementwise"].append(rec(f"row_sums_{name}", t_rs, 8 * A.nnz + 8 * (n + 1) + 8 * n, None, cpu_rs,
                                       bit_exact=bool(np.array_equal(sums.cpu().numpy().view(np.uint64),
                                                                     rs_ref.view(np.uint64)))))
         A.close()
@@ -738,8 +833,9 @@ PROFILE_CASES = {
 }
 
 
-def run_profile_op(ctx, case, n, kind, reps):
-    """lock / transpose / SpGEMM cases of run_profile_case."""
+def run_profile_op(ctx, case, n, kind, reps, variants=""):
+    """lock / transpose / SpGEMM cases of run_profile_case (SpGEMM: each
+    variant named in `variants`, else the selected one)."""
     import spira_gb300 as sg
     from spira_gb300 import gen, gen_device
     ms = []
@@ -818,13 +914,21 @@ def run_profile_op(ctx, case, n, kind, reps):
         A = sg.Csr(ctx, n, n)
         A.lock(r, c, v)
         nnz = A.nnz
-        for _ in range(reps + 1):
-            ctx.sync()
-            t0 = time.perf_counter()
-            B = A.transpose() if kind == "transpose" else A.spgemm(A)
-            ctx.sync()
-            ms.append((time.perf_counter() - t0) * 1e3)
-            B.close()
+        names = [v for v in variants.split(",") if v in sg.SPGEMM_VARIANTS] if kind == "spgemm" else []
+        per = {}
+        for name in (names or ["auto"]):
+            vid = sg.SPGEMM_VARIANTS.get(name, sg.SPGEMM_AUTO)
+            ms = []
+            for _ in range(reps + 1):
+                ctx.sync()
+                t0 = time.perf_counter()
+                B = A.transpose() if kind == "transpose" else A.spgemm(A, vid)
+                ctx.sync()
+                ms.append((time.perf_counter() - t0) * 1e3)
+                B.close()
+            per[name] = [round(t, 3) for t in ms]
+        print(json.dumps({"profile_case": case, "n_rows": n, "nnz": nnz, "ms_per_call": per}))
+        return
     print(json.dumps({"profile_case": case, "n_rows": n, "nnz": nnz, "ms_per_call": [round(t, 3) for t in ms]}))
 
 
@@ -839,7 +943,7 @@ def run_profile_case(args):
     stream = torch.cuda.ExternalStream(ctx.stream)
     n, kind = PROFILE_CASES[args.profile_case]
     if kind in ("lock", "relock", "transpose", "spgemm", "batched", "add"):
-        run_profile_op(ctx, args.profile_case, n, kind, args.reps)
+        run_profile_op(ctx, args.profile_case, n, kind, args.reps, args.variants)
         return
     if kind == "zipf":
         r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
@@ -897,6 +1001,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-RHS section")
     ap.add_argument("--no-ops", action="store_true", help="skip the lock / transpose / SpGEMM section")
+    ap.add_argument("--no-selector", action="store_true", help="skip the selectors' held-out regret section")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)

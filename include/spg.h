@@ -60,9 +60,19 @@ enum spg_spmv_variant {
     SPG_SPMV_ADAPTIVE16 = 9, /* the same with 16 nonzeros per lane */
     SPG_SPMV_INTERLEAVED = 10, /* ADAPTIVE16's arithmetic over a copy of cols/vals stored
                                   lane-interleaved per 512-nonzero chunk, so every load is
-                                  one contiguous 512-byte warp access; the copy costs
-                                  12 B per nonzero of device memory while cached */
-    SPG_SPMV_N_VARIANTS = 11
+                                  one contiguous warp access; the copy costs 12 B per
+                                  nonzero of device memory while cached; 2-entry
+                                  sub-batches, 8 blocks of 256 threads per SM */
+    /* Tiles of the chunk kernels: the same variant's arithmetic and bits with
+     * another sub-batch depth (nonzeros whose loads and gathers a lane issues
+     * before their FMAs) and residency (blocks of 256 threads per SM). */
+    SPG_SPMV_INTERLEAVED_S4 = 11, /* INTERLEAVED, 4-entry sub-batches, 5 blocks per SM */
+    SPG_SPMV_INTERLEAVED_S8 = 12, /* INTERLEAVED, 8-entry sub-batches, 4 blocks per SM */
+    SPG_SPMV_ADAPTIVE16_S4 = 13,  /* ADAPTIVE16, 4-entry sub-batches, 6 blocks per SM
+                                     (ADAPTIVE16 itself: 8-entry, 4 blocks) */
+    SPG_SPMV_ADAPTIVE_S16 = 14,   /* ADAPTIVE, 16-entry sub-batches, 2 blocks per SM
+                                     (ADAPTIVE itself: 8-entry, 4 blocks) */
+    SPG_SPMV_N_VARIANTS = 15
 };
 
 typedef struct spg_ctx spg_ctx; /* one device + one stream + memory pool */
@@ -91,6 +101,21 @@ int spg_ctx_stream(spg_ctx *ctx, void **stream);
 /* Waits for the context stream; SPG_ERR_DEVICE_TIMEOUT if a kernel's bounded
  * wait gave up since the last check (the context stays usable). */
 int spg_ctx_sync(spg_ctx *ctx);
+/* Device time of operations that synchronise internally (lock, transpose,
+ * SpGEMM, addition, scaling: their output sizes are data-dependent). Between
+ * spg_ctx_timer_start and spg_ctx_timer_stop, every stretch of work on the
+ * context stream up to one of those synchronisations is timed with CUDA
+ * events and added up; the host round trips at the synchronisations are not
+ * counted. No Spira counterpart (a measurement aid). */
+int spg_ctx_timer_start(spg_ctx *ctx);
+int spg_ctx_timer_stop(spg_ctx *ctx, double *device_ms);
+/* Self-test of the device-side waits (SpGEMM's ordered scan of tile counts):
+ * runs one wait whose predecessor never publishes, bounded by wait_cycles SM
+ * clocks (1 .. 2^31). The kernel gives up, sets the context's status word
+ * and returns, so the next spg_ctx_sync reports SPG_ERR_DEVICE_TIMEOUT and
+ * the context stays usable; *gave_up = 1 when the wait gave up as designed.
+ * No Spira counterpart. */
+int spg_selftest_wait_timeout(spg_ctx *ctx, long long wait_cycles, int *gave_up);
 /* Bytes of the context's device memory pool (the device's default
  * stream-ordered pool, from which every device buffer of libspg comes) that
  * live buffers hold, and that the pool holds from the driver (freed buffers
@@ -342,8 +367,56 @@ int spg_transpose(spg_ctx *ctx, const spg_csr *A, spg_csr *AT);
  * is the left-to-right sum over ascending k of the rounded products
  * a_ik * b_kj from 0.0; exact-zero sums are dropped (serial/spgemm.hpp:12-53,
  * parallel/algorithms/spgemm.hpp:27-69). A.n_cols != B.n_rows gives
- * SPG_ERR_INVALID_ARGUMENT, an unlocked A or B SPG_ERR_LOGIC. */
+ * SPG_ERR_INVALID_ARGUMENT, an unlocked A or B SPG_ERR_LOGIC. The kernel
+ * path is SPG_SPGEMM_AUTO's choice (below); every path computes the same C. */
 int spg_spgemm(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, spg_csr *C);
+
+/* ---- SpGEMM variants and their choice ----------------------------------------
+ * No Spira counterpart: Spira has one SpGEMM code path (serial/spgemm.hpp:
+ * 28-48). These choose which of this engine's kernels computes it; C is the
+ * same bits whichever runs. */
+enum spg_spgemm_variant {
+    SPG_SPGEMM_AUTO = -1,        /* the context's policy, as for SpMV */
+    SPG_SPGEMM_ROWMERGE = 0,     /* a thread per row merges the row's B rows (k-way, by
+                                    column); rows with > 32 A entries or > 4096 products
+                                    go through expand-sort-compress; a compaction pass */
+    SPG_SPGEMM_ESC = 1,          /* expand every product, one global radix sort by
+                                    (row, column), left-to-right run sums */
+    SPG_SPGEMM_WARPSORT_64 = 2,  /* tiles of consecutive rows: a warp sorts each row's
+                                    (column, product) pairs in registers (bitonic, rows of
+                                    <= 64 products; heavier rows expand-sort-compress), a
+                                    thread per row sums the runs, each tile writes C in
+                                    place after an ordered scan of the tiles' counts;
+                                    tiles of <= 1024 products */
+    SPG_SPGEMM_WARPSORT_128 = 3, /* the same for rows of <= 128 products, 2048-product tiles */
+    SPG_SPGEMM_WARPSORT_256 = 4, /* the same for rows of <= 256 products, 4096-product tiles */
+    SPG_SPGEMM_N_VARIANTS = 5
+};
+/* C <- A * B with a given variant (SPG_SPGEMM_AUTO: as spg_spgemm). */
+int spg_spgemm_variant(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, spg_csr *C, int variant);
+/* The variant SPG_SPGEMM_AUTO resolves to for A * B. */
+int spg_spgemm_selected(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, int *variant);
+/* The 40 SpGEMM selector features of A * B (host array): 32-bin log2
+ * histogram of the products per row of A, then log sizes (rows, B's
+ * columns, nnz of A, products), mean / spread / maximum products per row and
+ * the mean A row length. */
+int spg_spgemm_features(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, float *features);
+/* Times every SpGEMM variant on A * B (median of `reps` runs after one
+ * warm-up, wall clock around the complete call: the calls synchronise):
+ * times_ms[SPG_SPGEMM_N_VARIANTS] (may be NULL) and the fastest in *best (may
+ * be NULL). */
+int spg_spgemm_autotune(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, int reps, float *times_ms, int *best);
+/* Installs a trained SpGEMM selector (same blob layout as spg_selector_load;
+ * output k predicts log(time of SpGEMM variant k / fastest time)); NULL
+ * removes it. The context loads spg_spgemm_selector.bin from beside the
+ * library (or $SPG_SPGEMM_SELECTOR_MODEL) when it is created. */
+int spg_spgemm_selector_load(spg_ctx *ctx, const float *blob, uint64_t n_floats, int n_outputs);
+/* Batched inference of the loaded SpGEMM selector on device features [B][40]. */
+int spg_spgemm_selector_predict(spg_ctx *ctx, const float *d_features, uint32_t B, float *d_out, void *stream);
+/* SPG_SPGEMM_AUTO's policy: SPG_POLICY_SELECTOR (the selector if loaded, else
+ * the autotuner), SPG_POLICY_AUTOTUNE, SPG_POLICY_FIXED (SPG_SPGEMM_WARPSORT_128
+ * without measuring). The choice is cached per (A, B) until either changes. */
+int spg_set_spgemm_policy(spg_ctx *ctx, int policy);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,10 @@ def orc():
         _orc.orc_spgemm_products.argtypes = [P, P]
         _orc.orc_spgemm_products.restype = C.c_uint64
         _orc.orc_transpose.argtypes = [P, P]
+        _orc.orc_spgemm_parallel.argtypes = [P, P, P, C.c_int, C.c_int]
+        _orc.orc_transpose_parallel.argtypes = [P, P, C.c_int]
+        _orc.orc_lock_parallel_time.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]
         _orc.orc_add.argtypes = [P, P, P]
         _orc.orc_scale.argtypes = [P, C.c_double, C.c_int, P]
         _orc.orc_row_sums.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
@@ -199,6 +203,44 @@ def spgemm(A, B, fused=False) -> Csr:
     rc = orc().orc_spgemm(C.byref(sa), C.byref(sb), C.byref(out), int(fused))
     assert rc == 0
     return _take(out, orc().orc_csr_free)
+
+
+def spgemm_parallel(A, B, n_threads: int, fused=False) -> Csr:
+    """parallel::algorithms::spgemm on t*n/T row partitions, one thread each."""
+    sa, ka = _as_c(A)
+    sb, kb = _as_c(B)
+    out = _OrcCsr()
+    rc = orc().orc_spgemm_parallel(C.byref(sa), C.byref(sb), C.byref(out), int(n_threads), int(fused))
+    assert rc == 0
+    return _take(out, orc().orc_csr_free)
+
+
+def transpose_parallel(A, n_threads: int) -> Csr:
+    """parallel::algorithms::transpose: each output partition scans all of A."""
+    sa, ka = _as_c(A)
+    out = _OrcCsr()
+    rc = orc().orc_transpose_parallel(C.byref(sa), C.byref(out), int(n_threads))
+    assert rc == 0
+    return _take(out, orc().orc_csr_free)
+
+
+def lock_parallel_time(n_rows: int, n_cols: int, epochs, n_threads: int):
+    """parallel_matrix::lock of each epoch on n_threads partitions: (wall
+    seconds per epoch, stored entries after the last)."""
+    keep = [(_arr(r, np.uint32), _arr(c, np.uint32), _arr(v, np.float64)) for r, c, v in epochs]
+    n = len(keep)
+    rp = (C.c_void_p * n)(*[k[0].ctypes.data for k in keep])
+    cp = (C.c_void_p * n)(*[k[1].ctypes.data for k in keep])
+    vp = (C.c_void_p * n)(*[k[2].ctypes.data for k in keep])
+    ms = np.array([len(k[0]) for k in keep], np.uint64)
+    secs = np.zeros(n, np.float64)
+    nnz = C.c_uint64()
+    rc = orc().orc_lock_parallel_time(n_rows, n_cols, int(n_threads), n, rp, cp, vp, ms.ctypes.data,
+                                      secs.ctypes.data, C.byref(nnz))
+    if rc == 3:
+        raise IndexError("oracle lock: index out of range")
+    assert rc == 0, rc
+    return secs, nnz.value
 
 
 def spgemm_products(A, B) -> int:

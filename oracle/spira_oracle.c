@@ -15,11 +15,13 @@
  * that Spira's compiled code may emit is written out as fma() and selected
  * by a `fused` flag, so results are identical on x86-64 and aarch64.
  */
+#define _POSIX_C_SOURCE 200809L /* clock_gettime under -std=c11 */
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #define ORC_OK 0
 #define ORC_ERR_ALLOC 4
@@ -534,4 +536,278 @@ void orc_partition(const uint64_t *off, uint64_t n_rows, uint64_t T, uint64_t *b
         }
         bounds[t] = lo < n_rows ? lo : n_rows;
     }
+}
+
+/* ------------------------------------------------------------------------
+ * Parallel forms, for the multi-core CPU baseline of lock, SpGEMM and
+ * transpose: parallel_matrix's static row partitions row_start = t*n/T
+ * (parallel_matrix.hpp:300-301), one pthread per partition.
+ * ---------------------------------------------------------------------- */
+static double orc_now(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+static uint64_t part_of(const uint64_t *bounds, int T, uint64_t r) {
+    int lo = 0, hi = T; /* last t with bounds[t] <= r */
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (bounds[mid] <= r) lo = mid;
+        else hi = mid;
+    }
+    return (uint64_t)lo;
+}
+
+/* lock(): parallel_matrix::lock (parallel_matrix.hpp:321-405) locks each
+ * partition's own matrix on its own thread. insert() already routed every
+ * triple to its partition's buffers (parallel_matrix.hpp:581-602), so that
+ * routing is done here before the clock starts. */
+typedef struct {
+    orc_csr part;
+    uint32_t *rows, *cols;
+    double *vals;
+    uint64_t m;
+    int rc;
+} orc_lock_part;
+
+static void *lock_worker(void *p) {
+    orc_lock_part *q = (orc_lock_part *)p;
+    q->rc = orc_lock(&q->part, q->rows, q->cols, q->vals, q->m);
+    return NULL;
+}
+
+/* Locks n_epochs epochs of staged inserts into an n_rows x n_cols matrix
+ * kept as T partitions; seconds[e] = wall time of epoch e's parallel lock;
+ * *nnz = stored entries after the last epoch. */
+int orc_lock_parallel_time(uint64_t n_rows, uint64_t n_cols, int T, int n_epochs, const uint32_t *const *rows,
+                           const uint32_t *const *cols, const double *const *vals, const uint64_t *ms,
+                           double *seconds, uint64_t *nnz) {
+    if (T < 1) T = 1;
+    uint64_t *bounds = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(T + 1));
+    orc_lock_part *parts = (orc_lock_part *)calloc((size_t)T, sizeof(orc_lock_part));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)T);
+    uint64_t *cnt = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)T);
+    if (!bounds || !parts || !th || !cnt) return ORC_ERR_ALLOC;
+    for (int t = 0; t <= T; ++t) bounds[t] = (uint64_t)t * n_rows / (uint64_t)T;
+    for (int t = 0; t < T; ++t) {
+        parts[t].part.n_rows = bounds[t + 1] - bounds[t];
+        parts[t].part.n_cols = n_cols;
+    }
+    int rc = ORC_OK;
+    for (int e = 0; e < n_epochs && rc == ORC_OK; ++e) {
+        const uint64_t m = ms[e];
+        for (int t = 0; t < T; ++t) cnt[t] = 0;
+        for (uint64_t i = 0; i < m; ++i) {
+            if ((uint64_t)rows[e][i] >= n_rows || (uint64_t)cols[e][i] >= n_cols) return ORC_ERR_RANGE;
+            cnt[part_of(bounds, T, rows[e][i])]++;
+        }
+        for (int t = 0; t < T; ++t) {
+            parts[t].rows = (uint32_t *)malloc((cnt[t] ? cnt[t] : 1) * sizeof(uint32_t));
+            parts[t].cols = (uint32_t *)malloc((cnt[t] ? cnt[t] : 1) * sizeof(uint32_t));
+            parts[t].vals = (double *)malloc((cnt[t] ? cnt[t] : 1) * sizeof(double));
+            if (!parts[t].rows || !parts[t].cols || !parts[t].vals) return ORC_ERR_ALLOC;
+            parts[t].m = 0;
+        }
+        for (uint64_t i = 0; i < m; ++i) { /* insertion order kept within each partition */
+            const uint64_t t = part_of(bounds, T, rows[e][i]);
+            orc_lock_part *q = &parts[t];
+            q->rows[q->m] = (uint32_t)(rows[e][i] - bounds[t]);
+            q->cols[q->m] = cols[e][i];
+            q->vals[q->m] = vals[e][i];
+            ++q->m;
+        }
+        const double t0 = orc_now();
+        for (int t = 1; t < T; ++t) pthread_create(&th[t], NULL, lock_worker, &parts[t]);
+        lock_worker(&parts[0]);
+        for (int t = 1; t < T; ++t) pthread_join(th[t], NULL);
+        seconds[e] = orc_now() - t0;
+        for (int t = 0; t < T; ++t) {
+            if (parts[t].rc != ORC_OK) rc = parts[t].rc;
+            free(parts[t].rows);
+            free(parts[t].cols);
+            free(parts[t].vals);
+        }
+    }
+    uint64_t total = 0;
+    for (int t = 0; t < T; ++t) {
+        total += parts[t].part.nnz;
+        orc_csr_free(&parts[t].part);
+    }
+    *nnz = total;
+    free(bounds);
+    free(parts);
+    free(th);
+    free(cnt);
+    return rc;
+}
+
+/* SpGEMM: parallel/algorithms/spgemm.hpp:27-69 — each partition's rows of A
+ * computed by its own thread (Gustavson, ascending k, drop zero sums, as
+ * orc_spgemm), then the partitions' rows assembled into C. */
+typedef struct {
+    const orc_csr *A, *B;
+    uint64_t r0, r1;
+    int fused;
+    orc_csr out; /* rows r0..r1-1 of C */
+    int rc;
+} orc_gemm_part;
+
+static void *gemm_worker(void *p) {
+    orc_gemm_part *q = (orc_gemm_part *)p;
+    orc_csr sub = *q->A;
+    sub.n_rows = q->r1 - q->r0;
+    sub.off = q->A->off + q->r0; /* offsets stay absolute: cols / vals are shared */
+    q->rc = orc_spgemm(&sub, q->B, &q->out, q->fused);
+    return NULL;
+}
+
+int orc_spgemm_parallel(const orc_csr *A, const orc_csr *B, orc_csr *C, int T, int fused) {
+    if (T < 1) T = 1;
+    orc_gemm_part *parts = (orc_gemm_part *)calloc((size_t)T, sizeof(orc_gemm_part));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)T);
+    if (!parts || !th) return ORC_ERR_ALLOC;
+    const uint64_t m = A->n_rows;
+    for (int t = 0; t < T; ++t) {
+        parts[t].A = A;
+        parts[t].B = B;
+        parts[t].r0 = (uint64_t)t * m / (uint64_t)T;
+        parts[t].r1 = (uint64_t)(t + 1) * m / (uint64_t)T;
+        parts[t].fused = fused;
+    }
+    for (int t = 1; t < T; ++t) pthread_create(&th[t], NULL, gemm_worker, &parts[t]);
+    gemm_worker(&parts[0]);
+    for (int t = 1; t < T; ++t) pthread_join(th[t], NULL);
+    uint64_t nnz = 0;
+    int rc = ORC_OK;
+    for (int t = 0; t < T; ++t) {
+        if (parts[t].rc != ORC_OK) rc = parts[t].rc;
+        nnz += parts[t].out.nnz;
+    }
+    uint64_t *off = (uint64_t *)malloc((m + 1) * sizeof(uint64_t));
+    uint32_t *cc = (uint32_t *)malloc((nnz ? nnz : 1) * sizeof(uint32_t));
+    double *cv = (double *)malloc((nnz ? nnz : 1) * sizeof(double));
+    if (!off || !cc || !cv) return ORC_ERR_ALLOC;
+    uint64_t base = 0;
+    off[0] = 0;
+    for (int t = 0; t < T; ++t) {
+        const orc_csr *o = &parts[t].out;
+        if (rc == ORC_OK) {
+            for (uint64_t r = 0; r < o->n_rows; ++r) off[parts[t].r0 + r + 1] = base + o->off[r + 1];
+            memcpy(cc + base, o->cols, o->nnz * sizeof(uint32_t));
+            memcpy(cv + base, o->vals, o->nnz * sizeof(double));
+            base += o->nnz;
+        }
+        orc_csr_free(&parts[t].out);
+    }
+    free(parts);
+    free(th);
+    C->n_rows = m;
+    C->n_cols = B->n_cols;
+    C->off = off;
+    C->cols = cc;
+    C->vals = cv;
+    C->nnz = nnz;
+    C->capacity = nnz;
+    return rc;
+}
+
+/* Transpose: parallel/algorithms/transpose.hpp:36-70 — output partition t
+ * (rows of A^T = columns of A in [c0, c1)) scans every entry of A in row
+ * order and keeps those of its columns (O(T nnz) reads, as Spira's); the
+ * partitions' rows are then assembled. Within an output row the source rows
+ * arrive ascending. */
+typedef struct {
+    const orc_csr *A;
+    uint64_t c0, c1;
+    uint64_t *off; /* c1 - c0 + 1, local */
+    uint32_t *tc;
+    double *tv;
+    int rc;
+} orc_tr_part;
+
+static void *tr_worker(void *p) {
+    orc_tr_part *q = (orc_tr_part *)p;
+    const orc_csr *A = q->A;
+    const uint64_t w = q->c1 - q->c0;
+    q->off = (uint64_t *)calloc(w + 1, sizeof(uint64_t));
+    uint64_t *cur = (uint64_t *)malloc((w + 1) * sizeof(uint64_t));
+    if (!q->off || !cur) {
+        q->rc = ORC_ERR_ALLOC;
+        return NULL;
+    }
+    for (uint64_t k = 0; k < A->nnz; ++k) {
+        const uint64_t c = A->cols[k];
+        if (c >= q->c0 && c < q->c1) q->off[c - q->c0 + 1]++;
+    }
+    for (uint64_t j = 0; j < w; ++j) q->off[j + 1] += q->off[j];
+    memcpy(cur, q->off, (w + 1) * sizeof(uint64_t));
+    const uint64_t n = q->off[w];
+    q->tc = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    q->tv = (double *)malloc((n ? n : 1) * sizeof(double));
+    if (!q->tc || !q->tv) {
+        q->rc = ORC_ERR_ALLOC;
+        free(cur);
+        return NULL;
+    }
+    for (uint64_t i = 0; i < A->n_rows; ++i)
+        for (uint64_t k = A->off[i]; k < A->off[i + 1]; ++k) {
+            const uint64_t c = A->cols[k];
+            if (c >= q->c0 && c < q->c1) {
+                const uint64_t p2 = cur[c - q->c0]++;
+                q->tc[p2] = (uint32_t)i;
+                q->tv[p2] = A->vals[k];
+            }
+        }
+    free(cur);
+    q->rc = ORC_OK;
+    return NULL;
+}
+
+int orc_transpose_parallel(const orc_csr *A, orc_csr *Tr, int T) {
+    if (T < 1) T = 1;
+    orc_tr_part *parts = (orc_tr_part *)calloc((size_t)T, sizeof(orc_tr_part));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)T);
+    if (!parts || !th) return ORC_ERR_ALLOC;
+    const uint64_t c = A->n_cols;
+    for (int t = 0; t < T; ++t) {
+        parts[t].A = A;
+        parts[t].c0 = (uint64_t)t * c / (uint64_t)T;
+        parts[t].c1 = (uint64_t)(t + 1) * c / (uint64_t)T;
+    }
+    for (int t = 1; t < T; ++t) pthread_create(&th[t], NULL, tr_worker, &parts[t]);
+    tr_worker(&parts[0]);
+    for (int t = 1; t < T; ++t) pthread_join(th[t], NULL);
+    int rc = ORC_OK;
+    for (int t = 0; t < T; ++t)
+        if (parts[t].rc != ORC_OK) rc = parts[t].rc;
+    uint64_t *off = (uint64_t *)malloc((c + 1) * sizeof(uint64_t));
+    uint32_t *tc = (uint32_t *)malloc((A->nnz ? A->nnz : 1) * sizeof(uint32_t));
+    double *tv = (double *)malloc((A->nnz ? A->nnz : 1) * sizeof(double));
+    if (!off || !tc || !tv) return ORC_ERR_ALLOC;
+    uint64_t base = 0;
+    off[0] = 0;
+    for (int t = 0; t < T; ++t) {
+        orc_tr_part *q = &parts[t];
+        if (rc == ORC_OK) {
+            const uint64_t w = q->c1 - q->c0, n = q->off[w];
+            for (uint64_t j = 0; j < w; ++j) off[q->c0 + j + 1] = base + q->off[j + 1];
+            memcpy(tc + base, q->tc, n * sizeof(uint32_t));
+            memcpy(tv + base, q->tv, n * sizeof(double));
+            base += n;
+        }
+        free(q->off);
+        free(q->tc);
+        free(q->tv);
+    }
+    free(parts);
+    free(th);
+    Tr->n_rows = c;
+    Tr->n_cols = A->n_rows;
+    Tr->off = off;
+    Tr->cols = tc;
+    Tr->vals = tv;
+    Tr->nnz = A->nnz;
+    Tr->capacity = A->nnz;
+    return rc;
 }

@@ -21,11 +21,18 @@ LIB_PATH = _PKG / "libspg.so"
 
 SPMV_AUTO, SPMV_SCALAR, SPMV_VECTOR2, SPMV_VECTOR4, SPMV_VECTOR8, SPMV_VECTOR16, SPMV_VECTOR32, \
     SPMV_STREAM, SPMV_MERGE, SPMV_ADAPTIVE, SPMV_ADAPTIVE16, SPMV_INTERLEAVED = -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
+SPMV_INTERLEAVED_S4, SPMV_INTERLEAVED_S8, SPMV_ADAPTIVE16_S4, SPMV_ADAPTIVE_S16 = 11, 12, 13, 14
+# (variant, tile) candidates: the chunk kernels' tiles (sub-batch depth x
+# blocks per SM) compute their base variant's bits
 SPMV_VARIANTS = {
     "scalar": 0, "vector2": 1, "vector4": 2, "vector8": 3, "vector16": 4, "vector32": 5,
     "stream": 6, "merge": 7, "adaptive": 8, "adaptive16": 9, "interleaved": 10,
+    "interleaved_s4": 11, "interleaved_s8": 12, "adaptive16_s4": 13, "adaptive_s16": 14,
 }
 SPMV_NAMES = {v: k for k, v in SPMV_VARIANTS.items()}
+SPGEMM_AUTO = -1
+SPGEMM_VARIANTS = {"rowmerge": 0, "esc": 1, "warpsort_64": 2, "warpsort_128": 3, "warpsort_256": 4}
+SPGEMM_NAMES = {v: k for k, v in SPGEMM_VARIANTS.items()}
 
 CsrHost = namedtuple("CsrHost", "n_rows n_cols off cols vals capacity")
 
@@ -93,6 +100,9 @@ _SIGS = [
     ("spg_ctx_stream", _I, [_P, C.POINTER(_P)]),
     ("spg_ctx_sync", _I, [_P]),
     ("spg_ctx_pool_used", _I, [_P, C.POINTER(_U64), C.POINTER(_U64)]),
+    ("spg_selftest_wait_timeout", _I, [_P, C.c_longlong, C.POINTER(_I)]),
+    ("spg_ctx_timer_start", _I, [_P]),
+    ("spg_ctx_timer_stop", _I, [_P, C.POINTER(C.c_double)]),
     ("spg_csr_create", _I, [_P, _U64, _U64, C.POINTER(_P)]),
     ("spg_csr_destroy", _I, [_P]),
     ("spg_csr_info_get", _I, [_P, C.POINTER(_Info)]),
@@ -142,6 +152,13 @@ _SIGS = [
     ("spg_csr_file_info", _I, [C.c_char_p, C.POINTER(_U64), C.POINTER(_U64), C.POINTER(_U64)]),
     ("spg_transpose", _I, [_P, _P, _P]),
     ("spg_spgemm", _I, [_P, _P, _P, _P]),
+    ("spg_spgemm_variant", _I, [_P, _P, _P, _P, _I]),
+    ("spg_spgemm_selected", _I, [_P, _P, _P, C.POINTER(_I)]),
+    ("spg_spgemm_features", _I, [_P, _P, _P, _P]),
+    ("spg_spgemm_autotune", _I, [_P, _P, _P, _I, _P, C.POINTER(_I)]),
+    ("spg_spgemm_selector_load", _I, [_P, _P, _U64, _I]),
+    ("spg_spgemm_selector_predict", _I, [_P, _P, _U32, _P, _P]),
+    ("spg_set_spgemm_policy", _I, [_P, _I]),
     # spg_gen.h
     ("spg_gen_draw", _I, [_P, _U64, _U64, _U64, _U64, _I, _U64, _P]),
     ("spg_gen_expand_rows", _I, [_P, _P, _U64, _P, C.POINTER(_U64)]),
@@ -217,6 +234,19 @@ class Context:
     def sync(self):
         _check(lib().spg_ctx_sync(self.h))
 
+    def device_ms(self, fn) -> float:
+        """Runs fn() and returns the device time of the work it put on the
+        context stream, host round trips at the operations' internal
+        synchronisations excluded (spg_ctx_timer_start / _stop)."""
+        _check(lib().spg_ctx_timer_start(self.h))
+        try:
+            fn()
+        finally:
+            ms = C.c_double()
+            st = lib().spg_ctx_timer_stop(self.h, C.byref(ms))
+        _check(st)
+        return ms.value
+
     def pool_used(self):
         """(bytes live buffers hold, bytes the pool holds) of the context's
         device memory pool."""
@@ -226,6 +256,17 @@ class Context:
 
     def set_spmv_policy(self, policy: int):
         _check(lib().spg_set_spmv_policy(self.h, policy))
+
+    def set_spgemm_policy(self, policy: int):
+        _check(lib().spg_set_spgemm_policy(self.h, policy))
+
+    def load_spgemm_selector(self, blob, n_outputs: int):
+        """Install an SpGEMM selector blob (numpy float32); None removes it."""
+        if blob is None:
+            _check(lib().spg_spgemm_selector_load(self.h, None, 0, 0))
+            return
+        blob = np.ascontiguousarray(blob, dtype=np.float32)
+        _check(lib().spg_spgemm_selector_load(self.h, _ptr(blob), len(blob), n_outputs))
 
     def load_selector(self, blob, n_outputs: int):
         """Install a selector blob (numpy float32) for SPMV_AUTO; None removes it."""
@@ -399,11 +440,32 @@ class Csr:
         _check(lib().spg_transpose(self.ctx.h, self.h, T.h))
         return T
 
-    def spgemm(self, B: "Csr") -> "Csr":
-        """A new device matrix holding self * B."""
+    def spgemm(self, B: "Csr", variant: int = SPGEMM_AUTO) -> "Csr":
+        """A new device matrix holding self * B (SPGEMM_AUTO: the context's
+        policy picks the kernel path; every path gives the same C)."""
         Cm = Csr(self.ctx, 0, 0)
-        _check(lib().spg_spgemm(self.ctx.h, self.h, B.h, Cm.h))
+        if variant == SPGEMM_AUTO:
+            _check(lib().spg_spgemm(self.ctx.h, self.h, B.h, Cm.h))
+        else:
+            _check(lib().spg_spgemm_variant(self.ctx.h, self.h, B.h, Cm.h, variant))
         return Cm
+
+    def spgemm_selected(self, B: "Csr") -> int:
+        v = C.c_int()
+        _check(lib().spg_spgemm_selected(self.ctx.h, self.h, B.h, C.byref(v)))
+        return v.value
+
+    def spgemm_features(self, B: "Csr") -> np.ndarray:
+        f = np.empty(N_FEATURES, np.float32)
+        _check(lib().spg_spgemm_features(self.ctx.h, self.h, B.h, _ptr(f)))
+        return f
+
+    def spgemm_autotune(self, B: "Csr", reps: int = 3):
+        """(times_ms per SpGEMM variant, fastest variant)."""
+        t = np.empty(len(SPGEMM_VARIANTS), np.float32)
+        b = C.c_int()
+        _check(lib().spg_spgemm_autotune(self.ctx.h, self.h, B.h, reps, _ptr(t), C.byref(b)))
+        return t, b.value
 
     def add(self, B: "Csr") -> "Csr":
         """A new device matrix holding self + B (MatrixAddition)."""

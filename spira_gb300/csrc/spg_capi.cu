@@ -24,6 +24,19 @@ int set_error(int code, const char *fmt, ...) {
 
 void clear_error() { g_last_error.clear(); }
 
+int Ctx::phase_sync(cudaStream_t s) {
+    const bool timed = timer_on && s == stream;
+    if (timed) SPG_CUDA_TRY(cudaEventRecord(timer_ev[1], s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (timed) {
+        float ms = 0.0f;
+        SPG_CUDA_TRY(cudaEventElapsedTime(&ms, timer_ev[0], timer_ev[1]));
+        timer_ms += ms;
+        SPG_CUDA_TRY(cudaEventRecord(timer_ev[0], s));  // the next phase starts with the next work
+    }
+    return SPG_OK;
+}
+
 int Ctx::ensure_pinned(size_t bytes) {
     if (pinned_bytes >= bytes) return SPG_OK;
     if (pinned) cudaFreeHost(pinned);
@@ -161,6 +174,7 @@ int spg_ctx_destroy(spg_ctx *c) {
     for (Csr *A : c->live_csrs) A->orphan();
     c->live_csrs.clear();
     c->model.release();
+    c->gemm_model.release();
     c->xbuf.release();
     c->ybuf.release();
     cudaStreamSynchronize(c->stream);
@@ -172,6 +186,8 @@ int spg_ctx_destroy(spg_ctx *c) {
         if (c->host_events[i]) cudaEventDestroy(c->host_events[i]);
         if (c->upload_events[i]) cudaEventDestroy(c->upload_events[i]);
     }
+    for (cudaEvent_t e : c->timer_ev)
+        if (e) cudaEventDestroy(e);
     c->drop_multi();
     for (int l = 0; l < Ctx::MULTI_MAX; ++l) {
         for (cudaStream_t &st : c->multi_stream[l])
@@ -189,6 +205,29 @@ int spg_ctx_destroy(spg_ctx *c) {
 int spg_ctx_stream(spg_ctx *c, void **stream) {
     if (!c || !stream) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_stream: null argument");
     *stream = c->stream;
+    return SPG_OK;
+}
+
+int spg_ctx_timer_start(spg_ctx *c) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_timer_start: null context");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    for (cudaEvent_t &e : c->timer_ev)
+        if (!e) SPG_CUDA_TRY(cudaEventCreate(&e));
+    SPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->timer_ms = 0.0;
+    c->timer_on = true;
+    SPG_CUDA_TRY(cudaEventRecord(c->timer_ev[0], c->stream));
+    return SPG_OK;
+}
+
+int spg_ctx_timer_stop(spg_ctx *c, double *device_ms) {
+    if (!c || !device_ms) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_ctx_timer_stop: null argument");
+    if (!c->timer_on) return set_error(SPG_ERR_LOGIC, "spg_ctx_timer_stop: the timer is not running");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    const int rc = c->phase_sync(c->stream);
+    c->timer_on = false;
+    SPG_TRY(rc);
+    *device_ms = c->timer_ms;
     return SPG_OK;
 }
 
@@ -471,8 +510,7 @@ static int spmv_host_impl(spg_ctx *c, const spg_csr *Ac, const double *x, uint64
                            // 2 and 8 blocks measured slower (per-block launch and tail costs)
     static_assert(NB + 1 <= Ctx::N_HOST_EVENTS - 3, "a stage event per block, plus fork, join and ready");
     const bool row_parallel = variant == SPG_SPMV_SCALAR || (variant >= SPG_SPMV_VECTOR2 && variant <= SPG_SPMV_VECTOR32);
-    const bool adaptive =
-        variant == SPG_SPMV_ADAPTIVE || variant == SPG_SPMV_ADAPTIVE16 || variant == SPG_SPMV_INTERLEAVED;
+    const bool adaptive = spmv_is_seg(variant);
     std::vector<uint64_t> rows;
     if (A->nnz >= PIPELINE_MIN_NNZ && y_len && (row_parallel || adaptive)) {
         if (row_parallel) {
@@ -723,7 +761,7 @@ int spg_spmv_host_multi(spg_ctx *c, uint32_t n, const spg_csr *const *mats, cons
         p.dy = A->stage_y.as<double>();
         p.variant = v;
         p.row_parallel = v == SPG_SPMV_SCALAR || (v >= SPG_SPMV_VECTOR2 && v <= SPG_SPMV_VECTOR32);
-        const bool adaptive = v == SPG_SPMV_ADAPTIVE || v == SPG_SPMV_ADAPTIVE16 || v == SPG_SPMV_INTERLEAVED;
+        const bool adaptive = spmv_is_seg(v);
         constexpr uint64_t PIPELINE_MIN_NNZ = 4u << 20;
         constexpr int NB = 4;
         static_assert(NB + 1 <= Ctx::N_HOST_EVENTS - 1, "a stage event per block, plus the join event");
@@ -806,19 +844,17 @@ int spg_spmv_launches(spg_ctx *c, const spg_csr *Ac, int variant, int *n) {
         case SPG_SPMV_MERGE:
             *n = 2;
             break;
-        case SPG_SPMV_ADAPTIVE:
-        case SPG_SPMV_ADAPTIVE16:
-        case SPG_SPMV_INTERLEAVED: {
-            SPG_TRY(build_adaptive_plan(c, A, variant, c->stream));
-            const SpmvPlan &P = adaptive_plan_of(A, variant);
-            *n = (P.n_items ? 2 : 0) + (P.count1 ? 1 : 0);
-            break;
-        }
         case SPG_SPMV_STREAM:
             *n = 1;
             break;
         default:
-            *n = 1;
+            if (spmv_is_seg(variant)) {
+                SPG_TRY(build_adaptive_plan(c, A, variant, c->stream));
+                const SpmvPlan &P = adaptive_plan_of(A, variant);
+                *n = (P.n_items ? 2 : 0) + (P.count1 ? 1 : 0);
+            } else {
+                *n = 1;
+            }
     }
     return SPG_OK;
 }

@@ -149,6 +149,20 @@ struct Ctx {
     int spmv_policy = SPG_POLICY_SELECTOR;
     DevBuf model;  // FP32 selector blob
     int model_k = 0;
+    // The same for SpGEMM.
+    int spgemm_policy = SPG_POLICY_SELECTOR;
+    DevBuf gemm_model;
+    int gemm_model_k = 0;
+    // Device-time accounting of operations that synchronise internally
+    // (spg_ctx_timer_start / _stop): each stretch of work on the context
+    // stream between two host synchronisations is one phase, timed by an
+    // event pair; the host round trips between phases are not counted.
+    bool timer_on = false;
+    double timer_ms = 0.0;
+    cudaEvent_t timer_ev[2] = {nullptr, nullptr};
+    // Waits for `s` (the operations' synchronisation point); closes and opens
+    // a timed phase when the timer runs on this stream.
+    int phase_sync(cudaStream_t s);
 };
 
 struct Csr {
@@ -167,6 +181,10 @@ struct Csr {
     bool stats_valid = false;
     uint64_t max_row = 0;
     int selected_spmv = -1;
+    // SpGEMM variant chosen for this matrix times gemm_sel_b (at its epoch).
+    int gemm_selected = -1;
+    const Csr *gemm_sel_b = nullptr;
+    uint64_t gemm_sel_b_epoch = 0;
     SpmvPlan plan_stream, plan_merge, plan_adaptive, plan_inter;
     // For the host-buffer SpMV of row-parallel variants: the largest column
     // each of host_reach.size() equal row blocks reads (-1: empty block), so a
@@ -202,6 +220,8 @@ struct Csr {
         epoch = next_epoch();
         stats_valid = false;
         selected_spmv = -1;
+        gemm_selected = -1;
+        gemm_sel_b = nullptr;
         plan_stream = SpmvPlan{};
         plan_merge = SpmvPlan{};
         plan_adaptive = SpmvPlan{};
@@ -296,6 +316,21 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
                       uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s);
 
+// SpGEMM pieces shared by its variants (spg_spgemm.cu, spg_spgemm_sort.cu).
+// Expand - sort - compress output: kept entries in (row, column) order.
+struct EscOut {
+    DevBuf crow, ccol, cval;
+    uint64_t n = 0;
+};
+int spgemm_esc(Ctx *c, const Csr *A, const Csr *B, const uint64_t *hp, uint64_t HP, int rbits, int cbits,
+               EscOut *out, cudaStream_t s);
+void spgemm_install(Csr *Cm, uint64_t m, uint64_t n, DevBuf &&off, DevBuf &&cols, DevBuf &&vals, uint64_t nnz);
+uint64_t read_u64(Ctx *c, const uint64_t *d, cudaStream_t s, int *rc);
+int spgemm_warpsort(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cudaStream_t s);
+int spgemm_run(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cudaStream_t s);
+// SPG_SPGEMM_AUTO resolved by the context's policy (spg_tune.cu).
+int spgemm_resolve_auto(Ctx *c, const Csr *A, const Csr *B, int *variant);
+
 // CSR helpers used by several ops (spg_lock.cu).
 int csr_alloc(Csr *A, uint64_t capacity, cudaStream_t s);
 
@@ -332,9 +367,30 @@ int csr_max_row(Ctx *c, Csr *A, cudaStream_t s, bool *known);
 // enqueues work (plans synchronise: callers that record a CUDA graph call it
 // before the recording).
 int spmv_prepare(Ctx *c, Csr *A, int variant, cudaStream_t s);
-// The cached plan slot of one of those variants.
+// Shape of a chunk-kernel variant (ADAPTIVE, ADAPTIVE16, INTERLEAVED and
+// their tiles): nonzeros per lane, sub-batch depth, interleaved copy, blocks
+// of 256 threads per SM. items == 0 for every other variant.
+struct SegShape {
+    int items, sub;
+    bool inter;
+    int minb;
+};
+inline SegShape seg_shape(int variant) {
+    switch (variant) {
+        case SPG_SPMV_ADAPTIVE: return {32, 8, false, 4};
+        case SPG_SPMV_ADAPTIVE16: return {16, 8, false, 4};
+        case SPG_SPMV_INTERLEAVED: return {16, 2, true, 8};
+        case SPG_SPMV_INTERLEAVED_S4: return {16, 4, true, 5};
+        case SPG_SPMV_INTERLEAVED_S8: return {16, 8, true, 4};
+        case SPG_SPMV_ADAPTIVE16_S4: return {16, 4, false, 6};
+        case SPG_SPMV_ADAPTIVE_S16: return {32, 16, false, 2};
+        default: return {0, 0, false, 0};
+    }
+}
+inline bool spmv_is_seg(int variant) { return seg_shape(variant).items != 0; }
+// The cached plan slot of one of those variants (tiles share their base's).
 inline SpmvPlan &adaptive_plan_of(Csr *A, int variant) {
-    return variant == SPG_SPMV_INTERLEAVED ? A->plan_inter : A->plan_adaptive;
+    return seg_shape(variant).inter ? A->plan_inter : A->plan_adaptive;
 }
 
 }  // namespace spg

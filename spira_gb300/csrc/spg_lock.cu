@@ -587,7 +587,7 @@ int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, ui
         keys_descent<<<g, LB, 0, s>>>(keys.as<uint64_t>(), m, cbits, flag.as<unsigned>());
         SPG_LAUNCH_CHECK();
         SPG_CUDA_TRY(cudaMemcpyAsync(f, flag.ptr, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(c->phase_sync(s));
     }
     if (!f[0]) return make_keys();  // already sorted: the keys in input order
     if (!f[1]) {  // the row-grouped sort reads rows and columns directly
@@ -622,7 +622,7 @@ int sort_dedup(Ctx *c, const uint32_t *rows, const uint32_t *cols, const double 
     SPG_TRY(exclusive_scan_u64(c, pos.as<uint64_t>(), m, pos.as<uint64_t>() + m, s));
     uint64_t u = 0;
     SPG_CUDA_TRY(cudaMemcpyAsync(&u, pos.as<uint64_t>() + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     D.u = u;
     SPG_TRY(D.row.alloc(u * sizeof(uint32_t), s));
     SPG_TRY(D.col.alloc(u * sizeof(uint32_t), s));
@@ -664,7 +664,7 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         SPG_TRY(launch_row_offsets(c, rows, m, n, new_off.as<uint64_t>(), s));
         unsigned hz = 1;
         SPG_CUDA_TRY(cudaMemcpyAsync(&hz, zero.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(c->phase_sync(s));
         if (!hz) {
             A->invalidate_derived();
             A->off = std::move(new_off);
@@ -690,7 +690,7 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         SPG_LAUNCH_CHECK();
         SPG_TRY(exclusive_scan_u64(c, pos.as<uint64_t>(), tiles, pos.as<uint64_t>() + tiles, s));
         SPG_CUDA_TRY(cudaMemcpyAsync(&nnz, pos.as<uint64_t>() + tiles, 8, cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(c->phase_sync(s));
         SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
         SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
         SPG_TRY(orow.alloc((nnz ? nnz : 1) * sizeof(uint32_t), s));
@@ -712,7 +712,7 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
     A->capacity = nnz;  // build_csr: exact
     A->built = true;
     A->may_have_zeros = false;
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     return SPG_OK;
 }
 
@@ -737,7 +737,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
         SPG_LAUNCH_CHECK();
         unsigned h[5] = {0u, 0u, 1u, 1u, 1u};
         SPG_CUDA_TRY(cudaMemcpyAsync(h, stats.ptr, 5 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(c->phase_sync(s));
         if ((uint64_t)h[0] >= A->n_rows)
             return set_error(SPG_ERR_OUT_OF_RANGE, "spira::matrix: row_index out of range (%u >= %llu)", h[0],
                              (unsigned long long)A->n_rows);
@@ -770,7 +770,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
         SPG_TRY(exclusive_scan_u64(c, zpos.as<uint64_t>(), A->nnz, zpos.as<uint64_t>() + A->nnz, s));
         uint64_t nz = 0;
         SPG_CUDA_TRY(cudaMemcpyAsync(&nz, zpos.as<uint64_t>() + A->nnz, 8, cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(c->phase_sync(s));
         if (nz) {
             const uint64_t m2 = nz + D.u;
             DevBuf r2, c2, v2;
@@ -817,7 +817,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     SPG_TRY(exclusive_scan_u64(c, new_off.as<uint64_t>(), n + 1, nullptr, s));
     uint64_t new_nnz = 0;
     SPG_CUDA_TRY(cudaMemcpyAsync(&new_nnz, new_off.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
 
     uint64_t cap;
     if (!has_old) {
@@ -855,7 +855,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     A->capacity = cap;
     A->built = true;
     // Zeros of dirty rows were consumed; clean rows may still hold loaded zeros.
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     return SPG_OK;
 }
 

@@ -417,10 +417,9 @@ __global__ void partition_kernel(const uint64_t *__restrict__ off, uint64_t n_ro
     bounds[t] = lo < n_rows ? lo : n_rows;
 }
 
-int read_word(const uint64_t *d, cudaStream_t s, uint64_t *h) {
+int read_word(Ctx *c, const uint64_t *d, cudaStream_t s, uint64_t *h) {
     SPG_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
-    return SPG_OK;
+    return c->phase_sync(s);
 }
 
 // Installs (off, cols, vals, nnz) as the CSR of C; capacity defaults to nnz
@@ -465,7 +464,7 @@ int add_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
                                                         n, off.as<uint64_t>());
     SPG_LAUNCH_CHECK();
     uint64_t nnz = 0;
-    SPG_TRY(read_word(off.as<uint64_t>() + n, s, &nnz));
+    SPG_TRY(read_word(c, off.as<uint64_t>() + n, s, &nnz));
     SPG_TRY(cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
     if (na)
@@ -478,7 +477,7 @@ int add_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
                                                                 pb.as<uint64_t>(), cols.as<uint32_t>(),
                                                                 vals.as<double>());
     SPG_LAUNCH_CHECK();
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     install(Cm, n, A->n_cols, off, cols, vals, nnz);
     return SPG_OK;
 }
@@ -512,7 +511,7 @@ int scale_impl(Ctx *c, Csr *A, Csr *Cm, double sc, int divide, cudaStream_t s) {
                                                          zc.as<unsigned long long>());
     SPG_LAUNCH_CHECK();
     uint64_t zeros = 0;
-    SPG_TRY(read_word(zc.as<uint64_t>(), s, &zeros));
+    SPG_TRY(read_word(c, zc.as<uint64_t>(), s, &zeros));
     if (zeros == 0) {
         if (same_arrays) {
             A->invalidate_derived();  // cached plans hold copies of the values
@@ -523,7 +522,7 @@ int scale_impl(Ctx *c, Csr *A, Csr *Cm, double sc, int divide, cudaStream_t s) {
         SPG_CUDA_TRY(cudaMemcpyAsync(off.ptr, A->d_off(), (n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
         if (m)
             SPG_CUDA_TRY(cudaMemcpyAsync(cols.ptr, A->d_cols(), m * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        SPG_TRY(c->phase_sync(s));
         install(Cm, n, A->n_cols, off, cols, vals, m, out_cap);
         return SPG_OK;
     }
@@ -544,7 +543,7 @@ int scale_impl(Ctx *c, Csr *A, Csr *Cm, double sc, int divide, cudaStream_t s) {
     compact_entries<<<grid_for(m, OB, cap), OB, 0, s>>>(A->d_cols(), scaled, m, keep.as<uint64_t>(),
                                                         ncols.as<uint32_t>(), nvals.as<double>());
     SPG_LAUNCH_CHECK();
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     install(Cm, n, A->n_cols, off, ncols, nvals, nnz, out_cap);
     return SPG_OK;
 }

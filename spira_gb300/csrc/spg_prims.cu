@@ -582,7 +582,7 @@ int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const 
     SPG_LAUNCH_CHECK();
     unsigned h[3] = {1u, 0u, 0u};
     SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     if (h[0]) return SPG_OK;
     constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL, TS_SLICE_SMALL>);
     constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX, TS_SLICE_LARGE>);
@@ -603,7 +603,7 @@ int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const 
         SPG_LAUNCH_CHECK();
     }
     SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     *done = h[0] == 0;
     return SPG_OK;
 }

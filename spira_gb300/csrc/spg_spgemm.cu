@@ -7,23 +7,34 @@
 // the left-to-right sum over ascending k of the rounded products, starting
 // from 0.0, and exact-zero sums are dropped.
 //
-// GPU formulation. Products per row of A are counted and scanned; every row
-// owns a scratch region of its product count. Two paths fill the regions:
+// GPU formulation. Products per row of A are counted and scanned. Three
+// variants compute the same C (the autotuner and the learned selector choose
+// among them, spg_tune.cu):
 //
-//   light rows (at most MG_RMAX entries in A's row and MG_PMAX products):
-//   one thread merges the row's B rows (each sorted by column) as a k-way
-//   merge on the column, taking equal columns in ascending A-entry order, so
-//   every C(i, j) is summed in Spira's order; no global sort at all.
+//   SPG_SPGEMM_ROWMERGE: every row owns a scratch region of its product
+//   count. Light rows (at most MG_RMAX entries in A's row and MG_PMAX
+//   products): one thread merges the row's B rows (each sorted by column) as
+//   a k-way merge on the column, taking equal columns in ascending A-entry
+//   order, so every C(i, j) is summed in Spira's order. Heavy rows go through
+//   expand - sort - compress (below). A final pass compacts the regions.
 //
-//   heavy rows (expand - sort - compress): expand the row's products (key =
-//   i << cbits | j) in (row, A-entry, B-entry) order, stable radix sort with
-//   the product index as payload (equal (i, j) keep ascending k), sum each
-//   run left to right.
+//   SPG_SPGEMM_ESC: expand - sort - compress for every row: expand the
+//   products (key = i << cbits | j) in (row, A-entry, B-entry) order, stable
+//   radix sort with the product index as payload (equal (i, j) keep
+//   ascending k), sum each run left to right; the kept runs are C in order.
 //
-// Both use separate round-to-nearest multiply and add (__dmul_rn /
-// __dadd_rn, never contracted) from 0.0 and drop exact-zero sums; a final
-// pass compacts the regions into C. Values match Spira built without FMA
-// contraction (its x86-64 build) bit for bit; structure is exact.
+//   SPG_SPGEMM_WARPSORT_*: tiles of consecutive rows, a warp bitonic sort of
+//   each row's (column, product) pairs in registers, a thread per row summing
+//   the runs, and the output written in place through an ordered scan
+//   (spg_spgemm_sort.cu).
+//
+// All use separate round-to-nearest multiply and add (__dmul_rn / __dadd_rn,
+// never contracted) and drop exact-zero sums. Structure is exact; values
+// match, bit for bit, Spira built for a target without FMA instructions
+// (generic x86-64, as the oracle's recipe builds it). A Spira build that
+// contracts acc[j] += a * b into fma(a, b, acc) — GCC's default
+// -ffp-contract=fast on aarch64, or x86-64 with FMA enabled — differs in the
+// last bits; the tests bound the difference to that order within 1e-12.
 #include "spg_internal.cuh"
 
 namespace spg {
@@ -51,7 +62,8 @@ constexpr uint64_t MG_PMAX = 4096;  // and at most this many products
 
 __device__ __forceinline__ bool mg_light(uint64_t r, uint64_t p) { return r <= MG_RMAX && p <= MG_PMAX; }
 
-// Product counts of the heavy rows only (0 for light rows); entry m is 0.
+// Product counts of the rows the row merge leaves to expand - sort -
+// compress (0 for light rows); entry m is 0.
 __global__ void sg_heavy_products(const uint64_t *__restrict__ aoff, const uint64_t *__restrict__ pofs, uint64_t m,
                                   uint64_t *__restrict__ hp) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= m; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -88,7 +100,9 @@ sg_merge_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ ac
         return;
     }
     // per list: cursor, entries left, and the head's column and value (loaded
-    // one step ahead, so a step waits for at most one round of loads)
+    // one step ahead, so a step waits for at most one round of loads; a
+    // second register stage for the entry after the head measured slower:
+    // 124 registers, four blocks per SM instead of five)
     constexpr bool PF = R <= MG_RSMALL;  // head values in registers (the wide version would spill)
     uint64_t cur[R];
     uint32_t left[R], head[R];
@@ -290,44 +304,45 @@ __global__ void sg_write(const uint64_t *__restrict__ begin, const uint64_t *__r
     }
 }
 
-uint64_t read_u64(const uint64_t *d, cudaStream_t s, int *rc) {
+
+}  // namespace
+
+// One uint64 read back from the device (synchronises the stream).
+uint64_t read_u64(Ctx *c, const uint64_t *d, cudaStream_t s, int *rc) {
     uint64_t h = 0;
-    cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) *rc = set_error(SPG_ERR_CUDA, "spgemm: %s", cudaGetErrorString(e));
+    else *rc = c->phase_sync(s);
     return h;
 }
 
-// Expand - sort - compress for the rows the merge kernels leave (more than
-// MG_RMAX A entries or more than MG_PMAX products); results go to the rows'
-// scratch regions and counts.
-int spgemm_heavy_rows(Ctx *c, const Csr *A, const Csr *B, const uint64_t *pofs, uint32_t *tcols, double *tvals,
-                      uint64_t *rowcnt, int rbits, int cbits, cudaStream_t s) {
+// Expand - sort - compress over the rows whose entries of `hp` (the scanned
+// product counts of the selected rows, 0 for the others; hp[m] = HP, their
+// total) select: products in (row, A entry, B entry) order, a stable radix
+// sort by (row, column) carrying the product index, each run summed left to
+// right from 0.0, kept sums compacted in (row, column) order into out.
+int spgemm_esc(Ctx *c, const Csr *A, const Csr *B, const uint64_t *hp, uint64_t HP, int rbits, int cbits,
+               EscOut *out, cudaStream_t s) {
     const uint64_t m = A->n_rows;
     const unsigned gmax = (unsigned)c->n_sms * 32;
     int rc = SPG_OK;
-    DevBuf hp;
-    SPG_TRY(hp.alloc((m + 1) * sizeof(uint64_t), s));
-    sg_heavy_products<<<grid_for(m + 1, GB, gmax), GB, 0, s>>>(A->d_off(), pofs, m, hp.as<uint64_t>());
-    SPG_LAUNCH_CHECK();
-    SPG_TRY(exclusive_scan_u64(c, hp.as<uint64_t>(), m + 1, nullptr, s));
-    const uint64_t P = read_u64(hp.as<uint64_t>() + m, s, &rc);
-    SPG_TRY(rc);
-    if (P == 0) return SPG_OK;
-    DevBuf key, idx, pval, flag, begin, sum, keep, crow, ccol, cval;
+    out->n = 0;
+    if (HP == 0) return SPG_OK;
+    const uint64_t P = HP;
+    DevBuf key, idx, pval, flag, begin, sum, keep;
     SPG_TRY(key.alloc(P * sizeof(uint64_t), s));
     SPG_TRY(idx.alloc(P * sizeof(uint32_t), s));
     SPG_TRY(pval.alloc(P * sizeof(double), s));
     sg_expand<<<grid_for(m * 32, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), B->d_off(), B->d_cols(),
-                                                 B->d_vals(), m, cbits, hp.as<uint64_t>(), key.as<uint64_t>(),
-                                                 idx.as<uint32_t>(), pval.as<double>());
+                                                 B->d_vals(), m, cbits, hp, key.as<uint64_t>(), idx.as<uint32_t>(),
+                                                 pval.as<double>());
     SPG_LAUNCH_CHECK();
     SPG_TRY(radix_sort_pairs_u64(c, key.as<uint64_t>(), idx.as<uint32_t>(), P, rbits + cbits, s));
     SPG_TRY(flag.alloc((P + 1) * sizeof(uint64_t), s));
     sg_run_flags<<<grid_for(P, GB, gmax), GB, 0, s>>>(key.as<uint64_t>(), P, flag.as<uint64_t>());
     SPG_LAUNCH_CHECK();
     SPG_TRY(exclusive_scan_u64(c, flag.as<uint64_t>(), P, flag.as<uint64_t>() + P, s));
-    const uint64_t U = read_u64(flag.as<uint64_t>() + P, s, &rc);
+    const uint64_t U = read_u64(c, flag.as<uint64_t>() + P, s, &rc);
     SPG_TRY(rc);
     SPG_TRY(begin.alloc((U + 1) * sizeof(uint64_t), s));
     sg_run_begins<<<grid_for(P, GB, gmax), GB, 0, s>>>(key.as<uint64_t>(), flag.as<uint64_t>(), P, U,
@@ -339,39 +354,120 @@ int spgemm_heavy_rows(Ctx *c, const Csr *A, const Csr *B, const uint64_t *pofs, 
                                                     sum.as<double>(), keep.as<uint64_t>());
     SPG_LAUNCH_CHECK();
     SPG_TRY(exclusive_scan_u64(c, keep.as<uint64_t>(), U, keep.as<uint64_t>() + U, s));
-    const uint64_t nh = read_u64(keep.as<uint64_t>() + U, s, &rc);
+    const uint64_t nh = read_u64(c, keep.as<uint64_t>() + U, s, &rc);
     SPG_TRY(rc);
+    out->n = nh;
     if (nh == 0) return SPG_OK;
-    SPG_TRY(crow.alloc(nh * sizeof(uint32_t), s));
-    SPG_TRY(ccol.alloc(nh * sizeof(uint32_t), s));
-    SPG_TRY(cval.alloc(nh * sizeof(double), s));
+    // cols / vals padded like a CSR's, so the ESC variant can install them as C
+    SPG_TRY(out->crow.alloc(nh * sizeof(uint32_t), s));
+    SPG_TRY(out->ccol.alloc(csr_alloc_elems(nh) * sizeof(uint32_t), s));
+    SPG_TRY(out->cval.alloc(csr_alloc_elems(nh) * sizeof(double), s));
     sg_write<<<grid_for(U, GB, gmax), GB, 0, s>>>(begin.as<uint64_t>(), key.as<uint64_t>(), sum.as<double>(),
-                                                 keep.as<uint64_t>(), U, cbits, ccol.as<uint32_t>(), cval.as<double>(),
-                                                 crow.as<uint32_t>());
-    SPG_LAUNCH_CHECK();
-    sg_place_heavy<<<grid_for(nh, GB, gmax), GB, 0, s>>>(crow.as<uint32_t>(), ccol.as<uint32_t>(),
-                                                        cval.as<double>(), nh, pofs, tcols, tvals, rowcnt);
+                                                 keep.as<uint64_t>(), U, cbits, out->ccol.as<uint32_t>(),
+                                                 out->cval.as<double>(), out->crow.as<uint32_t>());
     SPG_LAUNCH_CHECK();
     return SPG_OK;
 }
 
-}  // namespace
+namespace {
 
-int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
-    const uint64_t m = A->n_rows, n = B->n_cols;
-    const int cbits = bits_for(n), rbits = bits_for(m);
+// Row merge's heavy rows: expand - sort - compress, results placed in the
+// rows' scratch regions with their counts.
+int spgemm_heavy_rows(Ctx *c, const Csr *A, const Csr *B, const uint64_t *pofs, uint32_t *tcols, double *tvals,
+                      uint64_t *rowcnt, int rbits, int cbits, cudaStream_t s) {
+    const uint64_t m = A->n_rows;
     const unsigned gmax = (unsigned)c->n_sms * 32;
     int rc = SPG_OK;
-    DevBuf pofs;
-    SPG_TRY(pofs.alloc((m + 1) * sizeof(uint64_t), s));
-    sg_row_products<<<grid_for(m + 1, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), B->d_off(), m,
-                                                             pofs.as<uint64_t>());
+    DevBuf hp;
+    SPG_TRY(hp.alloc((m + 1) * sizeof(uint64_t), s));
+    sg_heavy_products<<<grid_for(m + 1, GB, gmax), GB, 0, s>>>(A->d_off(), pofs, m, hp.as<uint64_t>());
     SPG_LAUNCH_CHECK();
-    SPG_TRY(exclusive_scan_u64(c, pofs.as<uint64_t>(), m + 1, nullptr, s));
-    const uint64_t P = read_u64(pofs.as<uint64_t>() + m, s, &rc);
+    SPG_TRY(exclusive_scan_u64(c, hp.as<uint64_t>(), m + 1, nullptr, s));
+    const uint64_t P = read_u64(c, hp.as<uint64_t>() + m, s, &rc);
     SPG_TRY(rc);
-    if (P >= (1ull << 32))
-        return set_error(SPG_ERR_UNSUPPORTED, "spgemm: %llu products exceed 2^32-1", (unsigned long long)P);
+    EscOut eo;
+    SPG_TRY(spgemm_esc(c, A, B, hp.as<uint64_t>(), P, rbits, cbits, &eo, s));
+    if (eo.n == 0) return SPG_OK;
+    sg_place_heavy<<<grid_for(eo.n, GB, gmax), GB, 0, s>>>(eo.crow.as<uint32_t>(), eo.ccol.as<uint32_t>(),
+                                                          eo.cval.as<double>(), eo.n, pofs, tcols, tvals, rowcnt);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+// Row counts of ESC's compacted output (crow sorted): cnt[crow[e]] += 1.
+__global__ void sg_count_rows(const uint32_t *__restrict__ crow, uint64_t n, unsigned long long *__restrict__ cnt) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(cnt + crow[e], 1ull);
+}
+
+}  // namespace
+
+// C's arrays installed into Cm (reshaped to m x n).
+void spgemm_install(Csr *Cm, uint64_t m, uint64_t n, DevBuf &&off, DevBuf &&cols, DevBuf &&vals, uint64_t nnz) {
+    Cm->invalidate_derived();
+    Cm->n_rows = m;
+    Cm->n_cols = n;
+    Cm->off = std::move(off);
+    Cm->cols = std::move(cols);
+    Cm->vals = std::move(vals);
+    Cm->nnz = nnz;
+    Cm->capacity = nnz;
+    Cm->built = true;
+    Cm->may_have_zeros = false;
+}
+
+// Products per row of A (pofs[i], scanned in place; pofs[m] = P) and P.
+int spgemm_products(Ctx *c, const Csr *A, const Csr *B, DevBuf *pofs, uint64_t *P, cudaStream_t s) {
+    const uint64_t m = A->n_rows;
+    int rc = SPG_OK;
+    SPG_TRY(pofs->alloc((m + 1) * sizeof(uint64_t), s));
+    sg_row_products<<<grid_for(m + 1, GB), GB, 0, s>>>(A->d_off(), A->d_cols(), B->d_off(), m,
+                                                             pofs->as<uint64_t>());
+    SPG_LAUNCH_CHECK();
+    SPG_TRY(exclusive_scan_u64(c, pofs->as<uint64_t>(), m + 1, nullptr, s));
+    *P = read_u64(c, pofs->as<uint64_t>() + m, s, &rc);
+    SPG_TRY(rc);
+    if (*P >= (1ull << 32))
+        return set_error(SPG_ERR_UNSUPPORTED, "spgemm: %llu products exceed 2^32-1", (unsigned long long)*P);
+    return SPG_OK;
+}
+
+// SPG_SPGEMM_ESC: expand - sort - compress for every row; its compacted
+// output is C in CSR order.
+int spgemm_esc_all(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
+    const uint64_t m = A->n_rows, n = B->n_cols;
+    const int cbits = bits_for(n), rbits = bits_for(m);
+    DevBuf pofs;
+    uint64_t P = 0;
+    SPG_TRY(spgemm_products(c, A, B, &pofs, &P, s));
+    EscOut eo;
+    SPG_TRY(spgemm_esc(c, A, B, pofs.as<uint64_t>(), P, rbits, cbits, &eo, s));
+    DevBuf off;
+    SPG_TRY(off.alloc(csr_off_elems(m) * sizeof(uint64_t), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(off.ptr, 0, csr_off_elems(m) * sizeof(uint64_t), s));
+    if (eo.n) {
+        sg_count_rows<<<grid_for(eo.n, GB, (unsigned)c->n_sms * 32), GB, 0, s>>>(
+            eo.crow.as<uint32_t>(), eo.n, reinterpret_cast<unsigned long long *>(off.as<uint64_t>()));
+        SPG_LAUNCH_CHECK();
+    }
+    SPG_TRY(exclusive_scan_u64(c, off.as<uint64_t>(), m + 1, nullptr, s));
+    if (!eo.n) {
+        SPG_TRY(eo.ccol.alloc(csr_alloc_elems(0) * sizeof(uint32_t), s));
+        SPG_TRY(eo.cval.alloc(csr_alloc_elems(0) * sizeof(double), s));
+    }
+    SPG_TRY(c->phase_sync(s));
+    spgemm_install(Cm, m, n, std::move(off), std::move(eo.ccol), std::move(eo.cval), eo.n);
+    return SPG_OK;
+}
+
+// SPG_SPGEMM_ROWMERGE.
+int spgemm_rowmerge(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
+    const uint64_t m = A->n_rows, n = B->n_cols;
+    const int cbits = bits_for(n), rbits = bits_for(m);
+    int rc = SPG_OK;
+    DevBuf pofs;
+    uint64_t P = 0;
+    SPG_TRY(spgemm_products(c, A, B, &pofs, &P, s));
     // out_off holds the per-row kept counts, then (scanned) C's offsets
     DevBuf tcols, tvals, out_off, out_cols, out_vals;
     SPG_TRY(out_off.alloc(csr_off_elems(m) * sizeof(uint64_t), s));
@@ -391,7 +487,7 @@ int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
                                   out_off.as<uint64_t>(), rbits, cbits, s));
     }
     SPG_TRY(exclusive_scan_u64(c, out_off.as<uint64_t>(), m + 1, nullptr, s));
-    const uint64_t nnz = read_u64(out_off.as<uint64_t>() + m, s, &rc);
+    const uint64_t nnz = read_u64(c, out_off.as<uint64_t>() + m, s, &rc);
     SPG_TRY(rc);
     SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
     SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
@@ -401,19 +497,20 @@ int spgemm_impl(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, cudaStream_t s) {
                                                            out_cols.as<uint32_t>(), out_vals.as<double>());
         SPG_LAUNCH_CHECK();
     }
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
-    (void)gmax;
-    Cm->invalidate_derived();
-    Cm->n_rows = m;
-    Cm->n_cols = n;
-    Cm->off = std::move(out_off);
-    Cm->cols = std::move(out_cols);
-    Cm->vals = std::move(out_vals);
-    Cm->nnz = nnz;
-    Cm->capacity = nnz;
-    Cm->built = true;
-    Cm->may_have_zeros = false;
+    SPG_TRY(c->phase_sync(s));
+    spgemm_install(Cm, m, n, std::move(out_off), std::move(out_cols), std::move(out_vals), nnz);
     return SPG_OK;
+}
+
+int spgemm_run(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cudaStream_t s) {
+    switch (variant) {
+        case SPG_SPGEMM_ROWMERGE: return spgemm_rowmerge(c, A, B, Cm, s);
+        case SPG_SPGEMM_ESC: return spgemm_esc_all(c, A, B, Cm, s);
+        case SPG_SPGEMM_WARPSORT_64:
+        case SPG_SPGEMM_WARPSORT_128:
+        case SPG_SPGEMM_WARPSORT_256: return spgemm_warpsort(c, A, B, Cm, variant, s);
+        default: return set_error(SPG_ERR_INVALID_ARGUMENT, "spgemm: unknown variant %d", variant);
+    }
 }
 
 }  // namespace spg
@@ -431,5 +528,23 @@ extern "C" int spg_spgemm(spg_ctx *c, const spg_csr *A, const spg_csr *B, spg_cs
     if (!B->built) return set_error(SPG_ERR_LOGIC, "spgemm: B must be locked");
     if (Cm == A || Cm == B) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm: output aliases an input");
     SPG_CUDA_TRY(cudaSetDevice(c->device));
-    return spgemm_impl(c, A, B, Cm, c->stream);
+    int v = SPG_SPGEMM_AUTO;
+    SPG_TRY(spgemm_resolve_auto(c, A, B, &v));
+    return spgemm_run(c, A, B, Cm, v, c->stream);
+}
+
+extern "C" int spg_spgemm_variant(spg_ctx *c, const spg_csr *A, const spg_csr *B, spg_csr *Cm, int variant) {
+    if (!c || !A || !B || !Cm) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_variant: null handle");
+    SPG_CHECK_LIVE(A);
+    SPG_CHECK_LIVE(B);
+    SPG_CHECK_LIVE(Cm);
+    if (A->n_cols != B->n_rows) return set_error(SPG_ERR_INVALID_ARGUMENT, "A.cols must equal B.rows");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spgemm: A must be locked");
+    if (!B->built) return set_error(SPG_ERR_LOGIC, "spgemm: B must be locked");
+    if (Cm == A || Cm == B) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm: output aliases an input");
+    if (variant < SPG_SPGEMM_AUTO || variant >= SPG_SPGEMM_N_VARIANTS)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_variant: unknown variant %d", variant);
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (variant == SPG_SPGEMM_AUTO) SPG_TRY(spgemm_resolve_auto(c, A, B, &variant));
+    return spgemm_run(c, A, B, Cm, variant, c->stream);
 }

@@ -588,12 +588,8 @@ int spmv_prepare(Ctx *c, Csr *A, int variant, cudaStream_t s) {
             return build_stream_plan(c, A, s);
         case SPG_SPMV_MERGE:
             return build_merge_plan(c, A, s);
-        case SPG_SPMV_ADAPTIVE:
-        case SPG_SPMV_ADAPTIVE16:
-        case SPG_SPMV_INTERLEAVED:
-            return build_adaptive_plan(c, A, variant, s);
         default:
-            return SPG_OK;
+            return spmv_is_seg(variant) ? build_adaptive_plan(c, A, variant, s) : SPG_OK;
     }
 }
 
@@ -636,11 +632,8 @@ int spmv_launch(Ctx *c, Csr *A, const double *x, double *y, int variant, cudaStr
             merge_fixup<<<grid_for(nt, 256), 256, 0, s>>>(A->plan_merge.aux.as<Carry>(), nt, n, y);
             break;
         }
-        case SPG_SPMV_ADAPTIVE:
-        case SPG_SPMV_ADAPTIVE16:
-        case SPG_SPMV_INTERLEAVED:
-            return spmv_adaptive(c, A, x, y, variant, s);
         default:
+            if (spmv_is_seg(variant)) return spmv_adaptive(c, A, x, y, variant, s);
             return set_error(SPG_ERR_INVALID_ARGUMENT, "spmv: unknown variant %d", variant);
     }
     SPG_LAUNCH_CHECK();

@@ -24,14 +24,15 @@
 // a second small kernel. Deterministic for a given matrix and variant.
 //
 // SPG_SPMV_INTERLEAVED runs the same kernel over a copy of cols and vals
-// stored lane-interleaved within each 512-nonzero chunk (vals in pairs, cols
-// in quads: the k-th 16-byte piece of every lane lies side by side). A lane
-// still owns 16 consecutive nonzeros and sums them in the same order, so y is
-// bit-identical to SPG_SPMV_ADAPTIVE16, but each warp load is one contiguous
-// 512-byte access instead of 32 strided 16-byte pieces. On random-column
-// matrices the x gathers saturate the L1 data pipe; the strided loads of the
-// in-place layout cost about as many L1 wavefronts again, the interleaved ones
-// an eighth of that.
+// stored lane-interleaved within each 512-nonzero chunk, both in pairs: the
+// k-th pair of nonzeros of every lane lies side by side (16 bytes of values,
+// 8 bytes of columns per lane). A lane still owns 16 consecutive nonzeros and
+// sums them in the same order, so y is bit-identical to SPG_SPMV_ADAPTIVE16,
+// but each warp load is one contiguous 512-byte (values) or 256-byte
+// (columns) access instead of 32 strided pieces, and every 128-byte line is
+// requested once. On random-column matrices the x gathers saturate the L1 to
+// L2 request path; the strided loads of the in-place layout cost about as
+// many L1 wavefronts again, the interleaved ones an eighth of that.
 #include "spg_internal.cuh"
 
 namespace spg {
@@ -101,7 +102,7 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
     const uint64_t w = c0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= c1) return;
-    static_assert(SUB % 4 == 0 || (INTER && SUB == 2), "column loads come in 16-byte pieces (interleaved: halves)");
+    static_assert(INTER ? SUB % 2 == 0 : SUB % 4 == 0, "loads come in 16-byte pieces (interleaved: pairs)");
     const uint64_t p0 = w * (32ull * ITEMS) + (uint64_t)lane * ITEMS;
     unsigned word = 0;
     if (p0 < nnz) {
@@ -129,7 +130,7 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
         uint32_t c[SUB];
         if (nv) {
             if constexpr (INTER) {
-                // piece k of lane l sits at chunk + 64 k + 2 l (vals), chunk + 128 k + 4 l (cols)
+                // pair k of lane l sits at chunk + 64 k + 2 l (vals and cols alike)
                 const uint64_t cb = w * (32ull * ITEMS);
 #pragma unroll
                 for (int u = 0; u < SUB; u += 2) {
@@ -138,21 +139,12 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
                     v[u] = t.x;
                     v[u + 1] = t.y;
                 }
-                if constexpr (SUB >= 4) {
 #pragma unroll
-                    for (int u = 0; u < SUB; u += 4) {
-                        const uint4 t = __ldcs(reinterpret_cast<const uint4 *>(
-                            cols + cb + 128u * (unsigned)((SUB * h + u) >> 2) + 4u * (unsigned)lane));
-                        c[u] = t.x;
-                        c[u + 1] = t.y;
-                        c[u + 2] = t.z;
-                        c[u + 3] = t.w;
-                    }
-                } else {  // SUB == 2: one half of the lane's 16-byte piece of columns
-                    const uint2 t = __ldcs(reinterpret_cast<const uint2 *>(
-                        cols + cb + 128u * (unsigned)((SUB * h) >> 2) + 4u * (unsigned)lane + ((SUB * h) & 3u)));
-                    c[0] = t.x;
-                    c[1] = t.y;
+                for (int u = 0; u < SUB; u += 2) {
+                    const uint2 q = __ldcs(reinterpret_cast<const uint2 *>(
+                        cols + cb + 64u * (unsigned)((SUB * h + u) >> 1) + 2u * (unsigned)lane));
+                    c[u] = q.x;
+                    c[u + 1] = q.y;
                 }
             } else {
 #pragma unroll
@@ -247,7 +239,7 @@ spmv_seg(const uint32_t *__restrict__ cols, const double *__restrict__ vals, con
 
 // Lane-interleaved copy for SPG_SPMV_INTERLEAVED: nonzero p = 512 w + 16 l + u
 // (chunk w, lane l, item u) goes to 512 w + 64 (u / 2) + 2 l + u % 2 in vals and
-// 512 w + 128 (u / 4) + 4 l + u % 4 in cols; the tail of the last chunk is zero.
+// cols alike; the tail of the last chunk is zero.
 __global__ void seg_interleave(const uint32_t *__restrict__ cols, const double *__restrict__ vals, uint64_t nnz,
                                uint64_t n_slots, uint32_t *__restrict__ icols, double *__restrict__ ivals) {
     for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_slots;
@@ -256,7 +248,7 @@ __global__ void seg_interleave(const uint32_t *__restrict__ cols, const double *
         const unsigned q = (unsigned)(p & 511), l = q >> 4, u = q & 15;
         const bool real = p < nnz;
         ivals[(w << 9) + 64u * (u >> 1) + 2u * l + (u & 1u)] = real ? vals[p] : 0.0;
-        icols[(w << 9) + 128u * (u >> 2) + 4u * l + (u & 3u)] = real ? cols[p] : 0u;
+        icols[(w << 9) + 64u * (u >> 1) + 2u * l + (u & 1u)] = real ? cols[p] : 0u;
     }
 }
 
@@ -303,10 +295,13 @@ __global__ void seg_empty_rows(const uint32_t *__restrict__ empty, uint64_t n_em
 // extra1 = nzrow, extra2 = empty rows, count1 = #empty; interleaved only:
 // extra3 = cols, extra4 = vals in lane-interleaved order.
 int build_adaptive_plan(Ctx *c, Csr *A, int variant, cudaStream_t s) {
-    const int items = variant == SPG_SPMV_ADAPTIVE ? 32 : 16;
-    const bool inter = variant == SPG_SPMV_INTERLEAVED;
+    const SegShape sh = seg_shape(variant);
+    const int items = sh.items;
+    const bool inter = sh.inter;
+    if (!items) return set_error(SPG_ERR_INVALID_ARGUMENT, "adaptive plan: variant %d", variant);
     SpmvPlan &slot = adaptive_plan_of(A, variant);
-    if (slot.kind == variant * 100 + items) return SPG_OK;
+    const int kind = 2 * items + (inter ? 1 : 0);  // tiles of one variant share its plan
+    if (slot.kind == kind) return SPG_OK;
     const uint64_t n = A->n_rows, nnz = A->nnz;
     const uint64_t chunk = 32ull * items;
     const uint64_t n_chunks = (nnz + chunk - 1) / chunk;
@@ -351,7 +346,7 @@ int build_adaptive_plan(Ctx *c, Csr *A, int variant, cudaStream_t s) {
             A->d_cols(), A->d_vals(), nnz, n_slots, P.extra3.as<uint32_t>(), P.extra4.as<double>());
         SPG_LAUNCH_CHECK();
     }
-    P.kind = variant * 100 + items;
+    P.kind = kind;
     P.n_items = n_chunks;
     P.items = std::move(bm);
     P.aux = std::move(recs);
@@ -371,16 +366,37 @@ int launch_seg(const SpmvPlan &P, const Csr *A, const double *x, double *y, int 
     if (c1 <= c0) return SPG_OK;
     const uint32_t *nzrow = P.count1 ? P.extra1.as<uint32_t>() : nullptr;
     const unsigned grid = grid_for((c1 - c0) * 32, 256);
-    if (variant == SPG_SPMV_INTERLEAVED)
-        spmv_seg<16, 2, true, 8><<<grid, 256, 0, s>>>(P.extra3.as<uint32_t>(), P.extra4.as<double>(), x, y, A->nnz,
-                                                P.items.as<unsigned>(), P.extra0.as<uint32_t>(), nzrow,
-                                                P.aux.as<Rec>(), c0, c1);
-    else if (variant == SPG_SPMV_ADAPTIVE16)
-        spmv_seg<16, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
-                                                 P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), c0, c1);
-    else
-        spmv_seg<32, 8, false><<<grid, 256, 0, s>>>(A->d_cols(), A->d_vals(), x, y, A->nnz, P.items.as<unsigned>(),
-                                                 P.extra0.as<uint32_t>(), nzrow, P.aux.as<Rec>(), c0, c1);
+    const uint32_t *ic = P.extra3.as<uint32_t>(), *cc = A->d_cols();
+    const double *iv = P.extra4.as<double>(), *cv = A->d_vals();
+    const unsigned *bm = P.items.as<unsigned>();
+    const uint32_t *cb = P.extra0.as<uint32_t>();
+    Rec *rc = P.aux.as<Rec>();
+    const uint64_t nnz = A->nnz;
+    switch (variant) {
+        case SPG_SPMV_INTERLEAVED:
+            spmv_seg<16, 2, true, 8><<<grid, 256, 0, s>>>(ic, iv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        case SPG_SPMV_INTERLEAVED_S4:
+            spmv_seg<16, 4, true, 5><<<grid, 256, 0, s>>>(ic, iv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        case SPG_SPMV_INTERLEAVED_S8:
+            spmv_seg<16, 8, true, 4><<<grid, 256, 0, s>>>(ic, iv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        case SPG_SPMV_ADAPTIVE16:
+            spmv_seg<16, 8, false, 4><<<grid, 256, 0, s>>>(cc, cv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        case SPG_SPMV_ADAPTIVE16_S4:
+            spmv_seg<16, 4, false, 6><<<grid, 256, 0, s>>>(cc, cv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        case SPG_SPMV_ADAPTIVE:
+            spmv_seg<32, 8, false, 4><<<grid, 256, 0, s>>>(cc, cv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        case SPG_SPMV_ADAPTIVE_S16:
+            spmv_seg<32, 16, false, 2><<<grid, 256, 0, s>>>(cc, cv, x, y, nnz, bm, cb, nzrow, rc, c0, c1);
+            break;
+        default:
+            return set_error(SPG_ERR_INVALID_ARGUMENT, "spmv: variant %d is not a chunk kernel", variant);
+    }
     SPG_LAUNCH_CHECK();
     return SPG_OK;
 }
@@ -425,7 +441,7 @@ int spmv_adaptive_blocks(Ctx *c, Csr *A, int variant, int nb, std::vector<uint64
     bool known = false;
     SPG_TRY(csr_max_row(c, A, s, &known));
     const uint64_t max_row = known ? A->max_row : A->nnz;  // no row is longer than nnz
-    const uint64_t chunk_nnz = 32ull * (variant == SPG_SPMV_ADAPTIVE ? 32 : 16);
+    const uint64_t chunk_nnz = 32ull * seg_shape(variant).items;
     while (nb > 1 && (nch / nb) * chunk_nnz < max_row + 2 * chunk_nnz) --nb;
     if (nb < 1) nb = 1;
     // first (actual) row starting at or after each block's first chunk

@@ -76,13 +76,19 @@ __global__ void tr_count(const uint32_t *__restrict__ cols, uint64_t nnz, unsign
 // overlap instead of queueing one after another).
 constexpr int SB = 8;
 
+// The sorting-network path runs before the host has seen the longest output
+// row: its kernels take the device-side longest row and do nothing when it
+// is above 32 (the grouped-sort path then runs instead).
+constexpr unsigned long long NET_MAX = 32;
+
 template <bool WRITE_ROW>
 __global__ void tr_scatter(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
                            const double *__restrict__ vals, uint64_t m, const uint64_t *__restrict__ toff,
                            unsigned *__restrict__ cursor, uint32_t *__restrict__ trow, uint32_t *__restrict__ tsrc,
-                           double *__restrict__ tval) {
+                           double *__restrict__ tval, const unsigned long long *__restrict__ longest) {
     const uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (w >= m) return;
+    if (longest && *longest > NET_MAX) return;
     const uint64_t e = off[w + 1];
     for (uint64_t k = off[w]; k < e; k += SB) {
         uint32_t col[SB];
@@ -189,7 +195,9 @@ __device__ __forceinline__ void sort_row_regs(const uint32_t *__restrict__ tsrc,
 __global__ void __launch_bounds__(TB)
 tr_sort_short(const uint64_t *__restrict__ toff, uint64_t n, const uint32_t *__restrict__ tsrc,
               const double *__restrict__ tval, uint32_t *__restrict__ out_cols, double *__restrict__ out_vals,
-              unsigned long long *__restrict__ n_mid, uint32_t *__restrict__ mid) {
+              unsigned long long *__restrict__ n_mid, uint32_t *__restrict__ mid,
+              const unsigned long long *__restrict__ longest) {
+    if (*longest > NET_MAX) return;
     for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t b = toff[c];
         const uint64_t L = toff[c + 1] - b;
@@ -202,7 +210,7 @@ tr_sort_short(const uint64_t *__restrict__ toff, uint64_t n, const uint32_t *__r
             sort_row_regs<8>(tsrc, tval, b, (uint32_t)L, out_cols, out_vals);
         } else if (L <= 16) {
             sort_row_regs<16>(tsrc, tval, b, (uint32_t)L, out_cols, out_vals);
-        } else {  // 17..32 (the caller checked the longest row)
+        } else {  // 17..32 (longer rows never reach this kernel)
             mid[atomicAdd(n_mid, 1ull)] = (uint32_t)c;
         }
     }
@@ -213,7 +221,9 @@ tr_sort_short(const uint64_t *__restrict__ toff, uint64_t n, const uint32_t *__r
 __global__ void __launch_bounds__(TB)
 tr_sort_mid(const uint64_t *__restrict__ toff, const uint32_t *__restrict__ mid,
             const unsigned long long *__restrict__ n_mid, const uint32_t *__restrict__ tsrc,
-            const double *__restrict__ tval, uint32_t *__restrict__ out_cols, double *__restrict__ out_vals) {
+            const double *__restrict__ tval, uint32_t *__restrict__ out_cols, double *__restrict__ out_vals,
+            const unsigned long long *__restrict__ longest) {
+    if (*longest > NET_MAX) return;
     const unsigned lane = threadIdx.x & 31;
     const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t cnt = *n_mid;
@@ -265,42 +275,45 @@ static int transpose_grouped(Ctx *c, const Csr *A, Csr *T, bool *done, cudaStrea
         SPG_LAUNCH_CHECK();
         SPG_TRY(exclusive_scan_u64(c, out_off.as<uint64_t>(), n + 1, nullptr, s));
         // the longest output row decides the sort: up to 32 entries, sorting
-        // networks per row (and the scatter need not record output rows)
+        // networks per row (and the scatter need not record output rows).
+        // That path is enqueued at once, its kernels checking the longest row
+        // on the device, so the common case costs no host round trip before
+        // the final one; a longer row sends every row through the grouped
+        // sort afterwards.
         DevBuf meta, midbuf;
         SPG_TRY(meta.alloc(16, s));  // [longest row (8 bytes)] [rows of 17..32 entries (8 bytes)]
         SPG_CUDA_TRY(cudaMemsetAsync(meta.ptr, 0, 16, s));
         unsigned long long *mx = meta.as<unsigned long long>(), *n_mid = mx + 1;
         tr_max_len<<<grid_for(n, TB, (unsigned)c->n_sms * 8), TB, 0, s>>>(out_off.as<uint64_t>(), n, mx);
         SPG_LAUNCH_CHECK();
-        unsigned long long longest = 0;
-        SPG_CUDA_TRY(cudaMemcpyAsync(&longest, mx, 8, cudaMemcpyDeviceToHost, s));
-        SPG_CUDA_TRY(cudaStreamSynchronize(s));
-        const bool networks = longest <= 32 && m < 0xFFFFFFFFull;  // source rows below the padding key
         SPG_TRY(cursor.alloc((n ? n : 1) * sizeof(unsigned), s));
         SPG_CUDA_TRY(cudaMemsetAsync(cursor.ptr, 0, (n ? n : 1) * sizeof(unsigned), s));
-        if (!networks) SPG_TRY(trow.alloc(nnz * sizeof(uint32_t), s));
         SPG_TRY(tsrc.alloc(nnz * sizeof(uint32_t), s));
         SPG_TRY(tval.alloc(nnz * sizeof(double), s));
-        if (networks)
+        unsigned long long longest = NET_MAX + 1;
+        if (m < 0xFFFFFFFFull) {  // source rows below the networks' padding key
+            SPG_TRY(midbuf.alloc((n ? n : 1) * sizeof(uint32_t), s));
             tr_scatter<false><<<grid_for(m, TB), TB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), m,
                                                              out_off.as<uint64_t>(), cursor.as<unsigned>(), nullptr,
-                                                             tsrc.as<uint32_t>(), tval.as<double>());
-        else
+                                                             tsrc.as<uint32_t>(), tval.as<double>(), mx);
+            tr_sort_short<<<grid_for(n, TB, gmax), TB, 0, s>>>(out_off.as<uint64_t>(), n, tsrc.as<uint32_t>(),
+                                                               tval.as<double>(), out_cols.as<uint32_t>(),
+                                                               out_vals.as<double>(), n_mid, midbuf.as<uint32_t>(),
+                                                               mx);
+            tr_sort_mid<<<(unsigned)c->n_sms * 8, TB, 0, s>>>(out_off.as<uint64_t>(), midbuf.as<uint32_t>(), n_mid,
+                                                             tsrc.as<uint32_t>(), tval.as<double>(),
+                                                             out_cols.as<uint32_t>(), out_vals.as<double>(), mx);
+            SPG_LAUNCH_CHECK();
+            SPG_CUDA_TRY(cudaMemcpyAsync(&longest, mx, 8, cudaMemcpyDeviceToHost, s));
+            SPG_TRY(c->phase_sync(s));
+        }
+        if (longest > NET_MAX) {  // the networks' kernels did nothing; cursors are still zero
+            SPG_TRY(trow.alloc(nnz * sizeof(uint32_t), s));
             tr_scatter<true><<<grid_for(m, TB), TB, 0, s>>>(A->d_off(), A->d_cols(), A->d_vals(), m,
                                                             out_off.as<uint64_t>(), cursor.as<unsigned>(),
                                                             trow.as<uint32_t>(), tsrc.as<uint32_t>(),
-                                                            tval.as<double>());
-        SPG_LAUNCH_CHECK();
-        if (networks) {
-            SPG_TRY(midbuf.alloc((n ? n : 1) * sizeof(uint32_t), s));
-            tr_sort_short<<<grid_for(n, TB, gmax), TB, 0, s>>>(out_off.as<uint64_t>(), n, tsrc.as<uint32_t>(),
-                                                               tval.as<double>(), out_cols.as<uint32_t>(),
-                                                               out_vals.as<double>(), n_mid, midbuf.as<uint32_t>());
-            tr_sort_mid<<<(unsigned)c->n_sms * 8, TB, 0, s>>>(out_off.as<uint64_t>(), midbuf.as<uint32_t>(), n_mid,
-                                                             tsrc.as<uint32_t>(), tval.as<double>(),
-                                                             out_cols.as<uint32_t>(), out_vals.as<double>());
+                                                            tval.as<double>(), nullptr);
             SPG_LAUNCH_CHECK();
-        } else {
             SPG_TRY(keys.alloc(nnz * sizeof(uint64_t), s));
             SPG_TRY(idx.alloc(nnz * sizeof(uint32_t), s));
             const int rbits = bits_for(m);
@@ -313,7 +326,7 @@ static int transpose_grouped(Ctx *c, const Csr *A, Csr *T, bool *done, cudaStrea
             SPG_LAUNCH_CHECK();
         }
     }
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     T->invalidate_derived();
     T->n_rows = n;
     T->n_cols = m;
@@ -355,7 +368,7 @@ int transpose_impl(Ctx *c, const Csr *A, Csr *T, cudaStream_t s) {
     tr_offsets<<<grid_for(n + 1, TB, (unsigned)c->n_sms * 32), TB, 0, s>>>(rk.as<uint32_t>(), nnz, n,
                                                                          out_off.as<uint64_t>());
     SPG_LAUNCH_CHECK();
-    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    SPG_TRY(c->phase_sync(s));
     T->invalidate_derived();
     T->n_rows = n;
     T->n_cols = m;

@@ -15,6 +15,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <string>
@@ -132,6 +133,41 @@ __global__ void feat_rows(const uint64_t *__restrict__ off, const uint32_t *__re
     atomicMax(reinterpret_cast<unsigned long long *>(&s[34]), __double_as_longlong(mx));
     __syncthreads();
     for (int i = threadIdx.x; i < 38; i += blockDim.x) {
+        if (i == 34) atomicMax(reinterpret_cast<unsigned long long *>(&acc[34]), __double_as_longlong(s[34]));
+        else atomicAdd(&acc[i], s[i]);
+    }
+}
+
+// SpGEMM features of A * B. acc layout (doubles): [0..31] histogram of the
+// products per row (bin 0: none, else 1 + floor(log2 p), capped at 31),
+// 32 sum p, 33 sum p^2, 34 max p.
+__global__ void feat_gemm_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols,
+                               const uint64_t *__restrict__ boff, uint64_t m, double *__restrict__ acc) {
+    __shared__ double s[35];
+    for (int i = threadIdx.x; i < 35; i += blockDim.x) s[i] = 0.0;
+    __syncthreads();
+    double sp = 0, sp2 = 0, mx = 0;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < m; r += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t p = 0;
+        for (uint64_t ka = aoff[r]; ka < aoff[r + 1]; ++ka) {
+            const uint32_t k = acols[ka];
+            p += boff[k + 1] - boff[k];
+        }
+        int bin = 0;
+        if (p) {
+            bin = 1 + (63 - __clzll((long long)p));
+            if (bin > 31) bin = 31;
+        }
+        atomicAdd(&s[bin], 1.0);
+        sp += (double)p;
+        sp2 += (double)p * (double)p;
+        mx = fmax(mx, (double)p);
+    }
+    atomicAdd(&s[32], sp);
+    atomicAdd(&s[33], sp2);
+    atomicMax(reinterpret_cast<unsigned long long *>(&s[34]), __double_as_longlong(mx));
+    __syncthreads();
+    for (int i = threadIdx.x; i < 35; i += blockDim.x) {
         if (i == 34) atomicMax(reinterpret_cast<unsigned long long *>(&acc[34]), __double_as_longlong(s[34]));
         else atomicAdd(&acc[i], s[i]);
     }
@@ -349,9 +385,8 @@ int spmv_autotune(Ctx *c, Csr *A, int reps, float *times_ms, int *best) {
     return SPG_OK;
 }
 
-int selector_predict_dev(Ctx *c, const float *d_x, uint32_t B, float *d_out, cudaStream_t s) {
-    const int K = c->model_k;
-    const float *mean = c->model.as<float>();
+int selector_predict_dev(const DevBuf &model, int K, const float *d_x, uint32_t B, float *d_out, cudaStream_t s) {
+    const float *mean = model.as<float>();
     const float *scale = mean + F;
     const float *P = scale + F;
     DevBuf xn, act;
@@ -379,7 +414,7 @@ int spmv_resolve_auto(Ctx *c, Csr *A, int *variant) {
         SPG_TRY(dout.alloc(c->model_k * sizeof(float), s));
         SPG_TRY(db.alloc(sizeof(int), s));
         SPG_CUDA_TRY(cudaMemcpyAsync(df.ptr, f, sizeof(f), cudaMemcpyHostToDevice, s));
-        SPG_TRY(selector_predict_dev(c, df.as<float>(), 1, dout.as<float>(), s));
+        SPG_TRY(selector_predict_dev(c->model, c->model_k, df.as<float>(), 1, dout.as<float>(), s));
         mlp_argmin<<<1, 32, 0, s>>>(dout.as<float>(), 1, c->model_k, db.as<int>());
         SPG_LAUNCH_CHECK();
         SPG_CUDA_TRY(cudaMemcpyAsync(&v, db.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -393,19 +428,19 @@ int spmv_resolve_auto(Ctx *c, Csr *A, int *variant) {
     return SPG_OK;
 }
 
-// The trained selector shipped beside the library (spg_selector.bin in the
-// directory of libspg.so) or named by SPG_SELECTOR_MODEL; absent or malformed
-// files leave the context on the autotuner.
-int selector_load_default(Ctx *c) {
+// A trained selector shipped beside the library (`file` in the directory of
+// libspg.so) or named by the environment variable `env`; absent or malformed
+// files leave the context on the autotuner for that operation.
+int selector_load_file(Ctx *c, const char *env, const char *file, int max_k, DevBuf *model, int *model_k) {
     std::string path;
-    if (const char *env = getenv("SPG_SELECTOR_MODEL")) {
-        path = env;
+    if (const char *e = getenv(env)) {
+        path = e;
     } else {
         Dl_info info;
-        if (dladdr(reinterpret_cast<void *>(&selector_load_default), &info) && info.dli_fname) {
+        if (dladdr(reinterpret_cast<void *>(&selector_load_file), &info) && info.dli_fname) {
             path = info.dli_fname;
             const size_t slash = path.rfind('/');
-            path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/spg_selector.bin";
+            path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/" + file;
         }
     }
     if (path.empty()) return SPG_OK;
@@ -421,15 +456,115 @@ int selector_load_default(Ctx *c) {
     const long long rest = (long long)blob.size() - base;
     if (rest <= 0 || rest % per_k) return SPG_OK;
     const int K = (int)(rest / per_k);
-    if (K < 1 || K > SPG_SPMV_N_VARIANTS) return SPG_OK;
-    if (c->model.alloc(blob.size() * sizeof(float), c->stream) != SPG_OK) return SPG_OK;
-    if (cudaMemcpyAsync(c->model.ptr, blob.data(), blob.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(c->stream) != cudaSuccess) {
-        c->model.release();
+    if (K < 1 || K > max_k) return SPG_OK;
+    if (model->alloc(blob.size() * sizeof(float), c->stream) != SPG_OK) {
+        clear_error();
         return SPG_OK;
     }
-    c->model_k = K;
+    if (cudaMemcpyAsync(model->ptr, blob.data(), blob.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        model->release();
+        return SPG_OK;
+    }
+    *model_k = K;
+    return SPG_OK;
+}
+
+int selector_load_default(Ctx *c) {
+    selector_load_file(c, "SPG_SELECTOR_MODEL", "spg_selector.bin", SPG_SPMV_N_VARIANTS, &c->model, &c->model_k);
+    selector_load_file(c, "SPG_SPGEMM_SELECTOR_MODEL", "spg_spgemm_selector.bin", SPG_SPGEMM_N_VARIANTS,
+                       &c->gemm_model, &c->gemm_model_k);
+    return SPG_OK;
+}
+
+// ---------------------------------------------------------------- SpGEMM choice
+int spgemm_features(Ctx *c, const Csr *A, const Csr *B, float *f) {
+    cudaStream_t s = c->stream;
+    DevBuf acc;
+    SPG_TRY(acc.alloc(35 * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(acc.ptr, 0, 35 * sizeof(double), s));
+    if (A->n_rows) {
+        feat_gemm_rows<<<grid_for(A->n_rows, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(
+            A->d_off(), A->d_cols(), B->d_off(), A->n_rows, acc.as<double>());
+        SPG_LAUNCH_CHECK();
+    }
+    double h[35];
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, acc.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    const double m = (double)(A->n_rows ? A->n_rows : 1);
+    for (int i = 0; i < 32; ++i) f[i] = (float)(h[i] / m);
+    const double mean = h[32] / m;
+    const double var = std::max(0.0, h[33] / m - mean * mean);
+    f[32] = (float)(std::log2((double)A->n_rows + 1.0) / 32.0);
+    f[33] = (float)(std::log2((double)B->n_cols + 1.0) / 32.0);
+    f[34] = (float)(std::log2((double)A->nnz + 1.0) / 40.0);
+    f[35] = (float)(std::log2(h[32] + 1.0) / 40.0);
+    f[36] = (float)(std::log2(mean + 1.0) / 16.0);
+    f[37] = (float)(std::log2(std::sqrt(var) + 1.0) / 16.0);
+    f[38] = (float)(std::log2(h[34] + 1.0) / 32.0);
+    f[39] = (float)(std::log2((double)A->nnz / m + 1.0) / 16.0);
+    return SPG_OK;
+}
+
+int spgemm_autotune(Ctx *c, const Csr *A, const Csr *B, int reps, float *times_ms, int *best) {
+    cudaStream_t s = c->stream;
+    if (reps < 1) reps = 1;
+    int bi = 0;
+    double bt = 0.0;
+    for (int v = 0; v < SPG_SPGEMM_N_VARIANTS; ++v) {
+        std::vector<double> ts;
+        for (int r = 0; r <= reps; ++r) {  // run 0 warms up
+            Csr tmp;
+            tmp.ctx = c;
+            SPG_CUDA_TRY(cudaStreamSynchronize(s));
+            const auto t0 = std::chrono::steady_clock::now();
+            SPG_TRY(spgemm_run(c, A, B, &tmp, v, s));
+            SPG_CUDA_TRY(cudaStreamSynchronize(s));
+            const auto t1 = std::chrono::steady_clock::now();
+            if (r) ts.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+        }
+        std::sort(ts.begin(), ts.end());
+        const double t = ts[ts.size() / 2];
+        if (times_ms) times_ms[v] = (float)t;
+        if (v == 0 || t < bt) {
+            bt = t;
+            bi = v;
+        }
+    }
+    if (best) *best = bi;
+    return SPG_OK;
+}
+
+int spgemm_resolve_auto(Ctx *c, const Csr *A, const Csr *B, int *variant) {
+    Csr *Am = const_cast<Csr *>(A);
+    if (Am->gemm_selected >= 0 && Am->gemm_sel_b == B && Am->gemm_sel_b_epoch == B->epoch) {
+        *variant = Am->gemm_selected;
+        return SPG_OK;
+    }
+    int v = SPG_SPGEMM_WARPSORT_128;
+    if (c->spgemm_policy == SPG_POLICY_SELECTOR && c->gemm_model_k > 0) {
+        float f[F];
+        SPG_TRY(spgemm_features(c, A, B, f));
+        cudaStream_t s = c->stream;
+        DevBuf df, dout, db;
+        SPG_TRY(df.alloc(F * sizeof(float), s));
+        SPG_TRY(dout.alloc(c->gemm_model_k * sizeof(float), s));
+        SPG_TRY(db.alloc(sizeof(int), s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(df.ptr, f, sizeof(f), cudaMemcpyHostToDevice, s));
+        SPG_TRY(selector_predict_dev(c->gemm_model, c->gemm_model_k, df.as<float>(), 1, dout.as<float>(), s));
+        mlp_argmin<<<1, 32, 0, s>>>(dout.as<float>(), 1, c->gemm_model_k, db.as<int>());
+        SPG_LAUNCH_CHECK();
+        SPG_CUDA_TRY(cudaMemcpyAsync(&v, db.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SPG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (v < 0 || v >= SPG_SPGEMM_N_VARIANTS) v = SPG_SPGEMM_WARPSORT_128;
+    } else if (c->spgemm_policy != SPG_POLICY_FIXED) {
+        SPG_TRY(spgemm_autotune(c, A, B, 3, nullptr, &v));
+    }
+    Am->gemm_selected = v;
+    Am->gemm_sel_b = B;
+    Am->gemm_sel_b_epoch = B->epoch;
+    *variant = v;
     return SPG_OK;
 }
 
@@ -451,6 +586,69 @@ int spg_spmv_autotune(spg_ctx *c, const spg_csr *A, int reps, float *times_ms, i
     if (!A->built) return set_error(SPG_ERR_LOGIC, "spmv: matrix must be locked");
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     return spmv_autotune(c, const_cast<spg_csr *>(A), reps, times_ms, best);
+}
+
+int spg_spgemm_features(spg_ctx *c, const spg_csr *A, const spg_csr *B, float *features) {
+    if (!c || !A || !B || !features) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_features: null argument");
+    if (A->n_cols != B->n_rows) return set_error(SPG_ERR_INVALID_ARGUMENT, "A.cols must equal B.rows");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spgemm: A must be locked");
+    if (!B->built) return set_error(SPG_ERR_LOGIC, "spgemm: B must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return spgemm_features(c, A, B, features);
+}
+
+int spg_spgemm_autotune(spg_ctx *c, const spg_csr *A, const spg_csr *B, int reps, float *times_ms, int *best) {
+    if (!c || !A || !B) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_autotune: null argument");
+    if (A->n_cols != B->n_rows) return set_error(SPG_ERR_INVALID_ARGUMENT, "A.cols must equal B.rows");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spgemm: A must be locked");
+    if (!B->built) return set_error(SPG_ERR_LOGIC, "spgemm: B must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return spgemm_autotune(c, A, B, reps, times_ms, best);
+}
+
+int spg_spgemm_selected(spg_ctx *c, const spg_csr *A, const spg_csr *B, int *variant) {
+    if (!c || !A || !B || !variant) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_selected: null argument");
+    if (A->n_cols != B->n_rows) return set_error(SPG_ERR_INVALID_ARGUMENT, "A.cols must equal B.rows");
+    if (!A->built) return set_error(SPG_ERR_LOGIC, "spgemm: A must be locked");
+    if (!B->built) return set_error(SPG_ERR_LOGIC, "spgemm: B must be locked");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    return spgemm_resolve_auto(c, A, B, variant);
+}
+
+int spg_set_spgemm_policy(spg_ctx *c, int policy) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_set_spgemm_policy: null context");
+    if (policy < SPG_POLICY_SELECTOR || policy > SPG_POLICY_FIXED)
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_set_spgemm_policy: unknown policy %d", policy);
+    c->spgemm_policy = policy;
+    return SPG_OK;
+}
+
+int spg_spgemm_selector_load(spg_ctx *c, const float *blob, uint64_t n_floats, int n_outputs) {
+    if (!c) return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_selector_load: null context");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!blob) {
+        c->gemm_model.release();
+        c->gemm_model_k = 0;
+        return SPG_OK;
+    }
+    if (n_outputs < 1 || n_outputs > SPG_SPGEMM_N_VARIANTS || n_floats != 2 * F + n_params(n_outputs))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_selector_load: blob of %llu floats does not fit K=%d",
+                         (unsigned long long)n_floats, n_outputs);
+    SPG_TRY(c->gemm_model.alloc(n_floats * sizeof(float), c->stream));
+    SPG_CUDA_TRY(
+        cudaMemcpyAsync(c->gemm_model.ptr, blob, n_floats * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    SPG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->gemm_model_k = n_outputs;
+    return SPG_OK;
+}
+
+int spg_spgemm_selector_predict(spg_ctx *c, const float *d_features, uint32_t B, float *d_out, void *stream) {
+    if (!c || (B && (!d_features || !d_out)))
+        return set_error(SPG_ERR_INVALID_ARGUMENT, "spg_spgemm_selector_predict: null");
+    if (c->gemm_model_k <= 0) return set_error(SPG_ERR_LOGIC, "spg_spgemm_selector_predict: no selector loaded");
+    SPG_CUDA_TRY(cudaSetDevice(c->device));
+    if (!B) return SPG_OK;
+    return selector_predict_dev(c->gemm_model, c->gemm_model_k, d_features, B, d_out, pick_stream(c, stream));
 }
 
 int spg_set_spmv_policy(spg_ctx *c, int policy) {
@@ -486,7 +684,7 @@ int spg_selector_predict(spg_ctx *c, const float *d_features, uint32_t B, float 
     if (c->model_k <= 0) return set_error(SPG_ERR_LOGIC, "spg_selector_predict: no selector loaded");
     SPG_CUDA_TRY(cudaSetDevice(c->device));
     if (!B) return SPG_OK;
-    return selector_predict_dev(c, d_features, B, d_out, pick_stream(c, stream));
+    return selector_predict_dev(c->model, c->model_k, d_features, B, d_out, pick_stream(c, stream));
 }
 
 int spg_mlp_forward(spg_ctx *c, const float *d_params, int n_outputs, const float *d_x, uint32_t B, float *d_act,

@@ -1,17 +1,21 @@
-"""The learned SpMV variant selector.
+"""The learned variant selectors (SpMV and SpGEMM).
 
 A small FP32 MLP (40 -> 64 -> 64 -> K) reads 40 features of a locked matrix
-(32-bin log2 row-length histogram + 8 shape statistics, computed on the
-device) and predicts, for each of the K SpMV variants, log(time / fastest
-time). SPG_SPMV_AUTO then takes the argmin. The network is trained on the GPU
-with libspg's own forward / backward / Adam kernels on timings that the
-exhaustive autotuner (spg_spmv_autotune) measures on a generated corpus; the
-autotuner stays the fallback and the yardstick (regret is reported against it).
+(SpMV: 32-bin log2 row-length histogram + 8 shape statistics; SpGEMM of
+A * A: 32-bin log2 histogram of the products per row + 8 statistics; both
+computed on the device) and predicts, for each of the K candidates — SpMV
+(variant, tile) pairs or SpGEMM variants — log(time / fastest time).
+SPG_SPMV_AUTO / SPG_SPGEMM_AUTO then take the argmin. The networks are
+trained on the GPU with libspg's own forward / backward / Adam kernels on
+timings that the exhaustive autotuners (spg_spmv_autotune,
+spg_spgemm_autotune) measure on a generated corpus; the autotuners stay the
+fallback and the yardstick (regret is reported against them).
 
 Corpus: five families (banded with bandwidth 3..201, block-diagonal with
 blocks 4..64, power-law with Zipf alpha 1.5..2.5, uniform-random with
 4..64 nonzeros per row, 2D / 3D stencils), row counts log-uniform in
-[1e3, 4e6], nonzeros capped at NNZ_CAP per matrix (rows are scaled down to
+[1e3, 4e6], nonzeros capped per matrix (NNZ_CAP for SpMV, GEMM_NNZ_CAP for
+SpGEMM, whose products grow with the row lengths; rows are scaled down to
 fit), FP64 values. Matrix i of a corpus is a pure function of (seed, i).
 """
 from __future__ import annotations
@@ -23,11 +27,16 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import (FAM_BANDED, FAM_BLOCKDIAG, FAM_POWERLAW, FAM_STENCIL2D, FAM_STENCIL3D, FAM_UNIFORM, N_FEATURES,
-               N_HIDDEN, SPMV_VARIANTS, Context, Csr, Mlp, gen_family)
+               N_HIDDEN, SPGEMM_VARIANTS, SPMV_VARIANTS, Context, Csr, Mlp, gen_family)
 from . import gen
 
 K = len(SPMV_VARIANTS)
+K_GEMM = len(SPGEMM_VARIANTS)
 NNZ_CAP = 16_000_000
+GEMM_NNZ_CAP = 2_000_000
+# fixed variants "without the selector": the comparison a gain is measured against
+DEFAULT_SPMV = SPMV_VARIANTS["adaptive16"]
+DEFAULT_SPGEMM = SPGEMM_VARIANTS["rowmerge"]
 FAMILY_NAMES = ["banded", "blockdiag", "powerlaw", "uniform", "stencil"]
 
 
@@ -45,7 +54,7 @@ class Spec:
         return f"{self.family}:{self.n_rows}:{self.p}:{self.alpha:.3f}"
 
 
-def corpus_spec(i: int, seed: int) -> Spec:
+def corpus_spec(i: int, seed: int, nnz_cap: int = NNZ_CAP) -> Spec:
     """Matrix i of the corpus drawn with `seed`."""
     u = gen.unit(gen.hash3(seed, 50 + i % 7, np.arange(i * 8, i * 8 + 8, dtype=np.uint64)))
     fam = int(u[0] * 5)
@@ -53,27 +62,33 @@ def corpus_spec(i: int, seed: int) -> Spec:
     s = int(gen.hash3(seed, 60, np.array([i], np.uint64))[0] & np.uint64(0x7FFFFFFF))
     if fam == 0:
         bw = 3 + 2 * int(u[2] * 100)  # 3..201, odd
-        n = max(bw, min(n, NNZ_CAP // bw))
+        n = max(bw, min(n, nnz_cap // bw))
         return Spec(FAM_BANDED, n, bw, seed=s)
     if fam == 1:
         b = 4 + int(u[2] * 61)  # 4..64
-        n = max(b, min(n, NNZ_CAP // b))
+        n = max(b, min(n, nnz_cap // b))
         return Spec(FAM_BLOCKDIAG, n, b, seed=s)
     if fam == 2:
         alpha = 1.5 + u[2]  # 1.5..2.5
         cap = 10_000
         mean_target = 4.0 + u[3] * 28.0
-        n = min(n, int(NNZ_CAP / mean_target))
+        n = min(n, int(nnz_cap / mean_target))
         return Spec(FAM_POWERLAW, max(n, 16), cap, ls=mean_target, alpha=float(alpha), seed=s)
     if fam == 3:
         k = 4 + int(u[2] * 61)  # 4..64
-        n = max(k, min(n, NNZ_CAP // k))
+        n = max(k, min(n, nnz_cap // k))
         return Spec(FAM_UNIFORM, n, k, seed=s)
     if u[2] < 0.5:  # 2D 5-point on side g
-        g = max(4, int(round(math.sqrt(min(n, NNZ_CAP // 5)))))
+        g = max(4, int(round(math.sqrt(min(n, nnz_cap // 5)))))
         return Spec(FAM_STENCIL2D, g * g, g, seed=s)
-    g = max(3, int(round(min(n, NNZ_CAP // 7) ** (1.0 / 3.0))))
+    g = max(3, int(round(min(n, nnz_cap // 7) ** (1.0 / 3.0))))
     return Spec(FAM_STENCIL3D, g ** 3, g, seed=s)
+
+
+def gemm_corpus_spec(i: int, seed: int) -> Spec:
+    """Matrix i of the SpGEMM corpus (C = A * A): the same families with
+    nonzeros capped at GEMM_NNZ_CAP."""
+    return corpus_spec(i, seed, GEMM_NNZ_CAP)
 
 
 def build(ctx: Context, spec: Spec) -> Csr:
@@ -99,22 +114,31 @@ def build(ctx: Context, spec: Spec) -> Csr:
     return A
 
 
-def collect(ctx: Context, indices, seed: int, reps: int = 3, log_every: int = 0):
+def collect(ctx: Context, indices, seed: int, reps: int = 3, log_every: int = 0, op: str = "spmv",
+            time_cap_s: float | None = None):
     """(features [n, 40] float32, times [n, K] float32, specs) for corpus
-    matrices `indices`, labelled by the exhaustive autotuner."""
+    matrices `indices`, labelled by the exhaustive autotuner of `op`
+    ("spmv": the SpMV (variant, tile) candidates of A; "spgemm": the SpGEMM
+    variants of A * A). Stops early once time_cap_s seconds have passed."""
     X, T, S = [], [], []
     t0 = time.time()
     for j, i in enumerate(indices):
-        spec = corpus_spec(int(i), seed)
+        if time_cap_s is not None and time.time() - t0 > time_cap_s:
+            break
+        spec = corpus_spec(int(i), seed) if op == "spmv" else gemm_corpus_spec(int(i), seed)
         A = build(ctx, spec)
-        X.append(A.features())
-        t, _ = A.autotune(reps)
+        if op == "spmv":
+            X.append(A.features())
+            t, _ = A.autotune(reps)
+        else:
+            X.append(A.spgemm_features(A))
+            t, _ = A.spgemm_autotune(A, reps)
         T.append(t)
         S.append(spec)
         A.close()
         if log_every and (j + 1) % log_every == 0:
             print(f"  corpus {j + 1}/{len(indices)}  {time.time() - t0:.1f}s", flush=True)
-    return np.array(X, np.float32), np.array(T, np.float32), S
+    return np.array(X, np.float32).reshape(-1, N_FEATURES), np.array(T, np.float32), S
 
 
 def targets(times: np.ndarray) -> np.ndarray:
@@ -144,8 +168,10 @@ def normalization(X: np.ndarray):
 
 def train(ctx: Context, X: np.ndarray, T: np.ndarray, epochs: int = 400, batch: int = 512, lr: float = 3e-3,
           seed: int = 0, log_every: int = 0):
-    """Train on the GPU with libspg's kernels; returns (blob, loss history)."""
+    """Train on the GPU with libspg's kernels (K = T's columns); returns
+    (blob, loss history)."""
     import torch
+    K = T.shape[1]
     mlp = Mlp(ctx, K)
     mean, scale = normalization(X)
     Xn = ((X - mean) * scale).astype(np.float32)
@@ -191,21 +217,34 @@ def train(ctx: Context, X: np.ndarray, T: np.ndarray, epochs: int = 400, batch: 
     return blob, hist
 
 
-def predict(ctx: Context, blob: np.ndarray, X: np.ndarray) -> np.ndarray:
-    """Predicted log-time ratios [n, K] via the loaded-selector inference path."""
+def blob_outputs(blob: np.ndarray) -> int:
+    """K of a selector blob [mean, scale, W1, b1, W2, b2, W3, b3]."""
+    base = 2 * N_FEATURES + N_HIDDEN * N_FEATURES + N_HIDDEN + N_HIDDEN * N_HIDDEN + N_HIDDEN
+    return (len(blob) - base) // (N_HIDDEN + 1)
+
+
+def predict(ctx: Context, blob: np.ndarray, X: np.ndarray, op: str = "spmv") -> np.ndarray:
+    """Predicted log-time ratios [n, K] via the loaded-selector inference path
+    (installs the blob as the context's `op` selector)."""
     import torch
     from . import _check, _ptr, lib
-    ctx.load_selector(blob, K)
+    Kb = blob_outputs(blob)
+    if op == "spmv":
+        ctx.load_selector(blob, Kb)
+    else:
+        ctx.load_spgemm_selector(blob, Kb)
     Xd = torch.from_numpy(np.ascontiguousarray(X, np.float32)).cuda()
-    out = torch.empty(len(X) * K, dtype=torch.float32, device="cuda")
+    out = torch.empty(max(len(X), 1) * Kb, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
-    _check(lib().spg_selector_predict(ctx.h, _ptr(Xd), len(X), _ptr(out), None))
+    fn = lib().spg_selector_predict if op == "spmv" else lib().spg_spgemm_selector_predict
+    _check(fn(ctx.h, _ptr(Xd), len(X), _ptr(out), None))
     ctx.sync()
-    return out.cpu().numpy().reshape(len(X), K)
+    return out.cpu().numpy()[:len(X) * Kb].reshape(len(X), Kb)
 
 
 def evaluate(T: np.ndarray, choice: np.ndarray, default: int) -> dict:
-    """Regret of `choice` against the exhaustive-autotune best on timings T."""
+    """Regret of `choice` against the exhaustive-autotune best on timings T,
+    and of the fixed `default` (the method without the selector)."""
     n = len(T)
     best = T.min(axis=1)
     t_choice = T[np.arange(n), choice]

@@ -165,3 +165,28 @@ def test_adaptive_model(items, lengths):
 def test_adaptive_model_zipf(items):
     L = gen.zipf_lengths(3000, 1.8, 10_000, 16.0, seed=3)
     check(L, items, seed=4)
+
+
+@pytest.mark.parametrize("sub", [2, 4, 8, 16])
+def test_interleaved_layout_is_a_bijection_read_in_order(sub):
+    """INTERLEAVED's plan-time copy: nonzero p = 512 w + 16 l + u (chunk w,
+    lane l, item u) is written to 512 w + 64 (u // 2) + 2 l + u % 2 (values
+    and columns alike), and the kernel's sub-batch h of SUB items reads pairs
+    at 64 ((SUB h + u) // 2) + 2 l, u = 0, 2, ...: every slot of a chunk is
+    written once, and each lane reads back its own 16 nonzeros in order."""
+    w = 3
+    dst = {}
+    for lane in range(32):
+        for u in range(16):
+            p = 512 * w + 16 * lane + u
+            d = 512 * w + 64 * (u >> 1) + 2 * lane + (u & 1)
+            assert d not in dst
+            dst[d] = p
+    assert sorted(dst) == list(range(512 * w, 512 * w + 512))
+    for lane in range(32):
+        got = []
+        for h in range(16 // sub):
+            for u in range(0, sub, 2):
+                at = 512 * w + 64 * ((sub * h + u) >> 1) + 2 * lane
+                got += [dst[at], dst[at + 1]]
+        assert got == [512 * w + 16 * lane + u for u in range(16)]

@@ -126,17 +126,52 @@ def test_autotune_reports_every_variant(ctx):
 
 @pytest.mark.gpu
 def test_small_training_run_beats_fixed_default(ctx):
-    """Trains on a small corpus; the selector must pick variants whose total
-    time on held-out matrices is no worse than the fixed default's."""
+    """Trains on a small corpus; on held-out matrices the variants the trained
+    network picks must take strictly less total time than the fixed default
+    (the method without the network)."""
     import spira_gb300 as sg
     X, T, specs = S.collect(ctx, range(120), seed=11, reps=2)
     blob, hist = S.train(ctx, X[:100], T[:100], epochs=150, batch=64, lr=3e-3)
     assert hist[-1] < hist[0]
     pred = S.predict(ctx, blob, X[100:])
-    ev = S.evaluate(T[100:], pred.argmin(axis=1), sg.SPMV_ADAPTIVE16)
-    assert ev["total_time_ratio"] <= ev["default_total_time_ratio"] * 1.05, ev
+    ev = S.evaluate(T[100:], pred.argmin(axis=1), S.DEFAULT_SPMV)
+    assert ev["total_time_ratio"] < ev["default_total_time_ratio"], ev
     # AUTO through the installed selector picks a valid variant
     A = S.build(ctx, specs[100])
     ctx.set_spmv_policy(sg.POLICY_SELECTOR)
     assert 0 <= A.selected_spmv() < K
     ctx.load_selector(None, 0)
+
+
+@pytest.mark.gpu
+def test_small_spgemm_training_run_beats_fixed_default(ctx):
+    """The same for the SpGEMM selector (C = A * A on the SpGEMM corpus)."""
+    import spira_gb300 as sg
+    X, T, specs = S.collect(ctx, range(90), seed=13, reps=1, op="spgemm")
+    assert T.shape == (90, S.K_GEMM)
+    blob, hist = S.train(ctx, X[:70], T[:70], epochs=150, batch=32, lr=3e-3)
+    assert hist[-1] < hist[0]
+    pred = S.predict(ctx, blob, X[70:], op="spgemm")
+    ev = S.evaluate(T[70:], pred.argmin(axis=1), S.DEFAULT_SPGEMM)
+    assert ev["total_time_ratio"] < ev["default_total_time_ratio"], ev
+    A = S.build(ctx, S.gemm_corpus_spec(70, 13))
+    ctx.set_spgemm_policy(sg.POLICY_SELECTOR)
+    assert 0 <= A.spgemm_selected(A) < S.K_GEMM
+    ctx.load_spgemm_selector(None, 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op, first, n, bound", [("spmv", 20_000, 60, 1.05), ("spgemm", 4_000, 40, 1.10)])
+def test_shipped_selector_on_unseen_matrices(ctx, op, first, n, bound):
+    """The shipped model, on corpus matrices past its training range: total
+    time within `bound` of exhaustive autotuning, and below the fixed
+    default's."""
+    import spira_gb300 as sg
+    path = sg._PKG / ("spg_selector.bin" if op == "spmv" else "spg_spgemm_selector.bin")
+    blob = np.fromfile(path, dtype=np.float32)
+    assert S.blob_outputs(blob) == (S.K if op == "spmv" else S.K_GEMM)
+    X, T, _ = S.collect(ctx, range(first, first + n), seed=7, reps=2, op=op)
+    ev = S.evaluate(T, S.predict(ctx, blob, X, op=op).argmin(axis=1),
+                    S.DEFAULT_SPMV if op == "spmv" else S.DEFAULT_SPGEMM)
+    assert ev["total_time_ratio"] <= bound, ev
+    assert ev["total_time_ratio"] < ev["default_total_time_ratio"], ev

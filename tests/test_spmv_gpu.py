@@ -299,3 +299,18 @@ def test_host_spmv_multi_builds_plans_before_recording(ctx):
     ctx.sync()
     for A, (v, _, _), x, y in zip(mats, specs, xs, ys):
         np.testing.assert_array_equal(y.numpy(), A.spmv_host(x.numpy().copy(), variant=v))
+
+
+@pytest.mark.parametrize("tile, base", [("interleaved_s4", "interleaved"), ("interleaved_s8", "interleaved"),
+                                        ("interleaved", "adaptive16"), ("adaptive16_s4", "adaptive16"),
+                                        ("adaptive_s16", "adaptive")])
+def test_spmv_tiles_give_their_variants_bits(ctx, tile, base):
+    """A tile changes only how many nonzeros a lane loads before its FMAs and
+    how many blocks share an SM, never a lane's FMA order: y is bit-identical
+    to its variant's (INTERLEAVED is ADAPTIVE16's arithmetic)."""
+    r, c, v = gen.zipf_rows(30_000, seed=21)
+    A = build(ctx, 30_000, 30_000, [(r, c, v)])
+    x = gen.dense_x(30_000, 22)
+    y_t = A.spmv_host(x, variant=sg.SPMV_VARIANTS[tile])
+    y_b = A.spmv_host(x, variant=sg.SPMV_VARIANTS[base])
+    np.testing.assert_array_equal(y_t.view(np.uint64), y_b.view(np.uint64))

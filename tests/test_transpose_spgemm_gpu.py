@@ -43,9 +43,14 @@ def test_transpose_kats(ctx, case):
     assert_csr_equal(T.download(), _gold_csr(case["T"]))
 
 
+VARIANTS = list(sg.SPGEMM_VARIANTS.values())
+VARIANT_IDS = list(sg.SPGEMM_VARIANTS.keys())
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=VARIANT_IDS)
 @pytest.mark.parametrize("case", GOLD["spgemm"], ids=[k["name"] for k in GOLD["spgemm"]])
-def test_spgemm_kats(ctx, case):
-    Cm = dev(ctx, _gold_csr(case["A"])).spgemm(dev(ctx, _gold_csr(case["B"])))
+def test_spgemm_kats(ctx, case, variant):
+    Cm = dev(ctx, _gold_csr(case["A"])).spgemm(dev(ctx, _gold_csr(case["B"])), variant)
     assert_csr_equal(Cm.download(), _gold_csr(case["C"]))
 
 
@@ -58,9 +63,10 @@ def test_golden_workload_digests(ctx, rec):
     for e in ep:
         A.lock(*e)
     assert oracle.csr_digest(A.transpose().download()) == rec["transpose_sha256"]
-    Cm = A.spgemm(A)
-    assert Cm.nnz == rec["spgemm_nnz"]
-    assert oracle.csr_digest(Cm.download()) == rec["spgemm_sha256"]
+    for v in VARIANTS:
+        Cm = A.spgemm(A, v)
+        assert Cm.nnz == rec["spgemm_nnz"], sg.SPGEMM_NAMES[v]
+        assert oracle.csr_digest(Cm.download()) == rec["spgemm_sha256"], sg.SPGEMM_NAMES[v]
 
 
 @pytest.mark.parametrize("shape", [(1, 1), (5, 9), (9, 5), (1, 70_000), (70_000, 1), (3000, 3000)])
@@ -107,7 +113,8 @@ def test_transpose_zipf_long_rows(ctx):
     assert_csr_equal(A.transpose().download(), oracle.transpose(A.download()))
 
 
-def test_spgemm_cancellation_and_rectangular(ctx):
+@pytest.mark.parametrize("variant", VARIANTS, ids=VARIANT_IDS)
+def test_spgemm_cancellation_and_rectangular(ctx, variant):
     # integer values: exact products, cancellations produce exact zeros to drop
     ctr = np.arange(60_000, dtype=np.uint64)
     r = gen.below(gen.hash3(2, 1, ctr), 3000)
@@ -117,14 +124,16 @@ def test_spgemm_cancellation_and_rectangular(ctx):
     ctr2 = np.arange(20_000, dtype=np.uint64)
     B = locked(ctx, 500, 4000, gen.below(gen.hash3(3, 1, ctr2), 500), gen.below(gen.hash3(3, 2, ctr2), 4000),
                (gen.below(gen.hash3(3, 3, ctr2), 5).astype(np.int64) - 2).astype(np.float64))
-    Cm = A.spgemm(B)
+    Cm = A.spgemm(B, variant)
     assert_csr_equal(Cm.download(), oracle.spgemm(A.download(), B.download()))
 
 
-def test_spgemm_every_row_class(ctx):
+@pytest.mark.parametrize("variant", VARIANTS, ids=VARIANT_IDS)
+def test_spgemm_every_row_class(ctx, variant):
     """Rows for each SpGEMM path: merge with <= 8 A entries, merge with 9..32,
-    expand-sort for > 32 entries and for > 4096 products; exact cancellations
-    (integer values) included. Bit-exact against the oracle."""
+    expand-sort for > 32 entries and for > 4096 products; warp sorts of 1, 2,
+    4 and 8 items per lane and heavy rows for the warp-sort tiles; exact
+    cancellations (integer values) included. Bit-exact against the oracle."""
     n = 3000
     lengths = np.array([0, 1, 3, 8, 9, 20, 32, 33, 60, 5] * (n // 10), np.int64)
     lengths[7::50] = 2000  # long rows: as B rows they push products past 4096
@@ -135,8 +144,78 @@ def test_spgemm_every_row_class(ctx):
     vals[::5] = gen.sym_unit(gen.hash3(5, 3, ctr[::5]))
     A = locked(ctx, n, n, rows, cols, vals)
     H = A.download()
-    Cm = A.spgemm(A)
+    Cm = A.spgemm(A, variant)
     assert_csr_equal(Cm.download(), oracle.spgemm(H, H))
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=VARIANT_IDS)
+def test_spgemm_edge_shapes(ctx, variant):
+    """Empty matrices, no products at all, one row, rows without products
+    between long runs, and a B with more than 2^26 columns (the warp sort's
+    64-bit keys)."""
+    E = locked(ctx, 0, 0, np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0))
+    C0 = E.spgemm(E, variant)
+    assert C0.nnz == 0 and C0.n_rows == 0
+    Z = locked(ctx, 50, 50, np.array([3], np.uint32), np.array([7], np.uint32), np.array([1.5]))
+    Cz = Z.spgemm(Z, variant)  # row 3 names B row 7, which is empty
+    assert_csr_equal(Cz.download(), oracle.spgemm(Z.download(), Z.download()))
+    n = 5000
+    rows = np.array([0, 0, 1, 2500, 2500, 4999], np.uint32)
+    cols = np.array([0, 2500, 4999, 0, 1, 2500], np.uint32)
+    A = locked(ctx, n, n, rows, cols, np.array([1.0, -2.0, 3.0, 0.5, 0.25, 4.0]))
+    H = A.download()
+    assert_csr_equal(A.spgemm(A, variant).download(), oracle.spgemm(H, H))
+    wide = (1 << 26) + 5
+    ctr = np.arange(3000, dtype=np.uint64)
+    B = locked(ctx, 300, wide, gen.below(gen.hash3(4, 1, ctr), 300), gen.below(gen.hash3(4, 2, ctr), wide),
+               gen.sym_unit(gen.hash3(4, 3, ctr)))
+    A2 = locked(ctx, 200, 300, gen.below(gen.hash3(5, 1, ctr), 200), gen.below(gen.hash3(5, 2, ctr), 300),
+                gen.sym_unit(gen.hash3(5, 3, ctr)))
+    assert_csr_equal(A2.spgemm(B, variant).download(), oracle.spgemm(A2.download(), B.download()))
+
+
+def test_spgemm_against_fused_order_within_tolerance(ctx):
+    """Spira built with FMA contraction (GCC's default on aarch64) sums
+    acc = fma(a, b, acc); the engine reproduces the uncontracted build bit for
+    bit, and stays within 1e-12 (relative to sum |a_ik b_kj|) of the
+    contracted order, with the same structure on generic values."""
+    n = 20_000
+    r, c, v = gen.uniform_rows(n, n, 12, seed=88)
+    A = locked(ctx, n, n, r, c, v)
+    H = A.download()
+    F = oracle.spgemm(H, H, fused=True)
+    Habs = H._replace(vals=np.abs(H.vals))
+    S = oracle.spgemm(Habs, Habs)  # per entry: sum of |a_ik b_kj|
+    for variant in VARIANTS:
+        G = A.spgemm(A, variant).download()
+        np.testing.assert_array_equal(G.off, F.off)
+        np.testing.assert_array_equal(G.cols, F.cols)
+        np.testing.assert_array_equal(S.cols, G.cols)
+        assert np.all(np.abs(G.vals - F.vals) <= 1e-12 * S.vals)
+
+
+def test_spgemm_selection(ctx):
+    """AUTO resolves to a valid variant under each policy; the autotuner
+    times every variant; the features describe the products per row."""
+    n = 30_000
+    r, c, v = gen.uniform_rows(n, n, 8, seed=3)
+    A = locked(ctx, n, n, r, c, v)
+    t, best = A.spgemm_autotune(A, 2)
+    assert len(t) == len(VARIANTS) and np.all(t > 0) and best == int(np.argmin(t))
+    f = A.spgemm_features(A)
+    H = A.download()
+    blen = np.diff(H.off.astype(np.int64))
+    cs = np.concatenate([[0], np.cumsum(blen[H.cols.astype(np.int64)])])
+    prods = cs[H.off[1:].astype(np.int64)] - cs[H.off[:-1].astype(np.int64)]
+    bins = np.where(prods > 0, 1 + np.floor(np.log2(np.maximum(prods, 1))).astype(np.int64), 0)
+    np.testing.assert_allclose(f[:32], np.bincount(np.minimum(bins, 31), minlength=32) / n, atol=1e-6)
+    assert abs(f[38] - np.log2(prods.max() + 1) / 32) < 1e-6
+    for policy in (sg.POLICY_AUTOTUNE, sg.POLICY_FIXED, sg.POLICY_SELECTOR):
+        ctx.set_spgemm_policy(policy)
+        B = locked(ctx, n, n, r, c, v)
+        assert 0 <= B.spgemm_selected(B) < len(VARIANTS)
+        assert_csr_equal(B.spgemm(B).download(), oracle.spgemm(B.download(), B.download()))
+    ctx.set_spgemm_policy(sg.POLICY_SELECTOR)
 
 
 def test_spgemm_errors(ctx):
@@ -158,9 +237,10 @@ def test_spgemm_transpose_laplacian_3a_full(ctx):
     A = locked(ctx, n, n, r, c, v)
     assert A.nnz == 6_940_000
     H = A.download()
-    Cm = A.spgemm(A)
-    assert Cm.nnz <= 24_581_200
-    assert_csr_equal(Cm.download(), oracle.spgemm(H, H))
+    ref = oracle.spgemm(H, H)
+    assert ref.cols.size <= 24_581_200
+    for v in VARIANTS:
+        assert_csr_equal(A.spgemm(A, v).download(), ref)
     assert_csr_equal(A.transpose().download(), oracle.transpose(H))
 
 
@@ -170,6 +250,7 @@ def test_spgemm_transpose_uniform_3b_full(ctx):
     r, c, v = gen.uniform_rows(n, n, 8, seed=77)
     A = locked(ctx, n, n, r, c, v)
     H = A.download()
-    Cm = A.spgemm(A)
-    assert_csr_equal(Cm.download(), oracle.spgemm(H, H))
+    ref = oracle.spgemm(H, H)
+    for v in VARIANTS:
+        assert_csr_equal(A.spgemm(A, v).download(), ref)
     assert_csr_equal(A.transpose().download(), oracle.transpose(H))
