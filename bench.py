@@ -617,11 +617,19 @@ def run_ops(ctx, peak):
                 B.lock(*first)
                 B.close()
             t_e2e = wall(do_host)[0]
-            ser_first, _ = cpu(lambda: oracle.lock_epochs(n, n, [first]))
-            ser_both, _ = cpu(lambda: oracle.lock_epochs(n, n, [first, delta]))
-            ser_relock = max(ser_both - ser_first, 0.0)
-            secs, _ = oracle.lock_parallel_time(n, n, [first, delta], nthr)
-            cpu_first, cpu_relock = secs[0] * 1e3, secs[1] * 1e3
+            # each epoch timed on its own inside the port (the second epoch's
+            # time is the relock alone); one thread is Spira's serial path
+            secs1, _ = oracle.lock_parallel_time(n, n, [first, delta], 1)
+            ser_first, ser_relock = secs1[0] * 1e3, secs1[1] * 1e3
+            host_epochs = [first, delta]
+        else:
+            # the same first epoch, copied back from the device; the serial
+            # path is skipped here (it alone would take most of a minute)
+            host_epochs = [(d_first[0][:m].cpu().numpy().view(np.uint32), d_first[1][:m].cpu().numpy().view(np.uint32),
+                            d_first[2][:m].cpu().numpy()), delta]
+        secs, _ = oracle.lock_parallel_time(n, n, host_epochs, nthr)
+        cpu_first, cpu_relock = secs[0] * 1e3, secs[1] * 1e3
+        del host_epochs
         out["lock"].append(rec(f"{name}_first", t_first, lock_bytes(n, m, 0, nnz0), cpu_first, ser_first,
                                staged=int(m), nnz=int(nnz0), staging="device",
                                **({"e2e_ms_host_staging": round(t_e2e, 3)} if t_e2e else {})))
@@ -823,6 +831,7 @@ PROFILE_CASES = {
     "zipf4m": (ZIPF_N, "zipf"),
     # lock / transpose / SpGEMM: `--reps` calls of the operation
     "lock_zipf1m": (1_000_000, "lock"),
+    "lock_zipf4m": (ZIPF_N, "lock"),
     "lock_laplacian2d": (GRID * GRID, "lock"),
     "relock_zipf1m": (1_000_000, "relock"),
     "batched256": (256, "batched"),  # the batched workload's first 256 matrices

@@ -399,7 +399,9 @@ int spg_spgemm_selected(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, int *v
 /* The 40 SpGEMM selector features of A * B (host array): 32-bin log2
  * histogram of the products per row of A, then log sizes (rows, B's
  * columns, nnz of A, products), mean / spread / maximum products per row and
- * the mean A row length. */
+ * the column spread of A (mean |col / n_cols - row / n_rows| over the first
+ * and last entry of sampled rows: small for banded, block and stencil
+ * patterns, whose products collapse onto few columns). */
 int spg_spgemm_features(spg_ctx *ctx, const spg_csr *A, const spg_csr *B, float *features);
 /* Times every SpGEMM variant on A * B (median of `reps` runs after one
  * warm-up, wall clock around the complete call: the calls synchronise):

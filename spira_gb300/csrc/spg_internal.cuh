@@ -309,10 +309,11 @@ int exclusive_scan_i64(Ctx *c, int64_t *d_data, uint64_t n, cudaStream_t s);
 int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
                          int key_bits, cudaStream_t s);
 // Stable (row, col) order of m pairs whose rows are non-decreasing, sorted
-// row by row on chip: keys_out = row << cbits | col, idx_out = input position.
+// row by row on chip (rows of up to 32 entries in registers, longer ones in
+// shared memory): keys_out = row << cbits | col, idx_out = input position.
 // s_off[r] = first position of row r (n_rows + 1 entries). *done = false when
-// some tile cannot be sorted on chip (a row of more than ~10 000 entries, or
-// a key wider than 32 bits inside a tile); the outputs are then undefined.
+// a row has more than 12 288 entries or columns need more than 26 bits; the
+// outputs are then undefined.
 int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
                       uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s);
 

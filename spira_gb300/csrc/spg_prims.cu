@@ -395,27 +395,228 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 
 // ---------------------------------------------------------------------------
 // Row-grouped sort: pairs (row, col) whose rows are already non-decreasing
-// (rows[i] <= rows[i+1]) are put in stable (row, col) order by sorting each
-// row's entries by column in shared memory, tile by tile. Tile t holds the
-// rows whose first entry lies in [t*TS_SPAN, (t+1)*TS_SPAN): its entries
-// [start_t, start_{t+1}) are contiguous and already in row order, so sorting
-// inside the tile by (row, column), stably, puts them in their final global
-// places. The sort is an LSD radix sort (8-bit digits) of 32-bit composite
-// keys (row - first row of the tile, column) with 16-bit tile indices,
-// ping-ponged in shared memory. Warp w owns positions [512 w, 512 w + 512) of
-// every pass (16 warps of 256 measured slower); each scatter also counts, per
-// destination slice, the digit of the next pass, so a pass is one sweep.
-// Tiles of at most TS_SMALL entries (three blocks per SM) and tiles of up to
-// TS_MAX (one holding a long row; one block per SM) run as two launches over
-// a tile plan. A tile longer than
-// TS_MAX (a row of more than ~10 000 entries) or whose key needs more than 32
-// bits makes the sort report failure; callers then sort globally.
+// (rows[i] <= rows[i+1], so row r's entries are [s_off[r], s_off[r+1])) are
+// put in stable (row, col) order by sorting every row by column on its own.
+// Rows are sorted by length class:
+//   * one entry: written through by the planning pass;
+//   * 2..32 entries: a bitonic network in registers, 32 / P rows of padded
+//     length P (2, 4, 8, 16, 32) per warp, keys (col << 5 | position), so the
+//     network's order is the stable order;
+//   * 33..SEG_SPAN entries: grouped by the span of SEG_SPAN input positions
+//     their first entry lies in (at most 63 such rows start in one span, as
+//     they lie 33 or more positions apart; together < 2 SEG_SPAN entries) and
+//     sorted tile by tile in shared memory: an LSD radix sort (8-bit digits)
+//     of 32-bit keys (rank of the row in the tile, col) with 16-bit tile
+//     positions, ping-ponged in shared memory; warp w owns positions
+//     [512 w, 512 w + 512) of every pass, and each scatter also counts, per
+//     destination slice, the digit of the next pass, so a pass is one sweep;
+//   * SEG_SPAN+1..TS_MAX entries: a tile of its own, sorted the same way (no
+//     rank bits: ceil(cbits / 8) passes); rows up to TS_SMALL entries in the
+//     kernel of the span tiles (three blocks per SM), longer ones in a kernel
+//     of one block per SM.
+// A tile's key needs rank bits (at most 6) + cbits <= 32, so columns of more
+// than 26 bits, and a row longer than TS_MAX, make the sort report failure;
+// callers then sort globally. Work lists are filled with atomics, in no
+// particular order: every row's output places are fixed by s_off, so the
+// result does not depend on that order.
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int TS_SPAN = 2048;
-constexpr int TS_SMALL = 4096, TS_SLICE_SMALL = 512;  // 8 warps
+constexpr int SEG_SPAN = 2048;
+constexpr int SEG_TILE_ROWS = 64;  // medium rows starting in one span: at most 63
+constexpr int TS_SMALL = 4096, TS_SLICE_SMALL = 512;  // 8 warps; a span's medium rows: < 2 SEG_SPAN
 constexpr int TS_MAX = 12288, TS_SLICE_LARGE = 512;   // 24 warps
+constexpr int SEG_MAX_CBITS = 26;
+constexpr uint64_t SEG_ROW_JOB = 1ull << 63;  // large job naming one row (else a span tile)
+
+// counters (unsigned) of the plan
+enum : int {
+    SC_SHORT = 0,       // [1..5]: rows of padded length 2^c
+    SC_SMALL = 6,       // small jobs: span tiles, rows of SEG_SPAN+1..TS_SMALL entries
+    SC_LARGE = 7,       // large jobs: rows of TS_SMALL+1..TS_MAX entries
+    SC_OVERFLOW = 8,    // a row or a tile the on-chip sort cannot take
+    SC_CURSOR = 9,      // [9 + c]: fill cursors of the short classes
+    SC_N = 16
+};
+
+// 0: nothing to sort (0 or 1 entry), 1..5: short of padded length 2^c,
+// 6: medium (span tile), 7: a small job of its own, 8: a large job of its
+// own, 9: too long.
+__device__ __forceinline__ int seg_class(uint64_t L) {
+    if (L <= 1) return 0;
+    if (L <= 32) return 32 - __clz((unsigned)(L - 1));
+    if (L <= (uint64_t)SEG_SPAN) return 6;
+    if (L <= (uint64_t)TS_SMALL) return 7;
+    if (L <= (uint64_t)TS_MAX) return 8;
+    return 9;
+}
+
+// Counts the short rows of every class.
+__global__ void __launch_bounds__(256) seg_count(const uint64_t *__restrict__ s_off, uint64_t n_rows,
+                                                 unsigned *__restrict__ ctr) {
+    __shared__ unsigned sc[6];
+    if (threadIdx.x < 6) sc[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n_rows;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        const int c = seg_class(s_off[r + 1] - s_off[r]);
+        if (c >= 1 && c <= 5) atomicAdd(&sc[c], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x >= 1 && threadIdx.x <= 5 && sc[threadIdx.x]) atomicAdd(&ctr[SC_SHORT + threadIdx.x], sc[threadIdx.x]);
+}
+
+// Writes single-entry rows through, lists short rows by class (class c in
+// short_rows[base_c ...], base_c = rows of the classes below), medium rows by
+// span tile (tile_rows[t * SEG_TILE_ROWS + k], tile_len[t] = their entries)
+// and longer rows as small or large jobs of their own.
+__global__ void __launch_bounds__(256) seg_place(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
+                                                 uint64_t n_rows, int cbits, unsigned *__restrict__ ctr,
+                                                 uint32_t *__restrict__ short_rows, unsigned *__restrict__ tile_cnt,
+                                                 unsigned *__restrict__ tile_len, uint32_t *__restrict__ tile_rows,
+                                                 uint64_t *__restrict__ small_jobs,
+                                                 uint64_t *__restrict__ large_jobs, uint64_t *__restrict__ keys_out,
+                                                 uint32_t *__restrict__ idx_out) {
+    __shared__ unsigned sc[8], sbase[8];
+    unsigned base[6];
+    base[0] = 0;
+#pragma unroll
+    for (int c = 1; c <= 5; ++c) base[c] = base[c - 1] + (c > 1 ? ctr[SC_SHORT + c - 1] : 0u);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_iter = (n_rows + stride - 1) / stride;  // the same for every thread: block-wide syncs below
+    for (uint64_t it = 0; it < n_iter; ++it) {
+        const uint64_t r = it * stride + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+        if (threadIdx.x < 8) sc[threadIdx.x] = 0;
+        __syncthreads();
+        int c = 0;
+        unsigned slot = 0;
+        uint64_t b = 0, L = 0;
+        if (r < n_rows) {
+            b = s_off[r];
+            L = s_off[r + 1] - b;
+            c = seg_class(L);
+            if (L == 1) {
+                keys_out[b] = ((uint64_t)r << cbits) | cols[b];
+                idx_out[b] = (uint32_t)b;
+            } else if (c >= 1 && c <= 5) {
+                slot = atomicAdd(&sc[c], 1u);
+            } else if (c == 7 || c == 8) {
+                slot = atomicAdd(&sc[c - 1], 1u);  // sc[6]: small, sc[7]: large
+            } else if (c == 6) {
+                const uint64_t t = b / SEG_SPAN;
+                const unsigned k = atomicAdd(&tile_cnt[t], 1u);
+                if (k < SEG_TILE_ROWS) {
+                    tile_rows[t * SEG_TILE_ROWS + k] = (uint32_t)r;
+                    atomicAdd(&tile_len[t], (unsigned)L);
+                } else {
+                    atomicOr(&ctr[SC_OVERFLOW], 1u);  // (not reachable: rows of > 32 entries start 33 apart)
+                }
+            } else if (c == 9) {
+                atomicOr(&ctr[SC_OVERFLOW], 1u);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x >= 1 && threadIdx.x <= 5 && sc[threadIdx.x])
+            sbase[threadIdx.x] = atomicAdd(&ctr[SC_CURSOR + threadIdx.x], sc[threadIdx.x]);
+        if (threadIdx.x == 6 && sc[6]) sbase[6] = atomicAdd(&ctr[SC_SMALL], sc[6]);
+        if (threadIdx.x == 7 && sc[7]) sbase[7] = atomicAdd(&ctr[SC_LARGE], sc[7]);
+        __syncthreads();
+        if (r < n_rows) {
+            if (c >= 1 && c <= 5) short_rows[base[c] + sbase[c] + slot] = (uint32_t)r;
+            else if (c == 7) small_jobs[sbase[6] + slot] = SEG_ROW_JOB | r;
+            else if (c == 8) large_jobs[sbase[7] + slot] = SEG_ROW_JOB | r;
+        }
+        __syncthreads();
+    }
+}
+
+// Span tiles holding medium rows onto the small job list (one atomic per warp).
+__global__ void seg_tiles(const unsigned *__restrict__ tile_len, uint64_t n_spans, unsigned *__restrict__ ctr,
+                          uint64_t *__restrict__ small_jobs) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const unsigned E = t < n_spans ? tile_len[t] : 0u;
+    if (E > (unsigned)TS_SMALL) atomicOr(&ctr[SC_OVERFLOW], 1u);  // (not reachable: < 2 SEG_SPAN)
+    const bool take = E != 0 && E <= (unsigned)TS_SMALL;
+    const unsigned want = __ballot_sync(0xffffffffu, take);
+    if (!want) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(&ctr[SC_SMALL], (unsigned)__popc(want));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take) small_jobs[base + __popc(want & ((1u << lane) - 1u))] = t;
+}
+
+// Bitonic sort of aligned P-lane segments of the warp, ascending in every
+// segment (P a power of two, <= 32).
+template <int P>
+__device__ __forceinline__ uint32_t segment_bitonic(uint32_t key, int lane) {
+#pragma unroll
+    for (int k = 2; k <= P; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t other = __shfl_xor_sync(0xffffffffu, key, j);
+            const bool up = k == P || (lane & k) == 0;  // direction of this lane's k-block
+            const bool low = (lane & j) == 0;           // lower partner keeps the smaller in an up block
+            key = (low == up) ? min(key, other) : max(key, other);
+        }
+    }
+    return key;
+}
+
+template <int P>
+__device__ __forceinline__ void sort_short_group(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
+                                                 const uint32_t *__restrict__ list, unsigned n_list, unsigned group,
+                                                 int cbits, uint64_t *__restrict__ keys_out,
+                                                 uint32_t *__restrict__ idx_out, int lane) {
+    const unsigned i = group * (32 / P) + lane / P;
+    const int j = lane % P;
+    uint32_t key = 0xFFFFFFFFu;  // real keys stay below 2^31: cbits <= 26
+    uint64_t b = 0, L = 0, r = 0;
+    if (i < n_list) {
+        r = list[i];
+        b = s_off[r];
+        L = s_off[r + 1] - b;
+        if ((uint64_t)j < L) key = (cols[b + j] << 5) | (uint32_t)j;
+    }
+    key = segment_bitonic<P>(key, lane);
+    if ((uint64_t)j < L) {
+        keys_out[b + j] = (r << cbits) | (key >> 5);
+        idx_out[b + j] = (uint32_t)(b + (key & 31u));
+    }
+}
+
+// Short rows: warp job g of class c sorts rows [g * 32 / P, (g + 1) * 32 / P)
+// of that class's list; jobs of all classes in one grid-stride sweep.
+__global__ void __launch_bounds__(256) seg_short_sort(const uint32_t *__restrict__ cols,
+                                                      const uint64_t *__restrict__ s_off,
+                                                      const uint32_t *__restrict__ short_rows,
+                                                      const unsigned *__restrict__ ctr, int cbits,
+                                                      uint64_t *__restrict__ keys_out, uint32_t *__restrict__ idx_out) {
+    unsigned cnt[6], base[6], jobs_end[6];
+    cnt[0] = base[0] = jobs_end[0] = 0;
+#pragma unroll
+    for (int c = 1; c <= 5; ++c) {
+        cnt[c] = ctr[SC_SHORT + c];
+        base[c] = base[c - 1] + cnt[c - 1];
+        const unsigned per = 32u >> c;  // rows per warp
+        jobs_end[c] = jobs_end[c - 1] + (cnt[c] + per - 1) / per;
+    }
+    const int lane = threadIdx.x & 31;
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned job = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); job < jobs_end[5]; job += warps) {
+        int c = 1;
+        while (job >= jobs_end[c]) ++c;  // warp-uniform
+        const unsigned g = job - jobs_end[c - 1];
+        const uint32_t *list = short_rows + base[c];
+        switch (c) {
+            case 1: sort_short_group<2>(cols, s_off, list, cnt[1], g, cbits, keys_out, idx_out, lane); break;
+            case 2: sort_short_group<4>(cols, s_off, list, cnt[2], g, cbits, keys_out, idx_out, lane); break;
+            case 3: sort_short_group<8>(cols, s_off, list, cnt[3], g, cbits, keys_out, idx_out, lane); break;
+            case 4: sort_short_group<16>(cols, s_off, list, cnt[4], g, cbits, keys_out, idx_out, lane); break;
+            default: sort_short_group<32>(cols, s_off, list, cnt[5], g, cbits, keys_out, idx_out, lane); break;
+        }
+    }
+}
 
 template <int MAXE, int SLICE>
 struct TileSortSmem {
@@ -423,140 +624,147 @@ struct TileSortSmem {
     uint16_t idx[2][MAXE];
     unsigned cnt[2][MAXE / SLICE][256];
     unsigned wsum[8];
+    uint64_t start[SEG_TILE_ROWS];  // first input position of the tile's rows, by rank
+    uint32_t row[SEG_TILE_ROWS];
+    unsigned pref[SEG_TILE_ROWS + 1];  // tile position of each rank's first entry
+    unsigned n_rows;
 };
 
-__device__ __forceinline__ uint64_t first_row_at_or_after(const uint64_t *__restrict__ s_off, uint64_t n,
-                                                          uint64_t pos) {
-    uint64_t lo = 0, hi = n;  // first r in [0, n] with s_off[r] >= pos
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if (s_off[mid] < pos) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// First row of every tile (entry n_tiles: n_rows), and the tiles sorted into
-// a list of small ones (<= TS_SMALL entries) and a list of large ones (<=
-// TS_MAX); *overflow = 1 if a tile is longer. List order does not matter: the
-// tiles are independent.
-__global__ void tile_plan(const uint64_t *__restrict__ s_off, uint64_t n_rows, uint64_t n_tiles,
-                          uint64_t *__restrict__ tile_r0, unsigned *__restrict__ small_list,
-                          unsigned *__restrict__ large_list, unsigned *__restrict__ counts /* [2] */,
-                          unsigned *__restrict__ overflow) {
-    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (t > n_tiles) return;
-    const uint64_t r0 = t == n_tiles ? n_rows : first_row_at_or_after(s_off, n_rows, t * TS_SPAN);
-    tile_r0[t] = r0;
-    if (t == n_tiles) return;
-    const uint64_t r1 = first_row_at_or_after(s_off, n_rows, (t + 1) * TS_SPAN);
-    const uint64_t E = s_off[r1] - s_off[r0];
-    if (E == 0) return;
-    if (E <= (uint64_t)TS_SMALL) small_list[atomicAdd(counts, 1u)] = (unsigned)t;
-    else if (E <= (uint64_t)TS_MAX) large_list[atomicAdd(counts + 1, 1u)] = (unsigned)t;
-    else *overflow = 1u;
-}
-
-// Sorts the tiles of `list` (each of at most MAXE entries); one warp per
-// TS_SLICE entries.
-template <int MAXE, int TS_SLICE>
-__global__ void __launch_bounds__(MAXE / TS_SLICE * 32)
-grouped_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
-                  const uint64_t *__restrict__ s_off, const uint64_t *__restrict__ tile_r0,
-                  const unsigned *__restrict__ list, int cbits, uint64_t *__restrict__ keys_out,
-                  uint32_t *__restrict__ idx_out, unsigned *__restrict__ overflow) {
-    constexpr int W = MAXE / TS_SLICE, T = W * 32;
+// Sorts the tiles of a job list (MAXE entries at most): a span tile's medium
+// rows, or (jobs with SEG_ROW_JOB set) one long row. Persistent blocks take
+// jobs in a grid-stride loop; one warp per SLICE entries.
+template <int MAXE, int SLICE>
+__global__ void __launch_bounds__(MAXE / SLICE * 32)
+seg_tile_sort(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
+              const unsigned *__restrict__ tile_cnt, const uint32_t *__restrict__ tile_rows,
+              const uint64_t *__restrict__ jobs, const unsigned *__restrict__ n_jobs, int cbits,
+              uint64_t *__restrict__ keys_out, uint32_t *__restrict__ idx_out, unsigned *__restrict__ overflow) {
+    constexpr int W = MAXE / SLICE, T = W * 32;
     extern __shared__ __align__(16) unsigned char ts_raw[];
-    TileSortSmem<MAXE, TS_SLICE> &S = *reinterpret_cast<TileSortSmem<MAXE, TS_SLICE> *>(ts_raw);
+    TileSortSmem<MAXE, SLICE> &S = *reinterpret_cast<TileSortSmem<MAXE, SLICE> *>(ts_raw);
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const unsigned tile = list[blockIdx.x];
-    const uint64_t r0 = tile_r0[tile], r1 = tile_r0[tile + 1];
-    const uint64_t start = s_off[r0], end = s_off[r1];
-    const uint64_t E64 = end - start;
-    if (E64 == 0 || E64 > (uint64_t)MAXE) return;  // (the plan never lists such tiles)
-    const int E = (int)E64;
-    const unsigned span = (unsigned)(r1 - r0 - 1);  // largest row offset inside the tile
-    const int bits = (span ? 32 - __clz(span) : 0) + cbits;
-    if (bits > 32 || cbits >= 32) {
-        if (t == 0) *overflow = 1u;
-        return;
-    }
-    const int passes = (bits + 7) / 8;
-    for (int e = t; e < E; e += T) {
-        S.key[0][e] = ((rows[start + e] - (uint32_t)r0) << cbits) | cols[start + e];
-        S.idx[0][e] = (uint16_t)e;
-    }
-    for (int i = t; i < 2 * W * 256; i += T) (&S.cnt[0][0][0])[i] = 0;
-    __syncthreads();
-    const int q0 = warp * TS_SLICE, q1 = min(E, q0 + TS_SLICE);
-    // digit counts of the first pass, per warp slice
-    for (int q = q0; q < q1 && passes > 0; q += 32) {
-        const int qq = q + lane;
-        const bool ok = qq < q1;
-        const unsigned valid = __ballot_sync(0xffffffffu, ok);
-        const unsigned d = ok ? (S.key[0][qq] & 0xFFu) : 0u;
-        const unsigned peers = warp_match_digit<8>(d) & valid;
-        if (ok && (peers & lanemask_lt()) == 0) S.cnt[0][warp][d] += __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    int cur = 0;
-    for (int p = 0; p < passes; ++p) {
-        const int c = p & 1, shift = 8 * p;
-        // digit t: start of each warp slice's run, then across digits
-        unsigned excl = 0;
-        if (t < 256) {
-            unsigned tot = 0;
-            for (int w = 0; w < W; ++w) {
-                const unsigned v = S.cnt[c][w][t];
-                S.cnt[c][w][t] = tot;
-                tot += v;
+    const unsigned nj = *n_jobs;
+    for (unsigned jb = blockIdx.x; jb < nj; jb += gridDim.x) {
+        const uint64_t job = jobs[jb];
+        if (job & SEG_ROW_JOB) {
+            if (t == 0) {
+                S.n_rows = 1;
+                S.row[0] = (uint32_t)(job & ~SEG_ROW_JOB);
             }
-            unsigned inc = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += v;
-            }
-            if (lane == 31) S.wsum[warp] = inc;
-            excl = inc - tot;
-        }
-        for (int i = t; i < W * 256; i += T) (&S.cnt[c ^ 1][0][0])[i] = 0;  // next pass's counts
-        __syncthreads();
-        if (t < 256) {
-            unsigned pre = 0;
-            for (int w = 0; w < warp; ++w) pre += S.wsum[w];
-            const unsigned base = excl + pre;
-            for (int w = 0; w < W; ++w) S.cnt[c][w][t] += base;
+        } else {
+            const unsigned nr = min(tile_cnt[job], (unsigned)SEG_TILE_ROWS);
+            if (t == 0) S.n_rows = nr;
+            if (t < (int)nr) S.row[t] = tile_rows[job * SEG_TILE_ROWS + t];
         }
         __syncthreads();
-        // stable scatter; count the next pass's digits per destination slice
-        for (int q = q0; q < q1; q += 32) {
+        const unsigned nr = S.n_rows;
+        if (t < (int)nr) {
+            const uint32_t r = S.row[t];
+            S.start[t] = s_off[r];
+            S.pref[t + 1] = (unsigned)(s_off[r + 1] - s_off[r]);
+        }
+        __syncthreads();
+        if (t == 0) {
+            S.pref[0] = 0;
+            for (unsigned i = 1; i <= nr; ++i) S.pref[i] += S.pref[i - 1];
+        }
+        __syncthreads();
+        const int E = (int)S.pref[nr];
+        const int rbits = nr > 1 ? 32 - __clz(nr - 1) : 0;
+        const int bits = rbits + cbits;
+        if (E > MAXE || bits > 32) {  // (the plan never lists such tiles; cbits <= 26 is checked before)
+            if (t == 0) atomicOr(overflow, 1u);
+            __syncthreads();
+            continue;
+        }
+        const int passes = (bits + 7) / 8;
+        for (int e = t; e < E; e += T) {
+            unsigned lo = 0, hi = nr - 1;  // rank: last i with pref[i] <= e
+            while (lo < hi) {
+                const unsigned mid = (lo + hi + 1) >> 1;
+                if (S.pref[mid] <= (unsigned)e) lo = mid;
+                else hi = mid - 1;
+            }
+            S.key[0][e] = (lo << cbits) | cols[S.start[lo] + (e - S.pref[lo])];
+            S.idx[0][e] = (uint16_t)e;
+        }
+        for (int i = t; i < 2 * W * 256; i += T) (&S.cnt[0][0][0])[i] = 0;
+        __syncthreads();
+        const int q0 = warp * SLICE, q1 = min(E, q0 + SLICE);
+        // digit counts of the first pass, per warp slice
+        for (int q = q0; q < q1 && passes > 0; q += 32) {
             const int qq = q + lane;
             const bool ok = qq < q1;
             const unsigned valid = __ballot_sync(0xffffffffu, ok);
-            const uint32_t k = ok ? S.key[cur][qq] : 0u;
-            const unsigned d = (k >> shift) & 0xFFu;
+            const unsigned d = ok ? (S.key[0][qq] & 0xFFu) : 0u;
             const unsigned peers = warp_match_digit<8>(d) & valid;
-            unsigned before = 0;
-            if (ok) before = S.cnt[c][warp][d];
-            __syncwarp();
-            if (ok) {
-                const unsigned lt = peers & lanemask_lt();
-                const unsigned pos = before + __popc(lt);
-                S.key[cur ^ 1][pos] = k;
-                S.idx[cur ^ 1][pos] = S.idx[cur][qq];
-                if (lt == 0) S.cnt[c][warp][d] = before + __popc(peers);
-                if (p + 1 < passes) atomicAdd(&S.cnt[c ^ 1][pos / TS_SLICE][(k >> (shift + 8)) & 0xFFu], 1u);
-            }
+            if (ok && (peers & lanemask_lt()) == 0) S.cnt[0][warp][d] += __popc(peers);
             __syncwarp();
         }
         __syncthreads();
-        cur ^= 1;
-    }
-    for (int q = t; q < E; q += T) {
-        keys_out[start + q] = ((uint64_t)r0 << cbits) + S.key[cur][q];
-        idx_out[start + q] = (uint32_t)(start + S.idx[cur][q]);
+        int cur = 0;
+        for (int p = 0; p < passes; ++p) {
+            const int c = p & 1, shift = 8 * p;
+            // digit t: start of each warp slice's run, then across digits
+            unsigned excl = 0;
+            if (t < 256) {
+                unsigned tot = 0;
+                for (int w = 0; w < W; ++w) {
+                    const unsigned v = S.cnt[c][w][t];
+                    S.cnt[c][w][t] = tot;
+                    tot += v;
+                }
+                unsigned inc = tot;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += v;
+                }
+                if (lane == 31) S.wsum[warp] = inc;
+                excl = inc - tot;
+            }
+            for (int i = t; i < W * 256; i += T) (&S.cnt[c ^ 1][0][0])[i] = 0;  // next pass's counts
+            __syncthreads();
+            if (t < 256) {
+                unsigned pre = 0;
+                for (int w = 0; w < warp; ++w) pre += S.wsum[w];
+                const unsigned base = excl + pre;
+                for (int w = 0; w < W; ++w) S.cnt[c][w][t] += base;
+            }
+            __syncthreads();
+            // stable scatter; count the next pass's digits per destination slice
+            for (int q = q0; q < q1; q += 32) {
+                const int qq = q + lane;
+                const bool ok = qq < q1;
+                const unsigned valid = __ballot_sync(0xffffffffu, ok);
+                const uint32_t k = ok ? S.key[cur][qq] : 0u;
+                const unsigned d = (k >> shift) & 0xFFu;
+                const unsigned peers = warp_match_digit<8>(d) & valid;
+                unsigned before = 0;
+                if (ok) before = S.cnt[c][warp][d];
+                __syncwarp();
+                if (ok) {
+                    const unsigned lt = peers & lanemask_lt();
+                    const unsigned pos = before + __popc(lt);
+                    S.key[cur ^ 1][pos] = k;
+                    S.idx[cur ^ 1][pos] = S.idx[cur][qq];
+                    if (lt == 0) S.cnt[c][warp][d] = before + __popc(peers);
+                    if (p + 1 < passes) atomicAdd(&S.cnt[c ^ 1][pos / SLICE][(k >> (shift + 8)) & 0xFFu], 1u);
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+            cur ^= 1;
+        }
+        const uint32_t cmask = (uint32_t)((1ull << cbits) - 1);
+        for (int q = t; q < E; q += T) {
+            const uint32_t k = S.key[cur][q];
+            const unsigned i = cbits < 32 ? (k >> cbits) : 0u;
+            const uint64_t out = S.start[i] + (unsigned)(q - S.pref[i]);
+            keys_out[out] = ((uint64_t)S.row[i] << cbits) | (k & cmask);
+            idx_out[out] = (uint32_t)(S.start[i] + (S.idx[cur][q] - S.pref[i]));
+        }
+        __syncthreads();  // shared state is rebuilt by the next job
     }
 }
 
@@ -564,47 +772,59 @@ grouped_tile_sort(const uint32_t *__restrict__ rows, const uint32_t *__restrict_
 
 int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
                       uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s) {
+    (void)rows;  // the rows are s_off's
     *done = false;
     if (m == 0) {
         *done = true;
         return SPG_OK;
     }
-    const uint64_t n_tiles = (m + TS_SPAN - 1) / TS_SPAN;
-    DevBuf tile_r0, lists, flags;
-    SPG_TRY(tile_r0.alloc((n_tiles + 1) * sizeof(uint64_t), s));
-    SPG_TRY(lists.alloc(2 * n_tiles * sizeof(unsigned), s));
-    SPG_TRY(flags.alloc(3 * sizeof(unsigned), s));  // overflow, small tiles, large tiles
-    SPG_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, 3 * sizeof(unsigned), s));
-    unsigned *small_list = lists.as<unsigned>(), *large_list = small_list + n_tiles;
-    unsigned *overflow = flags.as<unsigned>();
-    tile_plan<<<grid_for(n_tiles + 1, 256), 256, 0, s>>>(s_off, n_rows, n_tiles, tile_r0.as<uint64_t>(), small_list,
-                                                        large_list, overflow + 1, overflow);
+    if (cbits > SEG_MAX_CBITS || m > 0xFFFFFFFFull) return SPG_OK;
+    const uint64_t n_spans = (m + SEG_SPAN - 1) / SEG_SPAN;
+    const uint64_t n_small = n_spans + m / (SEG_SPAN + 1) + 1, n_large = m / (TS_SMALL + 1) + 1;
+    DevBuf ctr_b, tiles_b, tile_rows_b, short_b, jobs_b;
+    SPG_TRY(ctr_b.alloc(SC_N * sizeof(unsigned), s));
+    SPG_TRY(tiles_b.alloc(2 * n_spans * sizeof(unsigned), s));  // tile_cnt, tile_len
+    SPG_TRY(tile_rows_b.alloc(n_spans * SEG_TILE_ROWS * sizeof(uint32_t), s));
+    SPG_TRY(short_b.alloc(n_rows * sizeof(uint32_t), s));
+    SPG_TRY(jobs_b.alloc((n_small + n_large) * sizeof(uint64_t), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(ctr_b.ptr, 0, SC_N * sizeof(unsigned), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(tiles_b.ptr, 0, 2 * n_spans * sizeof(unsigned), s));
+    unsigned *ctr = ctr_b.as<unsigned>(), *tile_cnt = tiles_b.as<unsigned>(), *tile_len = tile_cnt + n_spans;
+    uint64_t *small_jobs = jobs_b.as<uint64_t>(), *large_jobs = small_jobs + n_small;
+    const unsigned gr = grid_for(n_rows, 256, (unsigned)c->n_sms * 8);
+    seg_count<<<gr, 256, 0, s>>>(s_off, n_rows, ctr);
     SPG_LAUNCH_CHECK();
-    unsigned h[3] = {1u, 0u, 0u};
-    SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    SPG_TRY(c->phase_sync(s));
-    if (h[0]) return SPG_OK;
+    seg_place<<<gr, 256, 0, s>>>(cols, s_off, n_rows, cbits, ctr, short_b.as<uint32_t>(), tile_cnt, tile_len,
+                                 tile_rows_b.as<uint32_t>(), small_jobs, large_jobs, keys_out, idx_out);
+    SPG_LAUNCH_CHECK();
+    seg_tiles<<<grid_for(n_spans, 256), 256, 0, s>>>(tile_len, n_spans, ctr, small_jobs);
+    SPG_LAUNCH_CHECK();
+    seg_short_sort<<<(unsigned)c->n_sms * 8, 256, 0, s>>>(cols, s_off, short_b.as<uint32_t>(), ctr, cbits, keys_out,
+                                                          idx_out);
+    SPG_LAUNCH_CHECK();
     constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL, TS_SLICE_SMALL>);
     constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX, TS_SLICE_LARGE>);
     constexpr unsigned small_threads = TS_SMALL / TS_SLICE_SMALL * 32;
     constexpr unsigned large_threads = TS_MAX / TS_SLICE_LARGE * 32;
-    auto small_k = grouped_tile_sort<TS_SMALL, TS_SLICE_SMALL>;
-    auto large_k = grouped_tile_sort<TS_MAX, TS_SLICE_LARGE>;
+    auto small_k = seg_tile_sort<TS_SMALL, TS_SLICE_SMALL>;
+    auto large_k = seg_tile_sort<TS_MAX, TS_SLICE_LARGE>;
     SPG_CUDA_TRY(cudaFuncSetAttribute(small_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
     SPG_CUDA_TRY(cudaFuncSetAttribute(large_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)large_smem));
-    if (h[1]) {
-        small_k<<<h[1], small_threads, small_smem, s>>>(rows, cols, s_off, tile_r0.as<uint64_t>(), small_list, cbits,
-                                                        keys_out, idx_out, overflow);
-        SPG_LAUNCH_CHECK();
-    }
-    if (h[2]) {
-        large_k<<<h[2], large_threads, large_smem, s>>>(rows, cols, s_off, tile_r0.as<uint64_t>(), large_list, cbits,
-                                                        keys_out, idx_out, overflow);
-        SPG_LAUNCH_CHECK();
-    }
-    SPG_CUDA_TRY(cudaMemcpyAsync(h, overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    // persistent blocks over the job lists, whose lengths stay on the device
+    const unsigned small_grid = (unsigned)std::min<uint64_t>(n_small, (uint64_t)c->n_sms * 3);
+    const unsigned large_grid = (unsigned)std::min<uint64_t>(n_large, (uint64_t)c->n_sms);
+    small_k<<<small_grid, small_threads, small_smem, s>>>(cols, s_off, tile_cnt, tile_rows_b.as<uint32_t>(),
+                                                          small_jobs, ctr + SC_SMALL, cbits, keys_out, idx_out,
+                                                          ctr + SC_OVERFLOW);
+    SPG_LAUNCH_CHECK();
+    large_k<<<large_grid, large_threads, large_smem, s>>>(cols, s_off, tile_cnt, tile_rows_b.as<uint32_t>(),
+                                                          large_jobs, ctr + SC_LARGE, cbits, keys_out, idx_out,
+                                                          ctr + SC_OVERFLOW);
+    SPG_LAUNCH_CHECK();
+    unsigned h = 1u;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&h, ctr + SC_OVERFLOW, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     SPG_TRY(c->phase_sync(s));
-    *done = h[0] == 0;
+    *done = h == 0;
     return SPG_OK;
 }
 

@@ -140,16 +140,24 @@ __global__ void feat_rows(const uint64_t *__restrict__ off, const uint32_t *__re
 
 // SpGEMM features of A * B. acc layout (doubles): [0..31] histogram of the
 // products per row (bin 0: none, else 1 + floor(log2 p), capped at 31),
-// 32 sum p, 33 sum p^2, 34 max p.
+// 32 sum p, 33 sum p^2, 34 max p, 35 sum of |col / n_cols - row / m| over the
+// first and last entry of every 16th non-empty row of A, 36 their number.
+// The spread tells local patterns (banded, block-diagonal, stencils: a row's
+// products fall on few columns, the output is several times smaller than
+// the products) from scattered ones (products mostly distinct), which the
+// counts alone do not: uniform rows of 8 and 8 x 8 diagonal blocks both give
+// 64 products per row, and the fastest variant differs.
 __global__ void feat_gemm_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols,
-                               const uint64_t *__restrict__ boff, uint64_t m, double *__restrict__ acc) {
-    __shared__ double s[35];
-    for (int i = threadIdx.x; i < 35; i += blockDim.x) s[i] = 0.0;
+                               const uint64_t *__restrict__ boff, uint64_t m, uint64_t n_cols_a,
+                               double *__restrict__ acc) {
+    __shared__ double s[37];
+    for (int i = threadIdx.x; i < 37; i += blockDim.x) s[i] = 0.0;
     __syncthreads();
-    double sp = 0, sp2 = 0, mx = 0;
+    double sp = 0, sp2 = 0, mx = 0, spread = 0, cnt = 0;
     for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < m; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a0 = aoff[r], a1 = aoff[r + 1];
         uint64_t p = 0;
-        for (uint64_t ka = aoff[r]; ka < aoff[r + 1]; ++ka) {
+        for (uint64_t ka = a0; ka < a1; ++ka) {
             const uint32_t k = acols[ka];
             p += boff[k + 1] - boff[k];
         }
@@ -162,12 +170,19 @@ __global__ void feat_gemm_rows(const uint64_t *__restrict__ aoff, const uint32_t
         sp += (double)p;
         sp2 += (double)p * (double)p;
         mx = fmax(mx, (double)p);
+        if ((r & 15) == 0 && a1 > a0) {
+            const double rr = (double)r / (double)m;
+            spread += fabs((double)acols[a0] / (double)n_cols_a - rr) + fabs((double)acols[a1 - 1] / (double)n_cols_a - rr);
+            cnt += 2;
+        }
     }
     atomicAdd(&s[32], sp);
     atomicAdd(&s[33], sp2);
     atomicMax(reinterpret_cast<unsigned long long *>(&s[34]), __double_as_longlong(mx));
+    atomicAdd(&s[35], spread);
+    atomicAdd(&s[36], cnt);
     __syncthreads();
-    for (int i = threadIdx.x; i < 35; i += blockDim.x) {
+    for (int i = threadIdx.x; i < 37; i += blockDim.x) {
         if (i == 34) atomicMax(reinterpret_cast<unsigned long long *>(&acc[34]), __double_as_longlong(s[34]));
         else atomicAdd(&acc[i], s[i]);
     }
@@ -482,14 +497,14 @@ int selector_load_default(Ctx *c) {
 int spgemm_features(Ctx *c, const Csr *A, const Csr *B, float *f) {
     cudaStream_t s = c->stream;
     DevBuf acc;
-    SPG_TRY(acc.alloc(35 * sizeof(double), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(acc.ptr, 0, 35 * sizeof(double), s));
+    SPG_TRY(acc.alloc(37 * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(acc.ptr, 0, 37 * sizeof(double), s));
     if (A->n_rows) {
         feat_gemm_rows<<<grid_for(A->n_rows, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(
-            A->d_off(), A->d_cols(), B->d_off(), A->n_rows, acc.as<double>());
+            A->d_off(), A->d_cols(), B->d_off(), A->n_rows, A->n_cols ? A->n_cols : 1, acc.as<double>());
         SPG_LAUNCH_CHECK();
     }
-    double h[35];
+    double h[37];
     SPG_CUDA_TRY(cudaMemcpyAsync(h, acc.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
     const double m = (double)(A->n_rows ? A->n_rows : 1);
@@ -503,7 +518,7 @@ int spgemm_features(Ctx *c, const Csr *A, const Csr *B, float *f) {
     f[36] = (float)(std::log2(mean + 1.0) / 16.0);
     f[37] = (float)(std::log2(std::sqrt(var) + 1.0) / 16.0);
     f[38] = (float)(std::log2(h[34] + 1.0) / 32.0);
-    f[39] = (float)(std::log2((double)A->nnz / m + 1.0) / 16.0);
+    f[39] = (float)(h[36] > 0 ? h[35] / h[36] : 0.0);
     return SPG_OK;
 }
 

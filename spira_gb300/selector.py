@@ -32,7 +32,7 @@ from . import gen
 
 K = len(SPMV_VARIANTS)
 K_GEMM = len(SPGEMM_VARIANTS)
-NNZ_CAP = 16_000_000
+NNZ_CAP = 64_000_000
 GEMM_NNZ_CAP = 2_000_000
 # fixed variants "without the selector": the comparison a gain is measured against
 DEFAULT_SPMV = SPMV_VARIANTS["adaptive16"]
@@ -139,6 +139,16 @@ def collect(ctx: Context, indices, seed: int, reps: int = 3, log_every: int = 0,
         if log_every and (j + 1) % log_every == 0:
             print(f"  corpus {j + 1}/{len(indices)}  {time.time() - t0:.1f}s", flush=True)
     return np.array(X, np.float32).reshape(-1, N_FEATURES), np.array(T, np.float32), S
+
+
+def features_of(ctx: Context, indices, seed: int, op: str = "spmv") -> np.ndarray:
+    """Features [n, 40] of corpus matrices `indices` (no timing)."""
+    X = []
+    for i in indices:
+        A = build(ctx, corpus_spec(int(i), seed) if op == "spmv" else gemm_corpus_spec(int(i), seed))
+        X.append(A.features() if op == "spmv" else A.spgemm_features(A))
+        A.close()
+    return np.array(X, np.float32).reshape(-1, N_FEATURES)
 
 
 def targets(times: np.ndarray) -> np.ndarray:

@@ -33,6 +33,8 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
     ap.add_argument("--corpus-cache", default=None, help="npz to reuse / store features and timings")
+    ap.add_argument("--refeature", action="store_true",
+                    help="with a cached corpus: keep its timings, recompute the features of its matrices")
     args = ap.parse_args()
 
     import spira_gb300 as sg
@@ -43,6 +45,9 @@ def main():
     if args.corpus_cache and Path(args.corpus_cache).exists():
         d = np.load(args.corpus_cache)
         X, T = d["X"], d["T"]
+        if args.refeature:  # the matrices are pure functions of (seed, index): rebuild, re-measure features only
+            X = S.features_of(ctx, range(len(T)), args.seed, op=args.op)
+            np.savez_compressed(args.corpus_cache, X=X, T=T)
     else:
         X, T, _ = S.collect(ctx, range(args.n), args.seed, reps=args.reps, log_every=500, op=args.op)
         if args.corpus_cache:

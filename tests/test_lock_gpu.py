@@ -135,6 +135,28 @@ def test_lock_row_grouped_inserts(ctx, lengths, n_rows, n_cols):
     assert_csr_equal(A.download(), oracle.lock_epochs(n_rows, n_cols, [(rows, cols, vals)]))
 
 
+@pytest.mark.parametrize("n_cols", [300, 1 << 22, 1 << 26, (1 << 26) + 1])
+def test_lock_row_grouped_every_length_class(ctx, n_cols):
+    """Grouped inserts with a row at every boundary of the on-chip sort's
+    length classes (written through, bitonic in registers for 2..32 entries,
+    span tiles up to 2048, single-row tiles up to 12 288), rows shuffled so
+    the classes interleave; duplicates and zeros included. 300 columns make
+    duplicates dense; 2^26 columns is the widest key the on-chip sort takes,
+    one more column sends the epoch to the global sort."""
+    base = [0, 1, 2, 3, 4, 5, 7, 8, 9, 15, 16, 17, 31, 32, 33, 34, 100, 2047, 2048, 2049, 4096, 4097, 12288]
+    lengths = np.array(base * 3, np.int64)
+    lengths = lengths[np.argsort(gen.hash3(5, 0, np.arange(len(lengths), dtype=np.uint64)))]
+    n_rows = len(lengths)
+    rows = np.repeat(np.arange(n_rows, dtype=np.uint32), lengths)
+    ctr = np.arange(len(rows), dtype=np.uint64)
+    cols = gen.below(gen.hash3(n_cols, 1, ctr), n_cols)
+    cols[7::50] = cols[6::50][: len(cols[7::50])]  # neighbours repeated: duplicates in every class
+    vals = gen.sym_unit(gen.hash3(n_cols, 2, ctr))
+    vals[::17] = 0.0
+    A = gpu_lock(ctx, n_rows, n_cols, [(rows, cols, vals)])
+    assert_csr_equal(A.download(), oracle.lock_epochs(n_rows, n_cols, [(rows, cols, vals)]))
+
+
 def test_lock_row_grouped_sparse_rows(ctx):
     """Grouped inserts whose rows are far apart (large row spans per tile)."""
     n = 3_000_000
