@@ -272,6 +272,45 @@ inline uint64_t csr_alloc_elems(uint64_t cap) { return ((cap + 15) & ~15ull) + 1
 // stays inside the allocation.
 inline uint64_t csr_off_elems(uint64_t n_rows) { return n_rows + 3; }
 
+// Ascending bitonic sort of the 32 * E keys a warp holds, key[e] of lane l
+// being element 32 e + l. Partners 32 or more apart share a lane (registers),
+// nearer ones are exchanged by shuffles.
+template <int E, class K>
+__device__ __forceinline__ void warp_bitonic(K (&key)[E], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * E; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jj = j >> 5;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    if ((e & jj) == 0) {
+                        const int f = e | jj;
+                        const bool up = ((32 * e) & k) == 0;  // k >= 64: the item decides
+                        const K a = key[e], b = key[f];
+                        const bool sw = up ? (a > b) : (a < b);
+                        key[e] = sw ? b : a;
+                        key[f] = sw ? a : b;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const K o = __shfl_xor_sync(0xffffffffu, key[e], j);
+                    const int i = 32 * e + lane;
+                    const bool keep_min = (((i & k) == 0) == ((i & j) == 0));
+                    key[e] = keep_min ? (o < key[e] ? o : key[e]) : (o > key[e] ? o : key[e]);
+                }
+            }
+        }
+    }
+}
+
+// Spira's ValueTraits<double>::is_zero (traits.hpp:73-80): +0 and -0 are
+// zero, NaN is not.
+__device__ __forceinline__ bool is_zero(double v) { return fabs(v) <= 0.0; }
+
 // Lanes of the (full) warp whose NB-bit value d (a radix digit, or 256 for
 // "no key" when NB = 9) equals this lane's: NB ballots on the ALU pipe,
 // cheaper on GB300 than match.any, which issues on the narrow
@@ -314,6 +353,13 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 // s_off[r] = first position of row r (n_rows + 1 entries). *done = false when
 // a row has more than 12 288 entries or columns need more than 26 bits; the
 // outputs are then undefined.
+// The first lock of row-grouped inserts in one pass of the same sort: every
+// row's last write per column, unless zero, in column order at the row's
+// first input positions (out_cols / out_vals[s_off[r] + k], k < kept[r]);
+// kept[r] for every row r < n_rows. *done as for sort_grouped_rows.
+int dedup_grouped_rows(Ctx *c, const uint32_t *cols, const double *vals, const uint64_t *s_off, uint64_t m,
+                       uint64_t n_rows, int cbits, uint32_t *out_cols, double *out_vals, uint64_t *kept, bool *done,
+                       cudaStream_t s);
 int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
                       uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s);
 

@@ -32,7 +32,6 @@ namespace {
 
 constexpr int LB = 256;
 
-__device__ __forceinline__ bool is_zero(double v) { return fabs(v) <= 0.0; }  // traits.hpp:73-80
 
 __global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
                                uint64_t m, int cbits, uint64_t *__restrict__ keys,
@@ -49,11 +48,50 @@ __global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t
 // some key is greater than its successor (not sorted), stats[3] = 1 if some
 // row is (rows not grouped), stats[4] = 1 if some key is not below its
 // successor (not strictly increasing: duplicates or unsorted).
+// VEC: rows and cols 16-byte aligned; each thread reads 4 rows and 4
+// columns per step in two 16-byte loads (the successor of its last pair
+// comes from the next lane, or one more load at the warp's edge).
+template <bool VEC>
 __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols, uint64_t m,
                              int cbits, unsigned *__restrict__ stats) {
     unsigned mr = 0, mc = 0;
     bool d = false, g = false, e = false;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+    if constexpr (VEC) {
+        const uint64_t n4 = m / 4;  // whole groups of 4; the tail below
+        const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+        const uint64_t n_iter = (n4 + stride - 1) / stride;  // warp-uniform: shuffles below
+        for (uint64_t it = 0; it < n_iter; ++it) {
+            const uint64_t q = it * stride + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+            const bool ok = q < n4;
+            uint4 r4 = make_uint4(0, 0, 0, 0), c4 = make_uint4(0, 0, 0, 0);
+            if (ok) {
+                r4 = reinterpret_cast<const uint4 *>(rows)[q];
+                c4 = reinterpret_cast<const uint4 *>(cols)[q];
+            }
+            uint32_t rn = __shfl_down_sync(0xffffffffu, r4.x, 1), cn = __shfl_down_sync(0xffffffffu, c4.x, 1);
+            const bool have_next = ok && 4 * q + 4 < m;
+            if (have_next && ((threadIdx.x & 31) == 31 || q + 1 >= n4)) {
+                rn = rows[4 * q + 4];
+                cn = cols[4 * q + 4];
+            }
+            if (ok) {
+                const uint32_t rr[5] = {r4.x, r4.y, r4.z, r4.w, rn}, cc[5] = {c4.x, c4.y, c4.z, c4.w, cn};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    mr = max(mr, rr[k]);
+                    mc = max(mc, cc[k]);
+                    if (k < 3 || have_next) {
+                        const uint64_t k1 = ((uint64_t)rr[k] << cbits) | cc[k];
+                        const uint64_t k2 = ((uint64_t)rr[k + 1] << cbits) | cc[k + 1];
+                        d |= k1 > k2;
+                        e |= k1 >= k2;
+                        g |= rr[k] > rr[k + 1];
+                    }
+                }
+            }
+        }
+    }
+    for (uint64_t i = (VEC ? (m & ~3ull) : 0) + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t r = rows[i], c = cols[i];
         const uint64_t k = ((uint64_t)r << cbits) | c;
@@ -96,6 +134,24 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
         if (bf & 1u) stats[2] = 1u;
         if (bf & 2u) stats[3] = 1u;
         if (bf & 4u) stats[4] = 1u;
+    }
+}
+
+// Moves the kept entries of a row-grouped first lock from their rows' input
+// positions (row r's at [s_off[r], s_off[r] + kept)) to their CSR positions
+// (off: the exclusive scan of the kept counts). The staged rows name each
+// position's row, as the rows are grouped.
+__global__ void first_grouped_compact(const uint32_t *__restrict__ rows, const uint64_t *__restrict__ s_off,
+                                      const uint64_t *__restrict__ off, const uint32_t *__restrict__ scols,
+                                      const double *__restrict__ svals, uint64_t m, uint32_t *__restrict__ ocols,
+                                      double *__restrict__ ovals) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = rows[e];
+        const uint64_t k = e - s_off[r], o0 = off[r];
+        if (k < off[r + 1] - o0) {
+            ocols[o0 + k] = scols[e];
+            ovals[o0 + k] = svals[e];
+        }
     }
 }
 
@@ -680,6 +736,48 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         out_cols.release();
         out_vals.release();
     }
+    if (m && pre && pre->ready && pre->unsorted && !pre->ungrouped) {
+        // Row-grouped inserts (rows non-decreasing, columns in any order, as
+        // row-by-row assembly stages them): every row is sorted, its last
+        // write per column kept unless zero, and compacted on chip in one
+        // pass, in place at the row's input positions; a scan of the kept
+        // counts gives the offsets, and entries move only if some were dropped.
+        DevBuf s_off, kept, scols, svals;
+        SPG_TRY(s_off.alloc((n + 1) * sizeof(uint64_t), s));
+        SPG_TRY(launch_row_offsets(c, rows, m, n, s_off.as<uint64_t>(), s));
+        SPG_TRY(kept.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
+        SPG_TRY(scols.alloc(csr_alloc_elems(m) * sizeof(uint32_t), s));
+        SPG_TRY(svals.alloc(csr_alloc_elems(m) * sizeof(double), s));
+        bool done = false;
+        SPG_TRY(dedup_grouped_rows(c, cols, vals, s_off.as<uint64_t>(), m, n, cbits, scols.as<uint32_t>(),
+                                   svals.as<double>(), kept.as<uint64_t>(), &done, s));
+        if (done) {
+            SPG_TRY(exclusive_scan_u64(c, kept.as<uint64_t>(), n, kept.as<uint64_t>() + n, s));
+            SPG_CUDA_TRY(cudaMemcpyAsync(&nnz, kept.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, s));
+            SPG_TRY(c->phase_sync(s));
+            if (nnz == m) {  // nothing dropped: the staging arrays are the CSR
+                out_cols = std::move(scols);
+                out_vals = std::move(svals);
+            } else {
+                SPG_TRY(out_cols.alloc(csr_alloc_elems(nnz) * sizeof(uint32_t), s));
+                SPG_TRY(out_vals.alloc(csr_alloc_elems(nnz) * sizeof(double), s));
+                first_grouped_compact<<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
+                    rows, s_off.as<uint64_t>(), kept.as<uint64_t>(), scols.as<uint32_t>(), svals.as<double>(), m,
+                    out_cols.as<uint32_t>(), out_vals.as<double>());
+                SPG_LAUNCH_CHECK();
+            }
+            A->invalidate_derived();
+            A->off = std::move(kept);
+            A->cols = std::move(out_cols);
+            A->vals = std::move(out_vals);
+            A->nnz = nnz;
+            A->capacity = nnz;  // build_csr: exact
+            A->built = true;
+            A->may_have_zeros = false;
+            SPG_TRY(c->phase_sync(s));
+            return SPG_OK;
+        }
+    }
     if (m) {
         const unsigned g = grid_for(m, LB, (unsigned)c->n_sms * 16);
         SPG_TRY(sort_keys(c, rows, cols, m, n, A->n_cols, keys, idx, pre, s));
@@ -732,8 +830,13 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
         DevBuf stats;
         SPG_TRY(stats.alloc(5 * sizeof(unsigned), s));
         SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 5 * sizeof(unsigned), s));
-        lock_prepare<<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(rows, cols, m, bits_for(A->n_cols),
-                                                                           stats.as<unsigned>());
+        if (((uintptr_t)rows | (uintptr_t)cols) % 16 == 0)
+            lock_prepare<true><<<grid_for((m + 3) / 4, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
+                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>());
+        else
+            lock_prepare<false><<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(rows, cols, m,
+                                                                                       bits_for(A->n_cols),
+                                                                                       stats.as<unsigned>());
         SPG_LAUNCH_CHECK();
         unsigned h[5] = {0u, 0u, 1u, 1u, 1u};
         SPG_CUDA_TRY(cudaMemcpyAsync(h, stats.ptr, 5 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));

@@ -40,7 +40,6 @@ namespace {
 constexpr int OB = 256;
 constexpr uint64_t COLLIDE = 1ull << 63;  // high bit of a found position: the columns are equal
 
-__device__ __forceinline__ bool is_zero(double v) { return fabs(v) <= 0.0; }  // traits.hpp:73-80
 
 // Row holding entry e: the last r with off[r] <= e (rows before it end at or
 // before e, empty rows share their successor's offset).

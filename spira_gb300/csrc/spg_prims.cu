@@ -400,150 +400,139 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 // Rows are sorted by length class:
 //   * one entry: written through by the planning pass;
 //   * 2..32 entries: a bitonic network in registers, 32 / P rows of padded
-//     length P (2, 4, 8, 16, 32) per warp, keys (col << 5 | position), so the
-//     network's order is the stable order;
-//   * 33..SEG_SPAN entries: grouped by the span of SEG_SPAN input positions
-//     their first entry lies in (at most 63 such rows start in one span, as
-//     they lie 33 or more positions apart; together < 2 SEG_SPAN entries) and
-//     sorted tile by tile in shared memory: an LSD radix sort (8-bit digits)
-//     of 32-bit keys (rank of the row in the tile, col) with 16-bit tile
-//     positions, ping-ponged in shared memory; warp w owns positions
-//     [512 w, 512 w + 512) of every pass, and each scatter also counts, per
-//     destination slice, the digit of the next pass, so a pass is one sweep;
-//   * SEG_SPAN+1..TS_MAX entries: a tile of its own, sorted the same way (no
-//     rank bits: ceil(cbits / 8) passes); rows up to TS_SMALL entries in the
-//     kernel of the span tiles (three blocks per SM), longer ones in a kernel
-//     of one block per SM.
-// A tile's key needs rank bits (at most 6) + cbits <= 32, so columns of more
-// than 26 bits, and a row longer than TS_MAX, make the sort report failure;
-// callers then sort globally. Work lists are filled with atomics, in no
-// particular order: every row's output places are fixed by s_off, so the
-// result does not depend on that order.
+//     length P (2, 4, 8, 16, 32) per warp, keys (col << 5 | position); a warp
+//     takes 32 consecutive rows (their offsets in one coalesced read) and
+//     sorts each class present among them in turn;
+//   * 33..SEG_MEDIUM entries: one warp per row, a bitonic network over the
+//     row padded to a power of two, 2..16 keys (col << 9 | position) to a
+//     lane; 32-bit keys while the columns need at most 22 bits, else 64-bit;
+//   * SEG_MEDIUM+1..TS_MAX entries: a block per row, in shared memory: an
+//     LSD radix sort of the 32-bit columns carrying 16-bit row positions,
+//     with 6-bit digits ranked the way Merrill and Grimshaw's block radix
+//     sort ranks them: every thread holds I consecutive entries (so thread
+//     order is input order), counts its digits in its own column of packed
+//     16-bit counters (two digits per word: d and d + 32), one raking scan
+//     over all counters in (digit, thread) order turns them into exclusive
+//     prefixes, and each entry's rank is its digit's prefix plus the count
+//     of the same digit before it in its thread: a stable scatter with no
+//     per-digit warp votes. Counters and the exchange arrays share memory,
+//     padded one word in 33 so that column and raking accesses and the
+//     blocked reads are free of bank conflicts. Three kernels sized to the
+//     rows (128 x 16, 256 x 16 and 1024 x 12 entries) keep few threads idle.
+// In every network the key carries the entry's position in its row, so the
+// sorted order is the stable order. Columns of more than 26 bits, or a row
+// longer than TS_MAX, make the sort report failure; callers then sort
+// globally. Work lists are filled with atomics, in no particular order: every
+// row's output places are fixed by s_off, so the result does not depend on
+// that order.
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int SEG_SPAN = 2048;
-constexpr int SEG_TILE_ROWS = 64;  // medium rows starting in one span: at most 63
-constexpr int TS_SMALL = 4096, TS_SLICE_SMALL = 512;  // 8 warps; a span's medium rows: < 2 SEG_SPAN
-constexpr int TS_MAX = 12288, TS_SLICE_LARGE = 512;   // 24 warps
+constexpr int SEG_MEDIUM = 512;   // rows of 33..SEG_MEDIUM entries: a warp each
+constexpr int TS0_T = 128, TS0_I = 16;   // rows up to 2048 entries
+constexpr int TS1_T = 256, TS1_I = 16;   // rows up to 4096
+constexpr int TS2_T = 1024, TS2_I = 12;  // rows up to TS_MAX
+constexpr int TS0 = TS0_T * TS0_I, TS1 = TS1_T * TS1_I, TS_MAX = TS2_T * TS2_I;
+constexpr int RS_DBITS = 6, RS_DIGITS = 1 << RS_DBITS, RS_WORDS = RS_DIGITS / 2;
 constexpr int SEG_MAX_CBITS = 26;
-constexpr uint64_t SEG_ROW_JOB = 1ull << 63;  // large job naming one row (else a span tile)
 
 // counters (unsigned) of the plan
 enum : int {
-    SC_SHORT = 0,       // [1..5]: rows of padded length 2^c
-    SC_SMALL = 6,       // small jobs: span tiles, rows of SEG_SPAN+1..TS_SMALL entries
-    SC_LARGE = 7,       // large jobs: rows of TS_SMALL+1..TS_MAX entries
-    SC_OVERFLOW = 8,    // a row or a tile the on-chip sort cannot take
-    SC_CURSOR = 9,      // [9 + c]: fill cursors of the short classes
+    SC_LIST = 0,        // [1..6]: rows of padded length 2^c (1..5), medium rows (6)
+    SC_JOBS = 7,        // [7..9]: rows of tile kernel 0, 1, 2
+    SC_OVERFLOW = 10,   // a row the on-chip sort cannot take
     SC_N = 16
 };
 
 // 0: nothing to sort (0 or 1 entry), 1..5: short of padded length 2^c,
-// 6: medium (span tile), 7: a small job of its own, 8: a large job of its
-// own, 9: too long.
+// 6: medium, 7..9: tile kernel 0..2, 10: too long.
 __device__ __forceinline__ int seg_class(uint64_t L) {
     if (L <= 1) return 0;
     if (L <= 32) return 32 - __clz((unsigned)(L - 1));
-    if (L <= (uint64_t)SEG_SPAN) return 6;
-    if (L <= (uint64_t)TS_SMALL) return 7;
-    if (L <= (uint64_t)TS_MAX) return 8;
-    return 9;
+    if (L <= (uint64_t)SEG_MEDIUM) return 6;
+    if (L <= (uint64_t)TS0) return 7;
+    if (L <= (uint64_t)TS1) return 8;
+    if (L <= (uint64_t)TS_MAX) return 9;
+    return 10;
 }
 
-// Counts the short rows of every class.
+// Where the sort puts a row's entries. Key mode (DEDUP = false): keys[p] =
+// row << cbits | col and idx[p] = input position, p over the row's input
+// positions in sorted order. Dedup mode (a first lock): the row's last write
+// per column, unless zero, in column order at the row's first input
+// positions (cols[s_off[r] + k], vals[s_off[r] + k]) and kept[r] = their
+// number.
+struct SegOut {
+    uint64_t *keys;
+    uint32_t *idx;
+    const double *in_vals;
+    uint32_t *cols;
+    double *vals;
+    uint64_t *kept;
+};
+
+// The rows of every class c (ctr[SC_LIST + c]; classes 6..9 are listed).
 __global__ void __launch_bounds__(256) seg_count(const uint64_t *__restrict__ s_off, uint64_t n_rows,
                                                  unsigned *__restrict__ ctr) {
-    __shared__ unsigned sc[6];
-    if (threadIdx.x < 6) sc[threadIdx.x] = 0;
+    __shared__ unsigned sc[10];
+    if (threadIdx.x < 10) sc[threadIdx.x] = 0;
     __syncthreads();
     for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n_rows;
          r += (uint64_t)gridDim.x * blockDim.x) {
         const int c = seg_class(s_off[r + 1] - s_off[r]);
-        if (c >= 1 && c <= 5) atomicAdd(&sc[c], 1u);
+        if (c >= 1 && c <= 9) atomicAdd(&sc[c], 1u);
+        else if (c == 10) atomicOr(&ctr[SC_OVERFLOW], 1u);
     }
     __syncthreads();
-    if (threadIdx.x >= 1 && threadIdx.x <= 5 && sc[threadIdx.x]) atomicAdd(&ctr[SC_SHORT + threadIdx.x], sc[threadIdx.x]);
+    if (threadIdx.x >= 1 && threadIdx.x <= 9 && sc[threadIdx.x]) atomicAdd(&ctr[SC_LIST + threadIdx.x], sc[threadIdx.x]);
 }
 
-// Writes single-entry rows through, lists short rows by class (class c in
-// short_rows[base_c ...], base_c = rows of the classes below), medium rows by
-// span tile (tile_rows[t * SEG_TILE_ROWS + k], tile_len[t] = their entries)
-// and longer rows as small or large jobs of their own.
+// Writes single-entry rows through and lists the rows of classes 6..9:
+// lists[base_c + k] for class c (base_c = the rows of the listed classes
+// below it; classes 7..9 are the tile kernels' lists). cur[c]: fill cursors.
+template <bool DEDUP>
 __global__ void __launch_bounds__(256) seg_place(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
-                                                 uint64_t n_rows, int cbits, unsigned *__restrict__ ctr,
-                                                 uint32_t *__restrict__ short_rows, unsigned *__restrict__ tile_cnt,
-                                                 unsigned *__restrict__ tile_len, uint32_t *__restrict__ tile_rows,
-                                                 uint64_t *__restrict__ small_jobs,
-                                                 uint64_t *__restrict__ large_jobs, uint64_t *__restrict__ keys_out,
-                                                 uint32_t *__restrict__ idx_out) {
-    __shared__ unsigned sc[8], sbase[8];
-    unsigned base[6];
-    base[0] = 0;
-#pragma unroll
-    for (int c = 1; c <= 5; ++c) base[c] = base[c - 1] + (c > 1 ? ctr[SC_SHORT + c - 1] : 0u);
+                                                 uint64_t n_rows, int cbits, const unsigned *__restrict__ ctr,
+                                                 unsigned *__restrict__ cur, uint32_t *__restrict__ lists, SegOut o) {
+    __shared__ unsigned sc[10], sbase[10], base[10];
+    if (threadIdx.x == 0) {
+        base[6] = 0;
+        for (int c = 7; c <= 9; ++c) base[c] = base[c - 1] + ctr[SC_LIST + c - 1];
+    }
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t n_iter = (n_rows + stride - 1) / stride;  // the same for every thread: block-wide syncs below
     for (uint64_t it = 0; it < n_iter; ++it) {
         const uint64_t r = it * stride + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-        if (threadIdx.x < 8) sc[threadIdx.x] = 0;
+        if (threadIdx.x < 10) sc[threadIdx.x] = 0;
         __syncthreads();
         int c = 0;
         unsigned slot = 0;
-        uint64_t b = 0, L = 0;
         if (r < n_rows) {
-            b = s_off[r];
-            L = s_off[r + 1] - b;
+            const uint64_t b = s_off[r], L = s_off[r + 1] - b;
             c = seg_class(L);
             if (L == 1) {
-                keys_out[b] = ((uint64_t)r << cbits) | cols[b];
-                idx_out[b] = (uint32_t)b;
-            } else if (c >= 1 && c <= 5) {
-                slot = atomicAdd(&sc[c], 1u);
-            } else if (c == 7 || c == 8) {
-                slot = atomicAdd(&sc[c - 1], 1u);  // sc[6]: small, sc[7]: large
-            } else if (c == 6) {
-                const uint64_t t = b / SEG_SPAN;
-                const unsigned k = atomicAdd(&tile_cnt[t], 1u);
-                if (k < SEG_TILE_ROWS) {
-                    tile_rows[t * SEG_TILE_ROWS + k] = (uint32_t)r;
-                    atomicAdd(&tile_len[t], (unsigned)L);
+                if constexpr (DEDUP) {
+                    const double v = o.in_vals[b];
+                    o.cols[b] = cols[b];
+                    o.vals[b] = v;
+                    o.kept[r] = is_zero(v) ? 0 : 1;
                 } else {
-                    atomicOr(&ctr[SC_OVERFLOW], 1u);  // (not reachable: rows of > 32 entries start 33 apart)
+                    o.keys[b] = ((uint64_t)r << cbits) | cols[b];
+                    o.idx[b] = (uint32_t)b;
                 }
-            } else if (c == 9) {
-                atomicOr(&ctr[SC_OVERFLOW], 1u);
+            } else if (L == 0) {
+                if constexpr (DEDUP) o.kept[r] = 0;
+            } else if (c >= 6 && c <= 9) {
+                slot = atomicAdd(&sc[c], 1u);
             }
         }
         __syncthreads();
-        if (threadIdx.x >= 1 && threadIdx.x <= 5 && sc[threadIdx.x])
-            sbase[threadIdx.x] = atomicAdd(&ctr[SC_CURSOR + threadIdx.x], sc[threadIdx.x]);
-        if (threadIdx.x == 6 && sc[6]) sbase[6] = atomicAdd(&ctr[SC_SMALL], sc[6]);
-        if (threadIdx.x == 7 && sc[7]) sbase[7] = atomicAdd(&ctr[SC_LARGE], sc[7]);
+        if (threadIdx.x >= 6 && threadIdx.x <= 9 && sc[threadIdx.x])
+            sbase[threadIdx.x] = atomicAdd(&cur[threadIdx.x], sc[threadIdx.x]);
         __syncthreads();
-        if (r < n_rows) {
-            if (c >= 1 && c <= 5) short_rows[base[c] + sbase[c] + slot] = (uint32_t)r;
-            else if (c == 7) small_jobs[sbase[6] + slot] = SEG_ROW_JOB | r;
-            else if (c == 8) large_jobs[sbase[7] + slot] = SEG_ROW_JOB | r;
-        }
+        if (r < n_rows && c >= 6 && c <= 9) lists[base[c] + sbase[c] + slot] = (uint32_t)r;
         __syncthreads();
     }
-}
-
-// Span tiles holding medium rows onto the small job list (one atomic per warp).
-__global__ void seg_tiles(const unsigned *__restrict__ tile_len, uint64_t n_spans, unsigned *__restrict__ ctr,
-                          uint64_t *__restrict__ small_jobs) {
-    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    const unsigned E = t < n_spans ? tile_len[t] : 0u;
-    if (E > (unsigned)TS_SMALL) atomicOr(&ctr[SC_OVERFLOW], 1u);  // (not reachable: < 2 SEG_SPAN)
-    const bool take = E != 0 && E <= (unsigned)TS_SMALL;
-    const unsigned want = __ballot_sync(0xffffffffu, take);
-    if (!want) return;
-    const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(&ctr[SC_SMALL], (unsigned)__popc(want));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (take) small_jobs[base + __popc(want & ((1u << lane) - 1u))] = t;
 }
 
 // Bitonic sort of aligned P-lane segments of the warp, ascending in every
@@ -563,209 +552,428 @@ __device__ __forceinline__ uint32_t segment_bitonic(uint32_t key, int lane) {
     return key;
 }
 
-template <int P>
-__device__ __forceinline__ void sort_short_group(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
-                                                 const uint32_t *__restrict__ list, unsigned n_list, unsigned group,
-                                                 int cbits, uint64_t *__restrict__ keys_out,
-                                                 uint32_t *__restrict__ idx_out, int lane) {
-    const unsigned i = group * (32 / P) + lane / P;
+// Rows (b, L, r) of one class, one per P-lane segment (L = 0: no row).
+template <int P, bool DEDUP>
+__device__ __forceinline__ void sort_short_group(const uint32_t *__restrict__ cols, uint64_t b, uint64_t L,
+                                                 uint64_t r, int cbits, const SegOut &o, int lane) {
     const int j = lane % P;
     uint32_t key = 0xFFFFFFFFu;  // real keys stay below 2^31: cbits <= 26
-    uint64_t b = 0, L = 0, r = 0;
-    if (i < n_list) {
-        r = list[i];
-        b = s_off[r];
-        L = s_off[r + 1] - b;
-        if ((uint64_t)j < L) key = (cols[b + j] << 5) | (uint32_t)j;
+    double v_in = 0.0;
+    {
+        if ((uint64_t)j < L) {
+            key = (cols[b + j] << 5) | (uint32_t)j;
+            if constexpr (DEDUP) v_in = o.in_vals[b + j];  // in input order: coalesced
+        }
     }
     key = segment_bitonic<P>(key, lane);
-    if ((uint64_t)j < L) {
-        keys_out[b + j] = (r << cbits) | (key >> 5);
-        idx_out[b + j] = (uint32_t)(b + (key & 31u));
+    if constexpr (!DEDUP) {
+        if ((uint64_t)j < L) {
+            o.keys[b + j] = (r << cbits) | (key >> 5);
+            o.idx[b + j] = (uint32_t)(b + (key & 31u));
+        }
+    } else {
+        // the last of a run of equal columns is the last write; kept unless
+        // zero. Its value comes from the lane that loaded it.
+        const uint32_t nxt = __shfl_down_sync(0xffffffffu, key, 1);
+        const double v = __shfl_sync(0xffffffffu, v_in, (lane & ~(P - 1)) | (int)(key & (uint32_t)(P - 1)));
+        bool keep = false;
+        if ((uint64_t)j < L && ((uint64_t)(j + 1) == L || (nxt >> 5) != (key >> 5))) keep = !is_zero(v);
+        const unsigned seg = P == 32 ? 0xffffffffu : ((1u << (P & 31)) - 1u) << (lane & ~(P - 1));
+        const unsigned bal = __ballot_sync(0xffffffffu, keep) & seg;
+        if (keep) {
+            const uint64_t w = b + (uint64_t)__popc(bal & ((1u << lane) - 1u));
+            o.cols[w] = key >> 5;
+            o.vals[w] = v;
+        }
+        if (j == 0 && L) o.kept[r] = (uint64_t)__popc(bal);
     }
 }
 
-// Short rows: warp job g of class c sorts rows [g * 32 / P, (g + 1) * 32 / P)
-// of that class's list; jobs of all classes in one grid-stride sweep.
+// Short rows: warp w takes rows [32 w, 32 w + 32) (grid-stride), reads
+// their offsets in one coalesced access, and sorts the rows of each short
+// class among them, 32 / P at a time (segment g of P lanes takes the class's
+// g-th remaining row).
+template <bool DEDUP>
 __global__ void __launch_bounds__(256) seg_short_sort(const uint32_t *__restrict__ cols,
-                                                      const uint64_t *__restrict__ s_off,
-                                                      const uint32_t *__restrict__ short_rows,
-                                                      const unsigned *__restrict__ ctr, int cbits,
-                                                      uint64_t *__restrict__ keys_out, uint32_t *__restrict__ idx_out) {
-    unsigned cnt[6], base[6], jobs_end[6];
-    cnt[0] = base[0] = jobs_end[0] = 0;
+                                                      const uint64_t *__restrict__ s_off, uint64_t n_rows, int cbits,
+                                                      SegOut o) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t w = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w * 32 < n_rows; w += warps) {
+        const uint64_t r = w * 32 + lane;
+        uint64_t b = 0, L = 0;
+        if (r < n_rows) {
+            b = s_off[r];
+            L = s_off[r + 1] - b;
+        }
+        const int c = (L >= 2 && L <= 32) ? 32 - __clz((unsigned)(L - 1)) : 0;
 #pragma unroll
-    for (int c = 1; c <= 5; ++c) {
-        cnt[c] = ctr[SC_SHORT + c];
-        base[c] = base[c - 1] + cnt[c - 1];
-        const unsigned per = 32u >> c;  // rows per warp
-        jobs_end[c] = jobs_end[c - 1] + (cnt[c] + per - 1) / per;
+        for (int cls = 1; cls <= 5; ++cls) {
+            unsigned mask = __ballot_sync(0xffffffffu, c == cls);
+            const int P = 1 << cls, per = 32 >> cls;
+            while (mask) {
+                const int g = lane >> cls;  // this lane's segment
+                const unsigned src = __fns(mask, 0, g + 1);  // the segment's row: g-th set lane of mask
+                const int sl = src < 32 ? (int)src : 0;
+                const uint64_t gb = __shfl_sync(0xffffffffu, b, sl), gL = __shfl_sync(0xffffffffu, L, sl);
+                const uint64_t gr = w * 32 + (uint64_t)sl;
+                const uint64_t len = src < 32 ? gL : 0;
+                switch (cls) {
+                    case 1: sort_short_group<2, DEDUP>(cols, gb, len, gr, cbits, o, lane); break;
+                    case 2: sort_short_group<4, DEDUP>(cols, gb, len, gr, cbits, o, lane); break;
+                    case 3: sort_short_group<8, DEDUP>(cols, gb, len, gr, cbits, o, lane); break;
+                    case 4: sort_short_group<16, DEDUP>(cols, gb, len, gr, cbits, o, lane); break;
+                    default: sort_short_group<32, DEDUP>(cols, gb, len, gr, cbits, o, lane); break;
+                }
+                (void)P;
+                for (int k = 0; k < per && mask; ++k) mask &= mask - 1;  // drop the rows just sorted
+            }
+        }
     }
+}
+
+// One medium row (33..32 E entries), one warp: element 32 e + lane in
+// key[e] = col << 9 | position (padding above every key), sorted, written.
+// (Holding E consecutive elements per lane instead, so that near partners
+// meet in registers, measured 2.6x slower: strided loads and stores, and
+// twice the registers.)
+template <int E, class K, bool DEDUP>
+__device__ __forceinline__ void sort_medium_row(const uint32_t *__restrict__ cols, uint64_t b, uint32_t L, uint64_t r,
+                                                int cbits, const SegOut &o, int lane) {
+    K key[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t p = 32u * e + lane;
+        key[e] = p < L ? (((K)cols[b + p] << 9) | (K)p) : ~(K)0;
+    }
+    warp_bitonic<E, K>(key, lane);
+    if constexpr (!DEDUP) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t p = 32u * e + lane;
+            if (p < L) {
+                o.keys[b + p] = (r << cbits) | (uint64_t)(key[e] >> 9);
+                o.idx[b + p] = (uint32_t)(b + (uint32_t)(key[e] & 511u));
+            }
+        }
+    } else {
+        uint32_t kept = 0;
+        const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t p = 32u * e + lane;
+            // the next element: lane + 1 of the same register, or lane 0 of the next
+            K nx = __shfl_down_sync(0xffffffffu, key[e], 1);
+            if (e + 1 < E) {
+                const K f = __shfl_sync(0xffffffffu, key[e + 1 < E ? e + 1 : e], 0);
+                if (lane == 31) nx = f;
+            }
+            bool keep = false;
+            double v = 0.0;
+            if (p < L && (p + 1 == L || (nx >> 9) != (key[e] >> 9))) {  // last write of its column
+                v = o.in_vals[b + (uint32_t)(key[e] & 511u)];
+                keep = !is_zero(v);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const uint64_t w = b + kept + (uint32_t)__popc(bal & lt);
+                o.cols[w] = (uint32_t)(key[e] >> 9);
+                o.vals[w] = v;
+            }
+            kept += (uint32_t)__popc(bal);
+        }
+        if (lane == 0) o.kept[r] = kept;
+    }
+}
+
+// Medium rows: a warp per row from the class-6 list.
+template <class K, bool DEDUP>
+__global__ void __launch_bounds__(256, sizeof(K) == 8 ? 2 : 4) seg_medium_sort(const uint32_t *__restrict__ cols,
+                                                       const uint64_t *__restrict__ s_off,
+                                                       const uint32_t *__restrict__ lists,
+                                                       const unsigned *__restrict__ ctr, int cbits, SegOut o) {
+    const unsigned n = ctr[SC_LIST + 6];  // class 6 heads the lists
     const int lane = threadIdx.x & 31;
     const unsigned warps = gridDim.x * (blockDim.x >> 5);
-    for (unsigned job = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); job < jobs_end[5]; job += warps) {
-        int c = 1;
-        while (job >= jobs_end[c]) ++c;  // warp-uniform
-        const unsigned g = job - jobs_end[c - 1];
-        const uint32_t *list = short_rows + base[c];
-        switch (c) {
-            case 1: sort_short_group<2>(cols, s_off, list, cnt[1], g, cbits, keys_out, idx_out, lane); break;
-            case 2: sort_short_group<4>(cols, s_off, list, cnt[2], g, cbits, keys_out, idx_out, lane); break;
-            case 3: sort_short_group<8>(cols, s_off, list, cnt[3], g, cbits, keys_out, idx_out, lane); break;
-            case 4: sort_short_group<16>(cols, s_off, list, cnt[4], g, cbits, keys_out, idx_out, lane); break;
-            default: sort_short_group<32>(cols, s_off, list, cnt[5], g, cbits, keys_out, idx_out, lane); break;
-        }
+    for (unsigned k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < n; k += warps) {
+        const uint64_t r = lists[k];
+        const uint64_t b = s_off[r];
+        const uint32_t L = (uint32_t)(s_off[r + 1] - b);
+        if (L <= 64) sort_medium_row<2, K, DEDUP>(cols, b, L, r, cbits, o, lane);
+        else if (L <= 128) sort_medium_row<4, K, DEDUP>(cols, b, L, r, cbits, o, lane);
+        else if (L <= 256) sort_medium_row<8, K, DEDUP>(cols, b, L, r, cbits, o, lane);
+        else sort_medium_row<16, K, DEDUP>(cols, b, L, r, cbits, o, lane);
     }
 }
 
-template <int MAXE, int SLICE>
-struct TileSortSmem {
-    uint32_t key[2][MAXE];
-    uint16_t idx[2][MAXE];
-    unsigned cnt[2][MAXE / SLICE][256];
-    unsigned wsum[8];
-    uint64_t start[SEG_TILE_ROWS];  // first input position of the tile's rows, by rank
-    uint32_t row[SEG_TILE_ROWS];
-    unsigned pref[SEG_TILE_ROWS + 1];  // tile position of each rank's first entry
-    unsigned n_rows;
+constexpr uint16_t IDX_ZERO = 0x8000;  // row positions are < 2^14
+
+// Shared-memory index with one pad word per 32: threads of a warp reading
+// word j of their own 32-word segment (the raking scan), or their k-th of 16
+// consecutive entries, hit distinct banks.
+__device__ __forceinline__ uint32_t pad33(uint32_t p) { return p + (p >> 5); }
+
+template <int T, int I, bool DEDUP>
+struct TileSmem {
+    static constexpr int MAXE = T * I;
+    static constexpr int NCTR = RS_WORDS * T;
+    static constexpr bool VSTAGE = DEDUP && MAXE <= 4096;  // values staged in shared memory
+    union {
+        uint32_t ctr[NCTR + NCTR / 32];  // counter word w of thread t at pad33(w T + t)
+        struct {
+            uint32_t key[MAXE + MAXE / 32];
+            uint16_t idx[MAXE + MAXE / 32];  // row position; dedup mode: | IDX_ZERO if the value is zero
+            uint32_t ex[MAXE + MAXE / 32 + 2];  // dedup mode: kept entries before each position
+            double val[VSTAGE ? MAXE : 1];      // dedup mode: values by row position
+        } x;
+    } u;
+    uint32_t wsum[T / 32];
 };
 
-// Sorts the tiles of a job list (MAXE entries at most): a span tile's medium
-// rows, or (jobs with SEG_ROW_JOB set) one long row. Persistent blocks take
-// jobs in a grid-stride loop; one warp per SLICE entries.
-template <int MAXE, int SLICE>
-__global__ void __launch_bounds__(MAXE / SLICE * 32)
+// Rows of tile kernel KI's list (class 7 + KI, T * I entries at most), a
+// block per row; persistent blocks take rows in a grid-stride loop.
+template <int T, int I, bool DEDUP>
+__global__ void __launch_bounds__(T, T <= 128 ? 6 : T <= 256 ? 3 : 1)
 seg_tile_sort(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_off,
-              const unsigned *__restrict__ tile_cnt, const uint32_t *__restrict__ tile_rows,
-              const uint64_t *__restrict__ jobs, const unsigned *__restrict__ n_jobs, int cbits,
-              uint64_t *__restrict__ keys_out, uint32_t *__restrict__ idx_out, unsigned *__restrict__ overflow) {
-    constexpr int W = MAXE / SLICE, T = W * 32;
+              const uint32_t *__restrict__ lists, const unsigned *__restrict__ ctr, int ki, int cbits, SegOut o,
+              unsigned *__restrict__ overflow) {
+    using Sm = TileSmem<T, I, DEDUP>;
+    constexpr int W = T / 32;
     extern __shared__ __align__(16) unsigned char ts_raw[];
-    TileSortSmem<MAXE, SLICE> &S = *reinterpret_cast<TileSortSmem<MAXE, SLICE> *>(ts_raw);
+    Sm &S = *reinterpret_cast<Sm *>(ts_raw);
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const unsigned nj = *n_jobs;
+    unsigned lbase = 0;
+    for (int c = 6; c < 7 + ki; ++c) lbase += ctr[SC_LIST + c];
+    const uint32_t *list = lists + lbase;
+    const unsigned nj = ctr[SC_JOBS + ki];
     for (unsigned jb = blockIdx.x; jb < nj; jb += gridDim.x) {
-        const uint64_t job = jobs[jb];
-        if (job & SEG_ROW_JOB) {
-            if (t == 0) {
-                S.n_rows = 1;
-                S.row[0] = (uint32_t)(job & ~SEG_ROW_JOB);
-            }
-        } else {
-            const unsigned nr = min(tile_cnt[job], (unsigned)SEG_TILE_ROWS);
-            if (t == 0) S.n_rows = nr;
-            if (t < (int)nr) S.row[t] = tile_rows[job * SEG_TILE_ROWS + t];
-        }
-        __syncthreads();
-        const unsigned nr = S.n_rows;
-        if (t < (int)nr) {
-            const uint32_t r = S.row[t];
-            S.start[t] = s_off[r];
-            S.pref[t + 1] = (unsigned)(s_off[r + 1] - s_off[r]);
-        }
-        __syncthreads();
-        if (t == 0) {
-            S.pref[0] = 0;
-            for (unsigned i = 1; i <= nr; ++i) S.pref[i] += S.pref[i - 1];
-        }
-        __syncthreads();
-        const int E = (int)S.pref[nr];
-        const int rbits = nr > 1 ? 32 - __clz(nr - 1) : 0;
-        const int bits = rbits + cbits;
-        if (E > MAXE || bits > 32) {  // (the plan never lists such tiles; cbits <= 26 is checked before)
+        const uint32_t r = list[jb];
+        const uint64_t b = s_off[r];
+        const int E = (int)(s_off[r + 1] - b);
+        if (E > Sm::MAXE) {  // (the plan never lists such rows)
             if (t == 0) atomicOr(overflow, 1u);
-            __syncthreads();
             continue;
         }
-        const int passes = (bits + 7) / 8;
+        const int passes = (cbits + RS_DBITS - 1) / RS_DBITS;
+        // coalesced load in input order into the exchange arrays (dedup mode:
+        // each value read once; its zero test rides in the position's top bit)
         for (int e = t; e < E; e += T) {
-            unsigned lo = 0, hi = nr - 1;  // rank: last i with pref[i] <= e
-            while (lo < hi) {
-                const unsigned mid = (lo + hi + 1) >> 1;
-                if (S.pref[mid] <= (unsigned)e) lo = mid;
-                else hi = mid - 1;
+            S.u.x.key[pad33(e)] = cols[b + e];
+            uint16_t ix = (uint16_t)e;
+            if constexpr (DEDUP) {
+                const double v = o.in_vals[b + e];
+                if (is_zero(v)) ix |= IDX_ZERO;
+                if constexpr (Sm::VSTAGE) S.u.x.val[e] = v;
             }
-            S.key[0][e] = (lo << cbits) | cols[S.start[lo] + (e - S.pref[lo])];
-            S.idx[0][e] = (uint16_t)e;
-        }
-        for (int i = t; i < 2 * W * 256; i += T) (&S.cnt[0][0][0])[i] = 0;
-        __syncthreads();
-        const int q0 = warp * SLICE, q1 = min(E, q0 + SLICE);
-        // digit counts of the first pass, per warp slice
-        for (int q = q0; q < q1 && passes > 0; q += 32) {
-            const int qq = q + lane;
-            const bool ok = qq < q1;
-            const unsigned valid = __ballot_sync(0xffffffffu, ok);
-            const unsigned d = ok ? (S.key[0][qq] & 0xFFu) : 0u;
-            const unsigned peers = warp_match_digit<8>(d) & valid;
-            if (ok && (peers & lanemask_lt()) == 0) S.cnt[0][warp][d] += __popc(peers);
-            __syncwarp();
+            S.u.x.idx[pad33(e)] = ix;
         }
         __syncthreads();
-        int cur = 0;
-        for (int p = 0; p < passes; ++p) {
-            const int c = p & 1, shift = 8 * p;
-            // digit t: start of each warp slice's run, then across digits
-            unsigned excl = 0;
-            if (t < 256) {
-                unsigned tot = 0;
-                for (int w = 0; w < W; ++w) {
-                    const unsigned v = S.cnt[c][w][t];
-                    S.cnt[c][w][t] = tot;
-                    tot += v;
-                }
-                unsigned inc = tot;
+        // thread t holds positions [t I, t I + I): thread order is input order.
+        // v[i] = row position << 16 | rank (16 bits each: E <= 12288)
+        const int nv = max(0, min(I, E - t * I));
+        uint32_t key[I], v[I];
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
-                    if (lane >= o) inc += v;
-                }
-                if (lane == 31) S.wsum[warp] = inc;
-                excl = inc - tot;
+        for (int i = 0; i < I; ++i) {
+            if (i < nv) {
+                key[i] = S.u.x.key[pad33(t * I + i)];
+                v[i] = (uint32_t)S.u.x.idx[pad33(t * I + i)] << 16;
             }
-            for (int i = t; i < W * 256; i += T) (&S.cnt[c ^ 1][0][0])[i] = 0;  // next pass's counts
-            __syncthreads();
-            if (t < 256) {
-                unsigned pre = 0;
-                for (int w = 0; w < warp; ++w) pre += S.wsum[w];
-                const unsigned base = excl + pre;
-                for (int w = 0; w < W; ++w) S.cnt[c][w][t] += base;
-            }
-            __syncthreads();
-            // stable scatter; count the next pass's digits per destination slice
-            for (int q = q0; q < q1; q += 32) {
-                const int qq = q + lane;
-                const bool ok = qq < q1;
-                const unsigned valid = __ballot_sync(0xffffffffu, ok);
-                const uint32_t k = ok ? S.key[cur][qq] : 0u;
-                const unsigned d = (k >> shift) & 0xFFu;
-                const unsigned peers = warp_match_digit<8>(d) & valid;
-                unsigned before = 0;
-                if (ok) before = S.cnt[c][warp][d];
-                __syncwarp();
-                if (ok) {
-                    const unsigned lt = peers & lanemask_lt();
-                    const unsigned pos = before + __popc(lt);
-                    S.key[cur ^ 1][pos] = k;
-                    S.idx[cur ^ 1][pos] = S.idx[cur][qq];
-                    if (lt == 0) S.cnt[c][warp][d] = before + __popc(peers);
-                    if (p + 1 < passes) atomicAdd(&S.cnt[c ^ 1][pos / SLICE][(k >> (shift + 8)) & 0xFFu], 1u);
-                }
-                __syncwarp();
-            }
-            __syncthreads();
-            cur ^= 1;
         }
-        const uint32_t cmask = (uint32_t)((1ull << cbits) - 1);
-        for (int q = t; q < E; q += T) {
-            const uint32_t k = S.key[cur][q];
-            const unsigned i = cbits < 32 ? (k >> cbits) : 0u;
-            const uint64_t out = S.start[i] + (unsigned)(q - S.pref[i]);
-            keys_out[out] = ((uint64_t)S.row[i] << cbits) | (k & cmask);
-            idx_out[out] = (uint32_t)(S.start[i] + (S.idx[cur][q] - S.pref[i]));
+        constexpr uint32_t kColStride = T + T / 32;  // pad33(w T + t) = w kColStride + pad33(t)
+        const uint32_t col0 = pad33(t), rake0 = 33u * t;  // pad33(RS_WORDS t + j) = 33 t + j
+        for (int p = 0; p < passes; ++p) {
+            const int shift = p * RS_DBITS;
+            __syncthreads();  // the exchange arrays are read: the counters take their place
+            // this thread's column of counters: zeroed and counted by it alone
+#pragma unroll 4
+            for (int w = 0; w < RS_WORDS; ++w) S.u.ctr[col0 + w * kColStride] = 0;
+            // (shared atomics on the thread's own column: no contention, and
+            // unlike a load / add / store chain the items' updates pipeline)
+#pragma unroll
+            for (int i = 0; i < I; ++i) {
+                if (i < nv) {
+                    const uint32_t d = (key[i] >> shift) & (RS_DIGITS - 1);
+                    const uint32_t a = col0 + (d & (RS_WORDS - 1)) * kColStride;
+                    const uint32_t sh = (d / RS_WORDS) * 16;  // digits d and d + 32 share a word
+                    const uint32_t cv = atomicAdd(&S.u.ctr[a], 1u << sh);
+                    v[i] = (v[i] & 0xFFFF0000u) | ((cv >> sh) & 0xFFFFu);  // same digit earlier in this thread
+                }
+            }
+            __syncthreads();
+            // raking exclusive scan in (word, thread) order: thread t owns
+            // flat counters [RS_WORDS t, RS_WORDS (t + 1)); both 16-bit halves
+            // add independently (totals < 2^16)
+            uint32_t sum = 0;
+#pragma unroll 8
+            for (int j = 0; j < RS_WORDS; ++j) sum += S.u.ctr[rake0 + j];
+            uint32_t inc = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= d) inc += x;
+            }
+            if (lane == 31) S.wsum[warp] = inc;
+            __syncthreads();
+            uint32_t run = inc - sum, total = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const uint32_t x = S.wsum[w];
+                if (w < warp) run += x;
+                total += x;
+            }
+#pragma unroll
+            for (int j0 = 0; j0 < RS_WORDS; j0 += 8) {  // 8 loads in flight, then 8 stores
+                uint32_t x[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) x[j] = S.u.ctr[rake0 + j0 + j];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    S.u.ctr[rake0 + j0 + j] = run;
+                    run += x[j];
+                }
+            }
+            const uint32_t low_total = total & 0xFFFFu;  // entries whose digit is below RS_WORDS
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < I; ++i) {
+                if (i < nv) {
+                    const uint32_t d = (key[i] >> shift) & (RS_DIGITS - 1);
+                    const uint32_t a = col0 + (d & (RS_WORDS - 1)) * kColStride;
+                    const uint32_t hi = d / RS_WORDS;
+                    v[i] += ((S.u.ctr[a] >> (16 * hi)) & 0xFFFFu) + (hi ? low_total : 0u);
+                }
+            }
+            __syncthreads();  // counters read: the exchange arrays take their place
+#pragma unroll
+            for (int i = 0; i < I; ++i) {
+                if (i < nv) {
+                    const uint32_t q = pad33(v[i] & 0xFFFFu);
+                    S.u.x.key[q] = key[i];
+                    S.u.x.idx[q] = (uint16_t)(v[i] >> 16);
+                }
+            }
+            __syncthreads();
+            if (p + 1 < passes) {
+#pragma unroll
+                for (int i = 0; i < I; ++i) {
+                    if (i < nv) {
+                        key[i] = S.u.x.key[pad33(t * I + i)];
+                        v[i] = (uint32_t)S.u.x.idx[pad33(t * I + i)] << 16;
+                    }
+                }
+            }
         }
-        __syncthreads();  // shared state is rebuilt by the next job
+        if constexpr (!DEDUP) {
+            for (int q = t; q < E; q += T) {
+                o.keys[b + q] = ((uint64_t)r << cbits) | S.u.x.key[pad33(q)];
+                o.idx[b + q] = (uint32_t)(b + S.u.x.idx[pad33(q)]);
+            }
+        } else {
+            // keep = last of a run of equal columns (the last write) and not
+            // zero; ex = exclusive count of kept entries
+            uint32_t keepm = 0, cnt = 0;
+#pragma unroll
+            for (int i = 0; i < I; ++i) {
+                const int q = t * I + i;
+                if (q < E) {
+                    const uint32_t k = S.u.x.key[pad33(q)];
+                    if ((q + 1 == E || S.u.x.key[pad33(q + 1)] != k) && !(S.u.x.idx[pad33(q)] & IDX_ZERO)) {
+                        keepm |= 1u << i;
+                        ++cnt;
+                    }
+                }
+            }
+            uint32_t inc = cnt;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= d) inc += x;
+            }
+            if (lane == 31) S.wsum[warp] = inc;
+            __syncthreads();
+            uint32_t run = inc - cnt, total = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const uint32_t x = S.wsum[w];
+                if (w < warp) run += x;
+                total += x;
+            }
+#pragma unroll
+            for (int i = 0; i < I; ++i) {
+                const int q = t * I + i;
+                if (q < E) {
+                    S.u.x.ex[pad33(q)] = run;
+                    run += (keepm >> i) & 1u;
+                }
+            }
+            if (t == 0) {
+                S.u.x.ex[pad33(E)] = total;
+                o.kept[r] = total;
+            }
+            __syncthreads();
+            for (int q = t; q < E; q += T) {
+                const uint32_t e0 = S.u.x.ex[pad33(q)];
+                if (S.u.x.ex[pad33(q + 1)] != e0) {
+                    const unsigned tp = S.u.x.idx[pad33(q)] & ~IDX_ZERO;
+                    o.cols[b + e0] = S.u.x.key[pad33(q)];
+                    if constexpr (Sm::VSTAGE) o.vals[b + e0] = S.u.x.val[tp];
+                    else o.vals[b + e0] = o.in_vals[b + tp];
+                }
+            }
+        }
+        __syncthreads();  // shared state is rebuilt by the next row
     }
+}
+
+template <int T, int I, bool DEDUP>
+int launch_tile_sort(Ctx *c, const uint32_t *cols, const uint64_t *s_off, const uint32_t *lists, const unsigned *ctr,
+                     int ki, uint64_t max_rows, int cbits, const SegOut &o, unsigned *overflow, cudaStream_t s) {
+    auto k = seg_tile_sort<T, I, DEDUP>;
+    constexpr size_t smem = sizeof(TileSmem<T, I, DEDUP>);
+    SPG_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    SPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, T, smem));
+    // persistent blocks over a list whose length stays on the device
+    const uint64_t grid = std::min<uint64_t>(max_rows, (uint64_t)c->n_sms * (uint64_t)std::max(per_sm, 1));
+    if (grid == 0) return SPG_OK;
+    k<<<(unsigned)grid, T, smem, s>>>(cols, s_off, lists, ctr, ki, cbits, o, overflow);
+    SPG_LAUNCH_CHECK();
+    return SPG_OK;
+}
+
+template <bool DEDUP>
+int seg_sort(Ctx *c, const uint32_t *cols, const uint64_t *s_off, uint64_t m, uint64_t n_rows, int cbits,
+             const SegOut &o, bool *done, cudaStream_t s) {
+    *done = false;
+    if (cbits > SEG_MAX_CBITS || m > 0xFFFFFFFFull) return SPG_OK;
+    DevBuf ctr_b, lists_b;
+    SPG_TRY(ctr_b.alloc(2 * SC_N * sizeof(unsigned), s));  // counters, then the fill cursors
+    SPG_TRY(lists_b.alloc(n_rows * sizeof(uint32_t), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(ctr_b.ptr, 0, 2 * SC_N * sizeof(unsigned), s));
+    unsigned *ctr = ctr_b.as<unsigned>(), *cur = ctr + SC_N, *ovf = ctr + SC_OVERFLOW;
+    uint32_t *lists = lists_b.as<uint32_t>();
+    const unsigned gr = grid_for(n_rows, 256, (unsigned)c->n_sms * 8);
+    seg_count<<<gr, 256, 0, s>>>(s_off, n_rows, ctr);
+    SPG_LAUNCH_CHECK();
+    seg_place<DEDUP><<<gr, 256, 0, s>>>(cols, s_off, n_rows, cbits, ctr, cur, lists, o);
+    SPG_LAUNCH_CHECK();
+    seg_short_sort<DEDUP><<<grid_for((n_rows + 31) / 32, 8, (unsigned)c->n_sms * 16), 256, 0, s>>>(cols, s_off, n_rows,
+                                                                                                cbits, o);
+    SPG_LAUNCH_CHECK();
+    if (cbits <= 22) seg_medium_sort<uint32_t, DEDUP><<<(unsigned)c->n_sms * 8, 256, 0, s>>>(cols, s_off, lists, ctr, cbits, o);
+    else seg_medium_sort<uint64_t, DEDUP><<<(unsigned)c->n_sms * 8, 256, 0, s>>>(cols, s_off, lists, ctr, cbits, o);
+    SPG_LAUNCH_CHECK();
+    SPG_TRY((launch_tile_sort<TS0_T, TS0_I, DEDUP>(c, cols, s_off, lists, ctr, 0, m / (SEG_MEDIUM + 1) + 1, cbits,
+                                                   o, ovf, s)));
+    SPG_TRY((launch_tile_sort<TS1_T, TS1_I, DEDUP>(c, cols, s_off, lists, ctr, 1, m / (TS0 + 1) + 1, cbits, o, ovf,
+                                                   s)));
+    SPG_TRY((launch_tile_sort<TS2_T, TS2_I, DEDUP>(c, cols, s_off, lists, ctr, 2, m / (TS1 + 1) + 1, cbits, o, ovf,
+                                                   s)));
+    unsigned h = 1u;
+    SPG_CUDA_TRY(cudaMemcpyAsync(&h, ovf, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    SPG_TRY(c->phase_sync(s));
+    *done = h == 0;
+    return SPG_OK;
 }
 
 }  // namespace
@@ -773,59 +981,30 @@ seg_tile_sort(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_
 int sort_grouped_rows(Ctx *c, const uint32_t *rows, const uint32_t *cols, const uint64_t *s_off, uint64_t m,
                       uint64_t n_rows, int cbits, uint64_t *keys_out, uint32_t *idx_out, bool *done, cudaStream_t s) {
     (void)rows;  // the rows are s_off's
-    *done = false;
     if (m == 0) {
         *done = true;
         return SPG_OK;
     }
-    if (cbits > SEG_MAX_CBITS || m > 0xFFFFFFFFull) return SPG_OK;
-    const uint64_t n_spans = (m + SEG_SPAN - 1) / SEG_SPAN;
-    const uint64_t n_small = n_spans + m / (SEG_SPAN + 1) + 1, n_large = m / (TS_SMALL + 1) + 1;
-    DevBuf ctr_b, tiles_b, tile_rows_b, short_b, jobs_b;
-    SPG_TRY(ctr_b.alloc(SC_N * sizeof(unsigned), s));
-    SPG_TRY(tiles_b.alloc(2 * n_spans * sizeof(unsigned), s));  // tile_cnt, tile_len
-    SPG_TRY(tile_rows_b.alloc(n_spans * SEG_TILE_ROWS * sizeof(uint32_t), s));
-    SPG_TRY(short_b.alloc(n_rows * sizeof(uint32_t), s));
-    SPG_TRY(jobs_b.alloc((n_small + n_large) * sizeof(uint64_t), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(ctr_b.ptr, 0, SC_N * sizeof(unsigned), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(tiles_b.ptr, 0, 2 * n_spans * sizeof(unsigned), s));
-    unsigned *ctr = ctr_b.as<unsigned>(), *tile_cnt = tiles_b.as<unsigned>(), *tile_len = tile_cnt + n_spans;
-    uint64_t *small_jobs = jobs_b.as<uint64_t>(), *large_jobs = small_jobs + n_small;
-    const unsigned gr = grid_for(n_rows, 256, (unsigned)c->n_sms * 8);
-    seg_count<<<gr, 256, 0, s>>>(s_off, n_rows, ctr);
-    SPG_LAUNCH_CHECK();
-    seg_place<<<gr, 256, 0, s>>>(cols, s_off, n_rows, cbits, ctr, short_b.as<uint32_t>(), tile_cnt, tile_len,
-                                 tile_rows_b.as<uint32_t>(), small_jobs, large_jobs, keys_out, idx_out);
-    SPG_LAUNCH_CHECK();
-    seg_tiles<<<grid_for(n_spans, 256), 256, 0, s>>>(tile_len, n_spans, ctr, small_jobs);
-    SPG_LAUNCH_CHECK();
-    seg_short_sort<<<(unsigned)c->n_sms * 8, 256, 0, s>>>(cols, s_off, short_b.as<uint32_t>(), ctr, cbits, keys_out,
-                                                          idx_out);
-    SPG_LAUNCH_CHECK();
-    constexpr size_t small_smem = sizeof(TileSortSmem<TS_SMALL, TS_SLICE_SMALL>);
-    constexpr size_t large_smem = sizeof(TileSortSmem<TS_MAX, TS_SLICE_LARGE>);
-    constexpr unsigned small_threads = TS_SMALL / TS_SLICE_SMALL * 32;
-    constexpr unsigned large_threads = TS_MAX / TS_SLICE_LARGE * 32;
-    auto small_k = seg_tile_sort<TS_SMALL, TS_SLICE_SMALL>;
-    auto large_k = seg_tile_sort<TS_MAX, TS_SLICE_LARGE>;
-    SPG_CUDA_TRY(cudaFuncSetAttribute(small_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
-    SPG_CUDA_TRY(cudaFuncSetAttribute(large_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)large_smem));
-    // persistent blocks over the job lists, whose lengths stay on the device
-    const unsigned small_grid = (unsigned)std::min<uint64_t>(n_small, (uint64_t)c->n_sms * 3);
-    const unsigned large_grid = (unsigned)std::min<uint64_t>(n_large, (uint64_t)c->n_sms);
-    small_k<<<small_grid, small_threads, small_smem, s>>>(cols, s_off, tile_cnt, tile_rows_b.as<uint32_t>(),
-                                                          small_jobs, ctr + SC_SMALL, cbits, keys_out, idx_out,
-                                                          ctr + SC_OVERFLOW);
-    SPG_LAUNCH_CHECK();
-    large_k<<<large_grid, large_threads, large_smem, s>>>(cols, s_off, tile_cnt, tile_rows_b.as<uint32_t>(),
-                                                          large_jobs, ctr + SC_LARGE, cbits, keys_out, idx_out,
-                                                          ctr + SC_OVERFLOW);
-    SPG_LAUNCH_CHECK();
-    unsigned h = 1u;
-    SPG_CUDA_TRY(cudaMemcpyAsync(&h, ctr + SC_OVERFLOW, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    SPG_TRY(c->phase_sync(s));
-    *done = h == 0;
-    return SPG_OK;
+    SegOut o{};
+    o.keys = keys_out;
+    o.idx = idx_out;
+    return seg_sort<false>(c, cols, s_off, m, n_rows, cbits, o, done, s);
+}
+
+int dedup_grouped_rows(Ctx *c, const uint32_t *cols, const double *vals, const uint64_t *s_off, uint64_t m,
+                       uint64_t n_rows, int cbits, uint32_t *out_cols, double *out_vals, uint64_t *kept, bool *done,
+                       cudaStream_t s) {
+    SegOut o{};
+    o.in_vals = vals;
+    o.cols = out_cols;
+    o.vals = out_vals;
+    o.kept = kept;
+    if (m == 0) {
+        SPG_CUDA_TRY(cudaMemsetAsync(kept, 0, n_rows * sizeof(uint64_t), s));
+        *done = true;
+        return SPG_OK;
+    }
+    return seg_sort<true>(c, cols, s_off, m, n_rows, cbits, o, done, s);
 }
 
 }  // namespace spg

@@ -16,13 +16,12 @@
 //      bitonic-sorted in registers. Column order with slot order inside a
 //      column is exactly ascending k for each (i, j). The sorted (column,
 //      product) pairs go to the tile's shared memory;
-//   2. per row, one thread: the row's runs of equal columns are summed left
-//      to right (__dadd_rn from the run's first product: +0.0 + p1 = p1
-//      whenever the sum can be kept, so starting at p1 changes no kept
-//      value) and the kept sums (not +-0) compacted in place. A thread per
-//      row keeps the FP64 lanes of a warp busy with 32 rows' additions: on
-//      GB300 a warp FP64 instruction costs its full issue slot whatever its
-//      active mask;
+//   2. the same warp: the lane holding the first product of a run of equal
+//      columns sums the run left to right (__dadd_rn from the run's first
+//      product: +0.0 + p1 = p1 whenever the sum can be kept, so starting at
+//      p1 changes no kept value); most runs are one product long and cost no
+//      FP64 instruction. The kept sums (not +-0) are ranked with ballots and
+//      compacted in place, and the row's kept count goes to the tile;
 //   3. the tile's kept count goes through an ordered scan (decoupled
 //      look-back over the tiles' published counts, 32 predecessors per step
 //      by one warp, every wait bounded), and
@@ -138,47 +137,14 @@ __global__ void sgs_heavy_index(const uint32_t *__restrict__ crow, uint64_t n, u
     }
 }
 
-// Ascending bitonic sort of the 32 * E keys a warp holds, key[e] of lane l
-// being element 32 e + l. Partners 32 or more apart share a lane (registers),
-// nearer ones are exchanged by shuffles.
-template <int E, class K>
-__device__ __forceinline__ void warp_bitonic(K (&key)[E], int lane) {
-#pragma unroll
-    for (int k = 2; k <= 32 * E; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j >= 32) {
-                const int jj = j >> 5;
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    if ((e & jj) == 0) {
-                        const int f = e | jj;
-                        const bool up = ((32 * e) & k) == 0;  // k >= 64: the item decides
-                        const K a = key[e], b = key[f];
-                        const bool sw = up ? (a > b) : (a < b);
-                        key[e] = sw ? b : a;
-                        key[f] = sw ? a : b;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const K o = __shfl_xor_sync(0xffffffffu, key[e], j);
-                    const int i = 32 * e + lane;
-                    const bool keep_min = (((i & k) == 0) == ((i & j) == 0));
-                    key[e] = keep_min ? (o < key[e] ? o : key[e]) : (o > key[e] ? o : key[e]);
-                }
-            }
-        }
-    }
-}
-
-// One row, one warp: expand, multiply, sort; writes the row's P sorted
-// (column, product) pairs at s_col / s_prod [reg, reg + P). Uses the warp's
-// w_a / w_b / w_own (HB entries each). P <= 32 E, A's row has <= HB entries.
+// One row, one warp: expand, multiply, sort, sum the runs of equal columns
+// and compact; leaves the row's kept (column, sum) pairs at s_col / s_prod
+// [reg, reg + kept) and returns kept (the same in every lane). Uses the
+// warp's w_a / w_b / w_own (HB entries each). P <= 32 E, A's row has <= HB
+// entries.
 template <int E, int SB, class K>
-__device__ void sgs_row(const SgsArgs &g, uint64_t i, uint32_t reg, uint32_t P, uint32_t *s_col, double *s_prod,
-                        double *w_a, int64_t *w_b, uint16_t *w_own, int lane) {
+__device__ uint32_t sgs_row(const SgsArgs &g, uint64_t i, uint32_t reg, uint32_t P, uint32_t *s_col, double *s_prod,
+                            double *w_a, int64_t *w_b, uint16_t *w_own, int lane) {
     const uint64_t ab = g.aoff[i];
     const uint32_t r = (uint32_t)(g.aoff[i + 1] - ab);
     for (uint32_t s = lane; s < P; s += 32) w_own[s] = 0;
@@ -252,6 +218,39 @@ __device__ void sgs_row(const SgsArgs &g, uint64_t i, uint32_t reg, uint32_t P, 
         }
     }
     __syncwarp();
+    // runs: the head lane sums its run in slot order (Spira's order)
+    uint32_t col[E];
+    bool keep[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t q = 32u * e + lane;
+        keep[e] = false;
+        col[e] = 0;
+        if (q < P) {
+            col[e] = (uint32_t)(key[e] >> SB);
+            if (q == 0 || s_col[reg + q - 1] != col[e]) {
+                double acc = pv[e];
+                for (uint32_t r = q + 1; r < P && s_col[reg + r] == col[e]; ++r) acc = __dadd_rn(acc, s_prod[reg + r]);
+                pv[e] = acc;
+                keep[e] = acc != 0.0;  // spgemm.hpp:44: v != V{}
+            }
+        }
+    }
+    __syncwarp();  // every run read before the compacted writes land
+    uint32_t kept = 0;
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const unsigned bal = __ballot_sync(0xffffffffu, keep[e]);
+        if (keep[e]) {
+            const uint32_t w = reg + kept + (uint32_t)__popc(bal & lt);
+            s_col[w] = col[e];
+            s_prod[w] = pv[e];
+        }
+        kept += (uint32_t)__popc(bal);
+    }
+    __syncwarp();
+    return kept;
 }
 
 // Ordered scan of the tiles' counts, by one warp: lane l reads the word of
@@ -323,6 +322,7 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
     __shared__ uint64_t sh_tile, sh_base;
     __shared__ uint32_t sh_reg[SGS_RB];
     __shared__ uint32_t sh_excl[SGS_RB + 1];
+    __shared__ uint32_t sh_kept[SGS_RB];
     __shared__ uint32_t sh_wsum[SGS_WARPS];
     __shared__ int sh_ok;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -343,48 +343,21 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
             const uint64_t i = row0 + j;
             const uint32_t reg = (uint32_t)(g.pofs[i] - p0) + j;
             const uint32_t P = (uint32_t)(g.pofs[i + 1] - g.pofs[i]);
-            if (P == 0) continue;
-            if (P <= 32) sgs_row<1, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
-            else if (P <= 64) sgs_row<2, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
+            uint32_t kept = 0;
+            if (P == 0) kept = 0;
+            else if (P <= 32) kept = sgs_row<1, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
+            else if (P <= 64) kept = sgs_row<2, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
             else if constexpr (HB >= 128) {
-                if (P <= 128) sgs_row<4, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
-                else if constexpr (HB >= 256) sgs_row<8, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
+                if (P <= 128) kept = sgs_row<4, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
+                else if constexpr (HB >= 256) kept = sgs_row<8, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
+            }
+            if (lane == 0) {
+                sh_kept[j] = kept;
+                sh_reg[j] = reg;
             }
         }
         __syncthreads();
-        if ((uint32_t)tid < nr) {
-            const uint64_t i = row0 + tid;
-            const uint32_t reg = (uint32_t)(g.pofs[i] - p0) + tid;
-            const uint32_t P = (uint32_t)(g.pofs[i + 1] - g.pofs[i]);
-            sh_reg[tid] = reg;
-            uint32_t w = reg;
-            if (P) {
-                const uint32_t end = reg + P;
-                uint32_t cc = s_col[reg];
-                double acc = s_prod[reg];
-                for (uint32_t q = reg + 1; q < end; ++q) {
-                    const uint32_t c2 = s_col[q];
-                    const double pq = s_prod[q];
-                    if (c2 == cc) {
-                        acc = __dadd_rn(acc, pq);
-                    } else {
-                        if (acc != 0.0) {  // spgemm.hpp:44: v != V{}
-                            s_col[w] = cc;
-                            s_prod[w] = acc;
-                            ++w;
-                        }
-                        cc = c2;
-                        acc = pq;
-                    }
-                }
-                if (acc != 0.0) {
-                    s_col[w] = cc;
-                    s_prod[w] = acc;
-                    ++w;
-                }
-            }
-            cnt = w - reg;
-        }
+        if ((uint32_t)tid < nr) cnt = sh_kept[tid];
     } else if (tid == 0) {
         cnt = g.hcnt[row0];
     }
@@ -496,10 +469,14 @@ int spgemm_warpsort(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cu
                                                      reinterpret_cast<unsigned long long *>(nh_dev.as<uint64_t>()));
     SPG_LAUNCH_CHECK();
     SPG_TRY(exclusive_scan_u64(c, pofs.as<uint64_t>(), m + 1, nh_dev.as<uint64_t>() + 1, s));
-    SPG_TRY(exclusive_scan_u64(c, hp.as<uint64_t>(), m + 1, nh_dev.as<uint64_t>() + 2, s));
     uint64_t h[3] = {0, 0, 0};  // heavy rows, products, heavy products
-    SPG_CUDA_TRY(cudaMemcpyAsync(h, nh_dev.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SPG_CUDA_TRY(cudaMemcpyAsync(h, nh_dev.ptr, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     SPG_TRY(c->phase_sync(s));
+    if (h[0]) {  // heavy rows' product offsets only when there are heavy rows
+        SPG_TRY(exclusive_scan_u64(c, hp.as<uint64_t>(), m + 1, nh_dev.as<uint64_t>() + 2, s));
+        SPG_CUDA_TRY(cudaMemcpyAsync(h + 2, nh_dev.as<uint64_t>() + 2, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        SPG_TRY(c->phase_sync(s));
+    }
     const uint64_t n_heavy = h[0], P = h[1], HP = h[2];
     if (P >= (1ull << 32))
         return set_error(SPG_ERR_UNSUPPORTED, "spgemm: %llu products exceed 2^32-1", (unsigned long long)P);

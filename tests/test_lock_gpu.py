@@ -139,11 +139,12 @@ def test_lock_row_grouped_inserts(ctx, lengths, n_rows, n_cols):
 def test_lock_row_grouped_every_length_class(ctx, n_cols):
     """Grouped inserts with a row at every boundary of the on-chip sort's
     length classes (written through, bitonic in registers for 2..32 entries,
-    span tiles up to 2048, single-row tiles up to 12 288), rows shuffled so
-    the classes interleave; duplicates and zeros included. 300 columns make
-    duplicates dense; 2^26 columns is the widest key the on-chip sort takes,
-    one more column sends the epoch to the global sort."""
-    base = [0, 1, 2, 3, 4, 5, 7, 8, 9, 15, 16, 17, 31, 32, 33, 34, 100, 2047, 2048, 2049, 4096, 4097, 12288]
+    a warp per row up to 512, a block per row up to 2048 / 4096 / 12 288),
+    rows shuffled so the classes interleave; duplicates and zeros included.
+    300 columns make duplicates dense; 2^26 columns is the widest key the
+    on-chip sort takes, one more column sends the epoch to the global sort."""
+    base = [0, 1, 2, 3, 4, 5, 7, 8, 9, 15, 16, 17, 31, 32, 33, 34, 100, 511, 512, 513, 2047, 2048, 2049, 4096,
+            4097, 12288]
     lengths = np.array(base * 3, np.int64)
     lengths = lengths[np.argsort(gen.hash3(5, 0, np.arange(len(lengths), dtype=np.uint64)))]
     n_rows = len(lengths)
@@ -155,6 +156,23 @@ def test_lock_row_grouped_every_length_class(ctx, n_cols):
     vals[::17] = 0.0
     A = gpu_lock(ctx, n_rows, n_cols, [(rows, cols, vals)])
     assert_csr_equal(A.download(), oracle.lock_epochs(n_rows, n_cols, [(rows, cols, vals)]))
+
+
+def test_lock_row_grouped_nothing_dropped(ctx):
+    """Grouped inserts with distinct columns in every row and no zeros: the
+    rows sorted in place are the CSR as they stand (nothing moves after the
+    sort); capacity stays exact."""
+    lengths = np.array([1, 2, 5, 31, 32, 33, 300, 512, 513, 2048, 2049, 5000, 0, 7] * 2, np.int64)
+    n_rows, n_cols = len(lengths), 1 << 20
+    rows = np.repeat(np.arange(n_rows, dtype=np.uint32), lengths)
+    start = np.repeat(np.cumsum(lengths) - lengths, lengths)
+    j = np.arange(len(rows), dtype=np.int64) - start  # position inside the row
+    cols = ((j * 40_503 + rows.astype(np.int64) * 977) % n_cols).astype(np.uint32)  # distinct within a row
+    vals = 1.0 + gen.unit(gen.hash3(3, 2, np.arange(len(rows), dtype=np.uint64)))
+    A = gpu_lock(ctx, n_rows, n_cols, [(rows, cols, vals)])
+    ref = oracle.lock_epochs(n_rows, n_cols, [(rows, cols, vals)])
+    assert int(ref.off[-1]) == len(rows)
+    assert_csr_equal(A.download(), ref)
 
 
 def test_lock_row_grouped_sparse_rows(ctx):
@@ -267,3 +285,26 @@ def test_spmv_before_lock_is_logic_error(ctx):
     np.testing.assert_array_equal(A.spmv_host(np.ones(3)), np.zeros(3))
     with pytest.raises(sg.InvalidArgument):
         A.spmv_host(np.zeros(2))
+
+
+@pytest.mark.parametrize("offset", [0, 1, 3])
+def test_lock_device_arrays_at_any_alignment(ctx, offset):
+    """Device-staged inserts whose arrays start 0, 4 or 12 bytes past a
+    16-byte boundary (the range check reads 16 bytes at a time only when both
+    index arrays are aligned); sizes not a multiple of 4, grouped and
+    ungrouped epochs."""
+    import torch
+    for grouped in (True, False):
+        n, m = 5000, 40_001
+        ctr = np.arange(m, dtype=np.uint64)
+        r = np.sort(gen.below(gen.hash3(offset, 1, ctr), n)) if grouped else gen.below(gen.hash3(offset, 1, ctr), n)
+        c = gen.below(gen.hash3(offset, 2, ctr), n)
+        v = gen.sym_unit(gen.hash3(offset, 3, ctr))
+        pad = np.zeros(offset, np.uint32)
+        dr = torch.from_numpy(np.concatenate([pad, r]).view(np.int32)).cuda()[offset:]
+        dc = torch.from_numpy(np.concatenate([pad, c]).view(np.int32)).cuda()[offset:]
+        dv = torch.from_numpy(v).cuda()
+        assert (dr.data_ptr() % 16 == 0) == (offset == 0)
+        A = sg.Csr(ctx, n, n)
+        A.lock_device(dr, dc, dv, m)
+        assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(r, c, v)]))

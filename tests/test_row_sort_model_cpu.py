@@ -1,9 +1,9 @@
 """CPU model of the row-grouped sort that lock() and transpose use when the
 staged rows are already grouped (spira_gb300/csrc/spg_prims.cu,
-sort_grouped_rows): the length classes, the segmented bitonic network of the
-short rows (lane by lane, as the warp runs it), the span tiles of the medium
-rows and the bounds the kernels rely on (rows per tile, entries per tile, key
-bits). The order it must give is Spira's: stable (row, col) order, the
+sort_grouped_rows and dedup_grouped_rows): the length classes, the segmented
+bitonic network of the short rows and the warp network of the medium rows
+(lane by lane, as the warp runs them), the block radix rank of the long rows,
+and the bounds the kernels rely on (key bits, bank conflicts). The order it must give is Spira's: stable (row, col) order, the
 staging position deciding among duplicates so that the last write wins
 (include/spira/matrix/buffer/aos_array_buffer.hpp:76-101, driven by
 include/spira/matrix/matrix.hpp:277-342)."""
@@ -12,7 +12,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-SEG_SPAN, SEG_TILE_ROWS, TS_SMALL, TS_MAX, SEG_MAX_CBITS = 2048, 64, 4096, 12288, 26
+SEG_MEDIUM, SEG_MAX_CBITS = 512, 26
+TS0, TS1, TS_MAX = 128 * 16, 256 * 16, 1024 * 12
 
 
 def seg_class(L: int) -> int:
@@ -20,13 +21,15 @@ def seg_class(L: int) -> int:
         return 0
     if L <= 32:
         return int(L - 1).bit_length()
-    if L <= SEG_SPAN:
+    if L <= SEG_MEDIUM:
         return 6
-    if L <= TS_SMALL:
+    if L <= TS0:
         return 7
-    if L <= TS_MAX:
+    if L <= TS1:
         return 8
-    return 9
+    if L <= TS_MAX:
+        return 9
+    return 10
 
 
 def segment_bitonic(keys: np.ndarray, P: int) -> np.ndarray:
@@ -48,7 +51,7 @@ def segment_bitonic(keys: np.ndarray, P: int) -> np.ndarray:
 
 def test_length_classes():
     assert [seg_class(L) for L in (0, 1, 2, 3, 4, 5, 8, 9, 16, 17, 32)] == [0, 0, 1, 2, 2, 3, 3, 4, 4, 5, 5]
-    assert [seg_class(L) for L in (33, 2048, 2049, 4096, 4097, 12288, 12289)] == [6, 6, 7, 7, 8, 8, 9]
+    assert [seg_class(L) for L in (33, 512, 513, 2048, 2049, 4096, 4097, 12288, 12289)] == [6, 6, 7, 7, 8, 8, 9, 9, 10]
     # the padded length 2^c holds the row
     for L in range(2, 33):
         c = seg_class(L)
@@ -80,64 +83,129 @@ def test_short_keys_stay_below_the_padding():
     assert (((1 << SEG_MAX_CBITS) - 1) << 5 | 31) < 0xFFFFFFFF
 
 
-def _spans(lengths):
-    """Span tiles of the medium rows: span -> [(row, start, length)]."""
-    off = np.concatenate([[0], np.cumsum(lengths)])
-    tiles = {}
-    for r, L in enumerate(lengths):
-        if seg_class(L) == 6:
-            tiles.setdefault(int(off[r]) // SEG_SPAN, []).append((r, int(off[r]), int(L)))
-    return tiles
+def warp_bitonic(keys: np.ndarray, E: int) -> np.ndarray:
+    """The warp network over 32 E elements (element 32 e + lane in key[e] of
+    that lane): partners 32 or more apart within a lane's registers, nearer
+    ones by shuffles; as the kernels run it."""
+    key = keys.reshape(E, 32).copy()  # key[e][lane]
+    lane = np.arange(32)
+    k = 2
+    while k <= 32 * E:
+        j = k >> 1
+        while j > 0:
+            if j >= 32:
+                jj = j >> 5
+                for e in range(E):
+                    if e & jj == 0:
+                        f = e | jj
+                        up = ((32 * e) & k) == 0
+                        a, b = key[e].copy(), key[f].copy()
+                        sw = (a > b) if up else (a < b)
+                        key[e] = np.where(sw, b, a)
+                        key[f] = np.where(sw, a, b)
+            else:
+                for e in range(E):
+                    o = key[e][lane ^ j]
+                    i = 32 * e + lane
+                    keep_min = ((i & k) == 0) == ((i & j) == 0)
+                    key[e] = np.where(keep_min, np.minimum(o, key[e]), np.maximum(o, key[e]))
+            j >>= 1
+        k <<= 1
+    return key.reshape(-1)
 
 
-@pytest.mark.parametrize("pattern", ["all33", "mixed", "zipf_like", "one_long_between"])
-def test_span_tiles_fit_the_small_kernel(pattern):
-    rng = np.random.default_rng(7)
-    if pattern == "all33":
-        lengths = np.full(5000, 33)
-    elif pattern == "mixed":
-        lengths = rng.choice([1, 2, 33, 40, 2048, 2047, 5000], 3000)
-    elif pattern == "zipf_like":
-        lengths = np.minimum(rng.zipf(1.8, 20000), 10000)
-    else:
-        lengths = np.array([2048, 33, 2048, 1, 2048, 4096, 33] * 50)
-    tiles = _spans(lengths)
-    for rows in tiles.values():
-        assert len(rows) <= SEG_TILE_ROWS - 1  # 33 apart in a 2048 span: <= 63
-        E = sum(L for _, _, L in rows)
-        assert E < 2 * SEG_SPAN <= TS_SMALL
-        rbits = (len(rows) - 1).bit_length()
-        assert rbits + SEG_MAX_CBITS <= 32
+@pytest.mark.parametrize("E", [2, 4, 8, 16])
+def test_medium_row_network_gives_stable_column_order(E):
+    """Rows of 33..512 entries: keys col << 9 | position, padding all ones;
+    32-bit keys while the columns need at most 22 bits."""
+    rng = np.random.default_rng(E)
+    for trial in range(20):
+        L = int(rng.integers(16 * E + 1, 32 * E + 1)) if E > 2 else int(rng.integers(33, 65))
+        cbits = [6, 22][trial % 2]
+        cols = rng.integers(0, 1 << cbits, L)
+        cols[1::9] = cols[0]  # duplicates: the position orders them
+        keys = np.full(32 * E, 0xFFFFFFFF, np.uint64)
+        keys[:L] = (cols.astype(np.uint64) << np.uint64(9)) | np.arange(L, dtype=np.uint64)
+        out = warp_bitonic(keys, E)
+        want = sorted(range(L), key=lambda p: (cols[p], p))
+        assert [int(k) & 511 for k in out[:L]] == want
+        assert (out[L:] == 0xFFFFFFFF).all()
+    # the largest real key stays below the padding only up to 22 column bits
+    assert (((1 << 22) - 1) << 9 | 511) < 0xFFFFFFFF
+    assert (((1 << 23) - 1) << 9 | 511) == 0xFFFFFFFF
 
 
-def tile_sort_model(cols_in, rows_in_tile, cbits):
-    """One tile: keys (rank << cbits | col), stable sort, outputs by rank."""
-    pref = np.concatenate([[0], np.cumsum([L for _, _, L in rows_in_tile])])
-    keys, pos = [], []
-    for i, (_, b, L) in enumerate(rows_in_tile):
-        for e in range(L):
-            keys.append((i << cbits) | int(cols_in[b + e]))
-            pos.append(pref[i] + e)
-    order = np.argsort(np.array(keys, np.uint64), kind="stable")
-    out = {}
-    for q, o in enumerate(order):
-        i = keys[o] >> cbits
-        r, b, _ = rows_in_tile[i]
-        out[b + (q - pref[i])] = (r, keys[o] & ((1 << cbits) - 1), b + (pos[o] - pref[i]))
-    return out
+RS_DBITS, RS_WORDS = 6, 32
 
 
-def test_tile_sort_model_matches_stable_row_column_order():
-    rng = np.random.default_rng(3)
-    lengths = rng.choice([33, 50, 200, 1000, 2048], 60)
-    n_cols = 1 << 22
-    cbits = (n_cols - 1).bit_length()
-    off = np.concatenate([[0], np.cumsum(lengths)])
-    cols = rng.integers(0, 64, off[-1])  # many duplicates inside every row
-    for rows in _spans(lengths).values():
-        got = tile_sort_model(cols, rows, cbits)
-        for r, b, L in rows:
-            want = sorted(range(L), key=lambda e: (cols[b + e], e))
-            for q in range(L):
-                rr, c, src = got[b + q]
-                assert rr == r and c == cols[b + want[q]] and src == b + want[q]
+def pad33(p):
+    return p + (p >> 5)
+
+
+def block_radix_pass(keys, idxs, T, I, shift):
+    """One pass of the tile kernel's ranking, index for index: packed 16-bit
+    counters (digit d in word d % 32, half d // 32) in a column per thread,
+    a raking scan over flat (word, thread) order, rank = prefix + earlier
+    same digit in the thread. Returns the scattered (keys, idxs)."""
+    E = len(keys)
+    col_stride = T + T // 32
+    ctr = np.zeros(RS_WORDS * T + RS_WORDS * T // 32, np.uint64)
+    local = {}
+    for t in range(T):
+        for i in range(I):
+            e = t * I + i
+            if e >= E:
+                break
+            d = (int(keys[e]) >> shift) & 63
+            a = pad33(t) + (d & 31) * col_stride
+            assert a == pad33((d & 31) * T + t)
+            sh = (d // 32) * 16
+            cv = int(ctr[a])
+            ctr[a] = cv + (1 << sh)
+            local[e] = (cv >> sh) & 0xFFFF
+    sums = [sum(int(ctr[33 * t + j]) for j in range(RS_WORDS)) for t in range(T)]
+    assert all(33 * t + j == pad33(RS_WORDS * t + j) for t in range(T) for j in range(RS_WORDS))
+    total = sum(sums)
+    run = 0
+    for t in range(T):
+        for j in range(RS_WORDS):
+            a = 33 * t + j
+            x = int(ctr[a])
+            ctr[a] = run
+            run += x
+    low_total = total & 0xFFFF
+    out_k = np.zeros(E, np.uint64)
+    out_i = np.zeros(E, np.int64)
+    for e in range(E):
+        t = e // I
+        d = (int(keys[e]) >> shift) & 63
+        a = pad33(t) + (d & 31) * col_stride
+        hi = d // 32
+        rank = ((int(ctr[a]) >> (16 * hi)) & 0xFFFF) + (low_total if hi else 0) + local[e]
+        out_k[rank] = keys[e]
+        out_i[rank] = idxs[e]
+    return out_k, out_i
+
+
+@pytest.mark.parametrize("T,I,E,bits", [(32, 4, 128, 12), (32, 4, 77, 18), (64, 3, 190, 28), (32, 8, 256, 6)])
+def test_block_radix_rank_model_is_a_stable_sort(T, I, E, bits):
+    rng = np.random.default_rng(E + bits)
+    keys = rng.integers(0, 1 << bits, E).astype(np.uint64)
+    keys[::7] = keys[0]  # ties: order must stay the input order
+    idxs = np.arange(E)
+    k, i = keys.copy(), idxs.copy()
+    for p in range((bits + RS_DBITS - 1) // RS_DBITS):
+        k, i = block_radix_pass(k, i, T, I, p * RS_DBITS)
+    order = np.argsort(keys, kind="stable")
+    assert (k == keys[order]).all() and (i == idxs[order]).all()
+
+
+@pytest.mark.parametrize("I", [16, 24])
+def test_blocked_reads_and_raking_are_bank_conflict_free(I):
+    lanes = np.arange(32)
+    for i in range(I):  # a warp's lanes reading their i-th of I consecutive entries
+        banks = [pad33(int(t) * I + i) % 32 for t in lanes]
+        # 16 entries per lane: one bank per lane; 24: at most two lanes share a bank
+        assert max(np.bincount(banks, minlength=32)) <= (1 if I == 16 else 2)
+    for j in range(RS_WORDS):  # raking: lane t reads word j of its own segment
+        assert len({(33 * int(t) + j) % 32 for t in lanes}) == 32
