@@ -48,12 +48,43 @@ __global__ void lock_make_keys(const uint32_t *__restrict__ rows, const uint32_t
 // some key is greater than its successor (not sorted), stats[3] = 1 if some
 // row is (rows not grouped), stats[4] = 1 if some key is not below its
 // successor (not strictly increasing: duplicates or unsorted).
+// Runs of more than GAP_LONG row offsets with one value (empty rows) are
+// listed for offsets_fill_gaps (up to GAP_SLOTS of them) rather than written
+// by one thread.
+constexpr uint64_t GAP_LONG = 4096;
+constexpr unsigned GAP_SLOTS = 1024;
+
+struct RowGap {
+    uint64_t lo, hi, pos;
+};
+
+// off[r] = pos for rows r in [lo, hi), hi clamped to n_rows + 1.
+__device__ __forceinline__ void write_row_starts(uint64_t *__restrict__ off, uint64_t n_rows, uint64_t lo,
+                                                 uint64_t hi, uint64_t pos, RowGap *__restrict__ gaps,
+                                                 unsigned *__restrict__ n_gaps) {
+    hi = min(hi, n_rows + 1);
+    if (lo >= hi) return;
+    if (hi - lo > GAP_LONG) {
+        const unsigned slot = atomicAdd(n_gaps, 1u);
+        if (slot < GAP_SLOTS) {
+            gaps[slot] = {lo, hi, pos};
+            return;
+        }
+    }
+    for (uint64_t r = lo; r < hi; ++r) off[r] = pos;
+}
+
+// With off: also the row offsets the inserts would have if their rows are
+// grouped (each step r1 < r2 between neighbours i, i + 1 starts rows
+// r1 + 1 .. r2 at i + 1), written as the rows stream past; meaningless
+// unless stats[3] stays 0, and every write inside off[0..n_rows].
 // VEC: rows and cols 16-byte aligned; each thread reads 4 rows and 4
 // columns per step in two 16-byte loads (the successor of its last pair
 // comes from the next lane, or one more load at the warp's edge).
 template <bool VEC>
 __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols, uint64_t m,
-                             int cbits, unsigned *__restrict__ stats) {
+                             int cbits, unsigned *__restrict__ stats, uint64_t n_rows, uint64_t *__restrict__ off,
+                             RowGap *__restrict__ gaps, unsigned *__restrict__ n_gaps) {
     unsigned mr = 0, mc = 0;
     bool d = false, g = false, e = false;
     if constexpr (VEC) {
@@ -86,8 +117,14 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
                         d |= k1 > k2;
                         e |= k1 >= k2;
                         g |= rr[k] > rr[k + 1];
+                        if (off && rr[k] < rr[k + 1])
+                            write_row_starts(off, n_rows, (uint64_t)rr[k] + 1, (uint64_t)rr[k + 1] + 1, 4 * q + k + 1,
+                                             gaps, n_gaps);
                     }
                 }
+                if (off && q == 0) write_row_starts(off, n_rows, 0, (uint64_t)rr[0] + 1, 0, gaps, n_gaps);
+                if (off && !have_next)  // 4 q + 3 is the last insert
+                    write_row_starts(off, n_rows, (uint64_t)rr[3] + 1, n_rows + 1, m, gaps, n_gaps);
             }
         }
     }
@@ -97,12 +134,16 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
         const uint64_t k = ((uint64_t)r << cbits) | c;
         mr = max(mr, r);
         mc = max(mc, c);
+        if (off && i == 0) write_row_starts(off, n_rows, 0, (uint64_t)r + 1, 0, gaps, n_gaps);
         if (i + 1 < m) {
             const uint32_t r2 = rows[i + 1];
             const uint64_t k2 = ((uint64_t)r2 << cbits) | cols[i + 1];
             d |= k > k2;
             e |= k >= k2;
             g |= r > r2;
+            if (off && r < r2) write_row_starts(off, n_rows, (uint64_t)r + 1, (uint64_t)r2 + 1, i + 1, gaps, n_gaps);
+        } else if (off) {
+            write_row_starts(off, n_rows, (uint64_t)r + 1, n_rows + 1, m, gaps, n_gaps);
         }
     }
 #pragma unroll
@@ -145,12 +186,32 @@ __global__ void first_grouped_compact(const uint32_t *__restrict__ rows, const u
                                       const uint64_t *__restrict__ off, const uint32_t *__restrict__ scols,
                                       const double *__restrict__ svals, uint64_t m, uint32_t *__restrict__ ocols,
                                       double *__restrict__ ovals) {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t r = rows[e];
-        const uint64_t k = e - s_off[r], o0 = off[r];
-        if (k < off[r + 1] - o0) {
-            ocols[o0 + k] = scols[e];
-            ovals[o0 + k] = svals[e];
+    // four positions per thread, their loads issued together: the row, the
+    // entry and then the row's offsets are a chain of dependent loads
+    constexpr int U = 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t e0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e0 < m; e0 += U * stride) {
+        uint32_t r[U], c[U];
+        double v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t e = e0 + u * stride;
+            if (e < m) {
+                r[u] = rows[e];
+                c[u] = scols[e];
+                v[u] = svals[e];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t e = e0 + u * stride;
+            if (e < m) {
+                const uint64_t k = e - s_off[r[u]], o0 = off[r[u]];
+                if (k < off[r[u] + 1] - o0) {
+                    ocols[o0 + k] = c[u];
+                    ovals[o0 + k] = v[u];
+                }
+            }
         }
     }
 }
@@ -221,12 +282,6 @@ __global__ void lock_gather_delta(const uint64_t *__restrict__ keys, const uint3
 // over the grid, and written by their thread once the list is full. A
 // decreasing step (never in the sorted input) writes nothing, so every write
 // stays inside [0, n_rows].
-constexpr uint64_t GAP_LONG = 4096;
-constexpr unsigned GAP_SLOTS = 1024;
-
-struct RowGap {
-    uint64_t lo, hi, pos;
-};
 
 constexpr int OFF_T = 256, OFF_E = 8, OFF_TILE = OFF_T * OFF_E;  // positions per block step
 
@@ -611,6 +666,7 @@ first_keep_gather(const uint64_t *__restrict__ keys, const uint32_t *__restrict_
 struct Prepared {
     unsigned unsorted = 1, ungrouped = 1, not_strict = 1;
     bool ready = false;
+    DevBuf s_off;  // first lock: the staged rows' offsets (valid when !ungrouped), csr_off_elems(n_rows)
 };
 
 int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, uint64_t n_rows, uint64_t n_cols,
@@ -716,8 +772,12 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
                                            zero.as<unsigned>());
         SPG_LAUNCH_CHECK();
         // the offsets go out before the zero check comes back: one host sync
-        SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
-        SPG_TRY(launch_row_offsets(c, rows, m, n, new_off.as<uint64_t>(), s));
+        if (pre->s_off.ptr) {
+            new_off = std::move(pre->s_off);
+        } else {
+            SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
+            SPG_TRY(launch_row_offsets(c, rows, m, n, new_off.as<uint64_t>(), s));
+        }
         unsigned hz = 1;
         SPG_CUDA_TRY(cudaMemcpyAsync(&hz, zero.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_TRY(c->phase_sync(s));
@@ -743,8 +803,12 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         // pass, in place at the row's input positions; a scan of the kept
         // counts gives the offsets, and entries move only if some were dropped.
         DevBuf s_off, kept, scols, svals;
-        SPG_TRY(s_off.alloc((n + 1) * sizeof(uint64_t), s));
-        SPG_TRY(launch_row_offsets(c, rows, m, n, s_off.as<uint64_t>(), s));
+        if (pre->s_off.ptr) {
+            s_off = std::move(pre->s_off);
+        } else {
+            SPG_TRY(s_off.alloc((n + 1) * sizeof(uint64_t), s));
+            SPG_TRY(launch_row_offsets(c, rows, m, n, s_off.as<uint64_t>(), s));
+        }
         SPG_TRY(kept.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
         SPG_TRY(scols.alloc(csr_alloc_elems(m) * sizeof(uint32_t), s));
         SPG_TRY(svals.alloc(csr_alloc_elems(m) * sizeof(double), s));
@@ -827,17 +891,29 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     // in order.
     Prepared pre;
     if (m) {
+        // [0..4] stats, [5] gap count, then the gap list (first lock)
         DevBuf stats;
-        SPG_TRY(stats.alloc(5 * sizeof(unsigned), s));
-        SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 5 * sizeof(unsigned), s));
+        const size_t gap_at = 8 * sizeof(unsigned);
+        SPG_TRY(stats.alloc(gap_at + GAP_SLOTS * sizeof(RowGap), s));
+        SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 6 * sizeof(unsigned), s));
+        unsigned *n_gaps = stats.as<unsigned>() + 5;
+        RowGap *gaps = reinterpret_cast<RowGap *>(stats.as<char>() + gap_at);
+        uint64_t *off = nullptr;
+        if (!A->built) {  // the first lock's row offsets come with the check
+            SPG_TRY(pre.s_off.alloc(csr_off_elems(A->n_rows) * sizeof(uint64_t), s));
+            off = pre.s_off.as<uint64_t>();
+        }
         if (((uintptr_t)rows | (uintptr_t)cols) % 16 == 0)
             lock_prepare<true><<<grid_for((m + 3) / 4, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
-                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>());
+                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>(), A->n_rows, off, gaps, n_gaps);
         else
-            lock_prepare<false><<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(rows, cols, m,
-                                                                                       bits_for(A->n_cols),
-                                                                                       stats.as<unsigned>());
+            lock_prepare<false><<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
+                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>(), A->n_rows, off, gaps, n_gaps);
         SPG_LAUNCH_CHECK();
+        if (off) {
+            offsets_fill_gaps<<<c->n_sms * 4, LB, 0, s>>>(gaps, n_gaps, off);
+            SPG_LAUNCH_CHECK();
+        }
         unsigned h[5] = {0u, 0u, 1u, 1u, 1u};
         SPG_CUDA_TRY(cudaMemcpyAsync(h, stats.ptr, 5 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_TRY(c->phase_sync(s));
@@ -851,6 +927,7 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
         pre.ungrouped = h[3];
         pre.not_strict = h[4];
         pre.ready = true;
+        if (pre.ungrouped) pre.s_off.release();
     }
     const uint64_t n = A->n_rows;
     const bool has_old = A->built;
