@@ -384,10 +384,10 @@ enum spg_spgemm_variant {
                                     (row, column), left-to-right run sums */
     SPG_SPGEMM_WARPSORT_64 = 2,  /* tiles of consecutive rows: a warp sorts each row's
                                     (column, product) pairs in registers (bitonic, rows of
-                                    <= 64 products; heavier rows expand-sort-compress), a
-                                    thread per row sums the runs, each tile writes C in
-                                    place after an ordered scan of the tiles' counts;
-                                    tiles of <= 1024 products */
+                                    <= 64 products; heavier rows expand-sort-compress) and
+                                    sums each run of equal columns in the run's first lane,
+                                    each tile writes C in place after an ordered scan of the
+                                    tiles' counts; tiles of <= 1024 products */
     SPG_SPGEMM_WARPSORT_128 = 3, /* the same for rows of <= 128 products, 2048-product tiles */
     SPG_SPGEMM_WARPSORT_256 = 4, /* the same for rows of <= 256 products, 4096-product tiles */
     SPG_SPGEMM_N_VARIANTS = 5
