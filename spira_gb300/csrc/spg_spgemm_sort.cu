@@ -71,6 +71,7 @@ struct SgsArgs {
     unsigned int *status;
     uint32_t tpb;                // product budget of a tile (shared memory)
     long long wait_cycles;       // bound of every look-back wait
+    uint64_t fixed_rows;         // nonzero: no heavy rows; tile t = rows [t F, t F + F), pofs = raw counts
 };
 
 __device__ __forceinline__ bool sgs_heavy(const uint64_t *aoff, const uint64_t *pofs, uint64_t i, uint32_t hb) {
@@ -78,27 +79,52 @@ __device__ __forceinline__ bool sgs_heavy(const uint64_t *aoff, const uint64_t *
 }
 
 // Products per row (pofs[i]) and the products of heavy rows only (hp[i], 0
-// for the others); entry m of both is 0; *n_heavy counts heavy rows.
-__global__ void sgs_products(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols,
-                             const uint64_t *__restrict__ boff, uint64_t m, uint32_t hb, uint64_t *__restrict__ pofs,
-                             uint64_t *__restrict__ hp, unsigned long long *__restrict__ n_heavy) {
+// for the others); entry m of both is 0; *n_heavy counts heavy rows and
+// *p_total sums the products (one atomic per block each).
+__global__ void __launch_bounds__(256) sgs_products(const uint64_t *__restrict__ aoff,
+                                                    const uint32_t *__restrict__ acols,
+                                                    const uint64_t *__restrict__ boff, uint64_t m, uint32_t hb,
+                                                    uint64_t *__restrict__ pofs, uint64_t *__restrict__ hp,
+                                                    unsigned long long *__restrict__ n_heavy,
+                                                    unsigned long long *__restrict__ p_total) {
+    __shared__ unsigned long long s_p[8], s_h[8];
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i > m) return;
-    if (i == m) {
+    uint64_t p = 0;
+    bool heavy = false;
+    if (i < m) {
+        const uint64_t a0 = aoff[i], a1 = aoff[i + 1];
+        for (uint64_t ka = a0; ka < a1; ++ka) {
+            const uint32_t k = acols[ka];
+            p += boff[k + 1] - boff[k];
+        }
+        heavy = p > hb || a1 - a0 > hb;
+        pofs[i] = p;
+        hp[i] = heavy ? p : 0;
+    } else if (i == m) {
         pofs[m] = 0;
         hp[m] = 0;
-        return;
     }
-    const uint64_t a0 = aoff[i], a1 = aoff[i + 1];
-    uint64_t p = 0;
-    for (uint64_t ka = a0; ka < a1; ++ka) {
-        const uint32_t k = acols[ka];
-        p += boff[k + 1] - boff[k];
+    unsigned long long sp = p, sh = heavy ? 1ull : 0ull;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        sp += __shfl_xor_sync(0xffffffffu, sp, o);
+        sh += __shfl_xor_sync(0xffffffffu, sh, o);
     }
-    const bool heavy = p > hb || a1 - a0 > hb;
-    pofs[i] = p;
-    hp[i] = heavy ? p : 0;
-    if (heavy) atomicAdd(n_heavy, 1ull);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_p[warp] = sp;
+        s_h[warp] = sh;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bp = 0, bh = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            bp += s_p[w];
+            bh += s_h[w];
+        }
+        if (bp) atomicAdd(p_total, bp);
+        if (bh) atomicAdd(n_heavy, bh);
+    }
 }
 
 // Row i starts a tile: every SGS_RB-th row, heavy rows and the rows after
@@ -323,17 +349,42 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
     __shared__ uint32_t sh_reg[SGS_RB];
     __shared__ uint32_t sh_excl[SGS_RB + 1];
     __shared__ uint32_t sh_kept[SGS_RB];
+    __shared__ uint32_t sh_P[32];  // fixed tiles: products of each row
     __shared__ uint32_t sh_wsum[SGS_WARPS];
     __shared__ int sh_ok;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) sh_tile = atomicAdd(g.ticket, 1ull);
     __syncthreads();
     const uint64_t t = sh_tile;
-    if (t >= *g.n_tiles) return;
-    const uint64_t row0 = g.tile_start[t], row1 = g.tile_start[t + 1];
+    const bool fixed = g.fixed_rows != 0;
+    if (t >= (fixed ? (g.m + g.fixed_rows - 1) / g.fixed_rows : *g.n_tiles)) return;
+    uint64_t row0, row1, p0 = 0;
+    if (fixed) {
+        row0 = t * g.fixed_rows;
+        row1 = min(g.m, row0 + g.fixed_rows);
+    } else {
+        row0 = g.tile_start[t];
+        row1 = g.tile_start[t + 1];
+        p0 = g.pofs[row0];
+    }
     const uint32_t nr = (uint32_t)(row1 - row0);
-    const uint64_t p0 = g.pofs[row0];
-    const bool heavy_tile = nr == 1 && sgs_heavy(g.aoff, g.pofs, row0, HB);
+    const bool heavy_tile = !fixed && nr == 1 && sgs_heavy(g.aoff, g.pofs, row0, HB);
+    if (fixed) {  // the rows' regions: an exclusive scan of their products (at most 32 rows)
+        if (warp == 0) {
+            const uint32_t P = (uint32_t)lane < nr ? (uint32_t)g.pofs[row0 + lane] : 0u;
+            uint32_t inc = P;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if ((uint32_t)lane < nr) {
+                sh_P[lane] = P;
+                sh_reg[lane] = inc - P + (uint32_t)lane;
+            }
+        }
+        __syncthreads();
+    }
     uint32_t cnt = 0;
     if (!heavy_tile) {
         double *w_a = w_a_all + warp * HB;
@@ -341,8 +392,8 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
         uint16_t *w_own = w_own_all + warp * HB;
         for (uint32_t j = warp; j < nr; j += SGS_WARPS) {
             const uint64_t i = row0 + j;
-            const uint32_t reg = (uint32_t)(g.pofs[i] - p0) + j;
-            const uint32_t P = (uint32_t)(g.pofs[i + 1] - g.pofs[i]);
+            const uint32_t reg = fixed ? sh_reg[j] : (uint32_t)(g.pofs[i] - p0) + j;
+            const uint32_t P = fixed ? sh_P[j] : (uint32_t)(g.pofs[i + 1] - g.pofs[i]);
             uint32_t kept = 0;
             if (P == 0) kept = 0;
             else if (P <= 32) kept = sgs_row<1, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
@@ -351,6 +402,7 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
                 if (P <= 128) kept = sgs_row<4, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
                 else if constexpr (HB >= 256) kept = sgs_row<8, SB, K>(g, i, reg, P, s_col, s_prod, w_a, w_b, w_own, lane);
             }
+            __syncwarp();
             if (lane == 0) {
                 sh_kept[j] = kept;
                 sh_reg[j] = reg;
@@ -464,15 +516,18 @@ int spgemm_warpsort(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cu
     SPG_TRY(hp.alloc((m + 1) * sizeof(uint64_t), s));
     SPG_TRY(nh_dev.alloc(3 * sizeof(uint64_t), s));
     SPG_CUDA_TRY(cudaMemsetAsync(nh_dev.ptr, 0, 3 * sizeof(uint64_t), s));
+    unsigned long long *nh = reinterpret_cast<unsigned long long *>(nh_dev.as<uint64_t>());
     sgs_products<<<grid_for(m + 1, 256), 256, 0, s>>>(A->d_off(), A->d_cols(), B->d_off(), m, cf.hb,
-                                                     pofs.as<uint64_t>(), hp.as<uint64_t>(),
-                                                     reinterpret_cast<unsigned long long *>(nh_dev.as<uint64_t>()));
+                                                     pofs.as<uint64_t>(), hp.as<uint64_t>(), nh, nh + 1);
     SPG_LAUNCH_CHECK();
-    SPG_TRY(exclusive_scan_u64(c, pofs.as<uint64_t>(), m + 1, nh_dev.as<uint64_t>() + 1, s));
     uint64_t h[3] = {0, 0, 0};  // heavy rows, products, heavy products
     SPG_CUDA_TRY(cudaMemcpyAsync(h, nh_dev.ptr, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     SPG_TRY(c->phase_sync(s));
-    if (h[0]) {  // heavy rows' product offsets only when there are heavy rows
+    // No heavy row: tiles of F consecutive rows (F rows of at most hb products fill a tile's budget
+    // at most), their regions scanned inside the kernel: no scan, no tile plan.
+    const uint64_t F = h[0] ? 0 : cf.tpb / cf.hb;
+    if (h[0]) {  // heavy rows: the row offsets for the tile plan, and the heavy rows' products
+        SPG_TRY(exclusive_scan_u64(c, pofs.as<uint64_t>(), m + 1, nh_dev.as<uint64_t>() + 1, s));
         SPG_TRY(exclusive_scan_u64(c, hp.as<uint64_t>(), m + 1, nh_dev.as<uint64_t>() + 2, s));
         SPG_CUDA_TRY(cudaMemcpyAsync(h + 2, nh_dev.as<uint64_t>() + 2, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
         SPG_TRY(c->phase_sync(s));
@@ -507,22 +562,24 @@ int spgemm_warpsort(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cu
     hp.release();
     // tiles
     const uint64_t W = cf.tpb - cf.hb;
-    const uint64_t t_max = (m + SGS_RB - 1) / SGS_RB + P / W + 2 * n_heavy + 3;
+    const uint64_t t_max = F ? (m + F - 1) / F : (m + SGS_RB - 1) / SGS_RB + P / W + 2 * n_heavy + 3;
     DevBuf flag, tile_start, tstate, ticket;
-    SPG_TRY(flag.alloc((m + 1) * sizeof(uint64_t), s));
-    SPG_TRY(tile_start.alloc((t_max + 1) * sizeof(uint64_t), s));
     SPG_TRY(tstate.alloc(t_max * sizeof(unsigned long long), s));
     SPG_TRY(ticket.alloc(2 * sizeof(uint64_t), s));  // [0] ticket counter, [1] tile count
     SPG_CUDA_TRY(cudaMemsetAsync(tstate.ptr, 0, t_max * sizeof(unsigned long long), s));
     SPG_CUDA_TRY(cudaMemsetAsync(ticket.ptr, 0, 2 * sizeof(uint64_t), s));
-    sgs_tile_flags<<<grid_for(m, 256, gmax), 256, 0, s>>>(A->d_off(), pofs.as<uint64_t>(), m, cf.hb, W,
-                                                         flag.as<uint64_t>());
-    SPG_LAUNCH_CHECK();
-    SPG_TRY(exclusive_scan_u64(c, flag.as<uint64_t>(), m, ticket.as<uint64_t>() + 1, s));
-    sgs_tile_scatter<<<grid_for(m, 256, gmax), 256, 0, s>>>(A->d_off(), pofs.as<uint64_t>(), m, cf.hb, W,
-                                                           flag.as<uint64_t>(), ticket.as<uint64_t>() + 1,
-                                                           tile_start.as<uint64_t>());
-    SPG_LAUNCH_CHECK();
+    if (!F) {
+        SPG_TRY(flag.alloc((m + 1) * sizeof(uint64_t), s));
+        SPG_TRY(tile_start.alloc((t_max + 1) * sizeof(uint64_t), s));
+        sgs_tile_flags<<<grid_for(m, 256, gmax), 256, 0, s>>>(A->d_off(), pofs.as<uint64_t>(), m, cf.hb, W,
+                                                             flag.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+        SPG_TRY(exclusive_scan_u64(c, flag.as<uint64_t>(), m, ticket.as<uint64_t>() + 1, s));
+        sgs_tile_scatter<<<grid_for(m, 256, gmax), 256, 0, s>>>(A->d_off(), pofs.as<uint64_t>(), m, cf.hb, W,
+                                                               flag.as<uint64_t>(), ticket.as<uint64_t>() + 1,
+                                                               tile_start.as<uint64_t>());
+        SPG_LAUNCH_CHECK();
+    }
     // C at the products' upper bound (kept entries <= products)
     SPG_TRY(cols.alloc(csr_alloc_elems(P) * sizeof(uint32_t), s));
     SPG_TRY(vals.alloc(csr_alloc_elems(P) * sizeof(double), s));
@@ -549,6 +606,7 @@ int spgemm_warpsort(Ctx *c, const Csr *A, const Csr *B, Csr *Cm, int variant, cu
     g.status = c->d_status;
     g.tpb = cf.tpb;
     g.wait_cycles = SGS_WAIT_CYCLES;
+    g.fixed_rows = F;
     const size_t smem = sgs_smem_bytes(cf);
     const unsigned grid = (unsigned)t_max;
     // keys: column << log2(hb) | slot, in 32 bits while the columns allow
