@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 SEG_MEDIUM, SEG_MAX_CBITS = 512, 26
-TS0, TS1, TS_MAX = 128 * 16, 256 * 16, 512 * 24
+TS0, TS1, TS_MAX = 128 * 16, 256 * 16, 768 * 16
 
 
 def seg_class(L: int) -> int:
