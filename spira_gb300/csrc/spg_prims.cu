@@ -429,7 +429,7 @@ int radix_sort_pairs_u64(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n,
 namespace {
 
 constexpr int SEG_MEDIUM = 512;   // rows of 33..SEG_MEDIUM entries: a warp each
-constexpr int TS0_T = 128, TS0_I = 16;   // rows up to 2048 entries
+constexpr int TS0_T = 128, TS0_I = 16;   // rows up to 2048 entries (256 x 8 measured 29 % slower)
 constexpr int TS1_T = 256, TS1_I = 16;   // rows up to 4096
 constexpr int TS2_T = 768, TS2_I = 16;   // rows up to TS_MAX
 constexpr int TS0 = TS0_T * TS0_I, TS1 = TS1_T * TS1_I, TS_MAX = TS2_T * TS2_I;
@@ -761,15 +761,15 @@ struct TileSmem {
     static constexpr int MAXE = T * I;
     static constexpr int NCTR = RS_WORDS * T;
     static constexpr bool VSTAGE = DEDUP && MAXE <= 4096;  // values staged in shared memory
-    union {
+    union {  // the counters live only inside a radix pass, the exchange arrays between passes
         uint32_t ctr[NCTR + NCTR / 32];  // counter word w of thread t at pad33(w T + t)
         struct {
             uint32_t key[MAXE + MAXE / 32];
             uint16_t idx[MAXE + MAXE / 32];  // row position; dedup mode: | IDX_ZERO if the value is zero
             uint32_t ex[MAXE + MAXE / 32 + 2];  // dedup mode: kept entries before each position
-            double val[VSTAGE ? MAXE : 1];      // dedup mode: values by row position
         } x;
     } u;
+    double val[VSTAGE ? MAXE : 1];  // dedup mode: values by row position, kept through every pass
     uint32_t wsum[T / 32];
 };
 
@@ -806,7 +806,7 @@ seg_tile_sort(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_
             if constexpr (DEDUP) {
                 const double v = o.in_vals[b + e];
                 if (is_zero(v)) ix |= IDX_ZERO;
-                if constexpr (Sm::VSTAGE) S.u.x.val[e] = v;
+                if constexpr (Sm::VSTAGE) S.val[e] = v;
             }
             S.u.x.idx[pad33(e)] = ix;
         }
@@ -959,7 +959,7 @@ seg_tile_sort(const uint32_t *__restrict__ cols, const uint64_t *__restrict__ s_
                 if (S.u.x.ex[pad33(q + 1)] != e0) {
                     const unsigned tp = S.u.x.idx[pad33(q)] & ~IDX_ZERO;
                     o.cols[b + e0] = S.u.x.key[pad33(q)];
-                    if constexpr (Sm::VSTAGE) o.vals[b + e0] = S.u.x.val[tp];
+                    if constexpr (Sm::VSTAGE) o.vals[b + e0] = S.val[tp];
                     else o.vals[b + e0] = o.in_vals[b + tp];
                 }
             }

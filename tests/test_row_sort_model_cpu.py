@@ -200,12 +200,12 @@ def test_block_radix_rank_model_is_a_stable_sort(T, I, E, bits):
     assert (k == keys[order]).all() and (i == idxs[order]).all()
 
 
-@pytest.mark.parametrize("I", [16, 24])
+@pytest.mark.parametrize("I", [8, 16, 24])
 def test_blocked_reads_and_raking_are_bank_conflict_free(I):
     lanes = np.arange(32)
     for i in range(I):  # a warp's lanes reading their i-th of I consecutive entries
         banks = [pad33(int(t) * I + i) % 32 for t in lanes]
-        # 16 entries per lane: one bank per lane; 24: at most two lanes share a bank
-        assert max(np.bincount(banks, minlength=32)) <= (1 if I == 16 else 2)
+        # 8 or 16 entries per lane (the kernels' sizes): one bank per lane; 24: two lanes at most
+        assert max(np.bincount(banks, minlength=32)) <= (1 if I in (8, 16) else 2)
     for j in range(RS_WORDS):  # raking: lane t reads word j of its own segment
         assert len({(33 * int(t) + j) % 32 for t in lanes}) == 32
