@@ -836,6 +836,7 @@ PROFILE_CASES = {
     "lock_zipf4m": (ZIPF_N, "lock"),
     "lock_laplacian2d": (GRID * GRID, "lock"),
     "relock_zipf1m": (1_000_000, "relock"),
+    "relock_laplacian2d": (GRID * GRID, "relock"),
     "batched256": (256, "batched"),  # the batched workload's first 256 matrices
     "transpose_laplacian3d": (100 ** 3, "transpose"),
     "spgemm_laplacian3d": (100 ** 3, "spgemm"),
@@ -885,11 +886,17 @@ def run_profile_op(ctx, case, n, kind, reps, variants=""):
         return
     if kind == "relock":
         import torch
-        r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
-        A = sg.Csr(ctx, n, n)
-        A.lock_device(r, c, v, m)
-        del r, c, v
-        dr, dc, dv = gen.relock_batch(n, n, A.nnz, seed=32)
+        if case == "relock_laplacian2d":  # the bench's 2a re-lock: 1 % new entries into 10 % of the rows
+            hr, hc, hv = gen.laplacian_2d(GRID)
+            A = sg.Csr(ctx, n, n)
+            A.lock(hr, hc, hv)
+            dr, dc, dv = gen.relock_batch(n, n, A.nnz, seed=21)
+        else:
+            r, c, v, m = gen_device.zipf_rows(ctx, n, seed=31)
+            A = sg.Csr(ctx, n, n)
+            A.lock_device(r, c, v, m)
+            del r, c, v
+            dr, dc, dv = gen.relock_batch(n, n, A.nnz, seed=32)
         d = (torch.from_numpy(dr.view(np.int32)).cuda(), torch.from_numpy(dc.view(np.int32)).cuda(),
              torch.from_numpy(dv).cuda())
         pristine = sg.Csr(ctx, n, n)

@@ -451,13 +451,40 @@ merge_write_old(const uint64_t *__restrict__ off, const uint32_t *__restrict__ c
             s_new[t] = new_off[rlo + t];
             s_doff[t] = doff[rlo + t];
         }
+        for (int t = threadIdx.x; t < MO_CHUNK; t += LB) s_row[t] = 0;
         __syncthreads();
-        // label the chunk's entries with their rows: warp per row
-        const int lane = threadIdx.x & 31;
-        for (int rr = threadIdx.x >> 5; rr <= (int)(rhi - rlo); rr += LB / 32) {
-            const uint64_t b = max(s_off[rr], k0), e = min(s_off[rr + 1], k1);
-            for (uint64_t k = b + lane; k < e; k += 32) s_row[k - k0] = (uint16_t)rr;
+        // label the chunk's entries with their rows: every non-empty row starting
+        // inside the chunk marks its first entry, then an inclusive max-scan
+        // carries each mark over the row's entries (a warp per row left most
+        // lanes idle on short rows)
+        for (uint64_t rr = threadIdx.x + 1; rr <= rhi - rlo; rr += LB) {
+            const uint64_t b = s_off[rr];
+            if (b >= k0 && b < k1 && s_off[rr + 1] > b) s_row[b - k0] = (uint16_t)rr;
         }
+        __syncthreads();
+        constexpr int PT = MO_CHUNK / LB;  // positions per thread, blocked
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint16_t lab[PT];
+        uint16_t run = 0;
+#pragma unroll
+        for (int i = 0; i < PT; ++i) {
+            run = max(run, s_row[threadIdx.x * PT + i]);
+            lab[i] = run;
+        }
+        uint16_t inc = run;  // inclusive max over threads 0..t
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint16_t v = (uint16_t)__shfl_up_sync(0xffffffffu, (unsigned)inc, o);
+            if (lane >= o) inc = max(inc, v);
+        }
+        __shared__ uint16_t s_wmax[LB / 32];
+        if (lane == 31) s_wmax[warp] = inc;
+        __syncthreads();
+        uint16_t carry = (uint16_t)__shfl_up_sync(0xffffffffu, (unsigned)inc, 1);
+        if (lane == 0) carry = 0;
+        for (int w = 0; w < warp; ++w) carry = max(carry, s_wmax[w]);
+#pragma unroll
+        for (int i = 0; i < PT; ++i) s_row[threadIdx.x * PT + i] = max(carry, lab[i]);
     }
     __syncthreads();
     // consecutive threads on consecutive entries (coalesced); a thread's
