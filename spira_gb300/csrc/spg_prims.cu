@@ -197,7 +197,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 template <int RS_ITERS>
 __global__ void __launch_bounds__(RS_BLOCK)
 radix_upsweep(const uint64_t *__restrict__ keys, uint64_t n, int shift, unsigned n_tiles,
-              unsigned *__restrict__ hist /* [RADIX][n_tiles] */) {
+              unsigned long long *__restrict__ hist /* [RADIX][n_tiles], scanned in place next */) {
     constexpr int RS_TILE = RS_BLOCK * RS_ITERS;
     __shared__ unsigned cnt[RS_WARPS][RS_RADIX];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -331,12 +331,6 @@ radix_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__
     }
 }
 
-__global__ void scan_u32_to_u64_copy(const unsigned *in, unsigned long long *out, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        out[i] = in[i];
-}
-
 }  // namespace
 
 namespace {
@@ -346,10 +340,9 @@ int radix_sort_impl(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n, int 
     constexpr int RS_TILE = RS_BLOCK * RS_ITERS;
     const unsigned n_tiles = (unsigned)((n + RS_TILE - 1) / RS_TILE);
     const uint64_t hist_n = (uint64_t)RS_RADIX * n_tiles;
-    DevBuf kalt, valt, hist, offs;
+    DevBuf kalt, valt, offs;
     SPG_TRY(kalt.alloc(n * sizeof(uint64_t), s));
     SPG_TRY(valt.alloc(n * sizeof(uint32_t), s));
-    SPG_TRY(hist.alloc(hist_n * sizeof(unsigned), s));
     SPG_TRY(offs.alloc(hist_n * sizeof(unsigned long long), s));
     uint64_t *kin = d_keys, *kout = kalt.as<uint64_t>();
     uint32_t *vin = d_vals, *vout = valt.as<uint32_t>();
@@ -359,10 +352,7 @@ int radix_sort_impl(Ctx *c, uint64_t *d_keys, uint32_t *d_vals, uint64_t n, int 
                                       (int)smem));
     for (int p = 0; p < passes; ++p) {
         const int shift = p * 8;
-        radix_upsweep<RS_ITERS><<<n_tiles, RS_BLOCK, 0, s>>>(kin, n, shift, n_tiles, hist.as<unsigned>());
-        SPG_LAUNCH_CHECK();
-        scan_u32_to_u64_copy<<<grid_for(hist_n, 256, 4096), 256, 0, s>>>(
-            hist.as<unsigned>(), offs.as<unsigned long long>(), hist_n);
+        radix_upsweep<RS_ITERS><<<n_tiles, RS_BLOCK, 0, s>>>(kin, n, shift, n_tiles, offs.as<unsigned long long>());
         SPG_LAUNCH_CHECK();
         SPG_TRY(exclusive_scan_u64(c, offs.as<uint64_t>(), hist_n, nullptr, s));
         radix_scatter<RS_ITERS><<<n_tiles, RS_BLOCK, smem, s>>>(kin, vin, kout, vout, n, shift, n_tiles,
