@@ -417,7 +417,10 @@ int spg_spgemm_selector_load(spg_ctx *ctx, const float *blob, uint64_t n_floats,
 int spg_spgemm_selector_predict(spg_ctx *ctx, const float *d_features, uint32_t B, float *d_out, void *stream);
 /* SPG_SPGEMM_AUTO's policy: SPG_POLICY_SELECTOR (the selector if loaded, else
  * the autotuner), SPG_POLICY_AUTOTUNE, SPG_POLICY_FIXED (SPG_SPGEMM_WARPSORT_128
- * without measuring). The choice is cached per (A, B) until either changes. */
+ * without measuring). The selector never picks a WARPSORT variant that a
+ * smaller one does the same work for: when every row of A * B has at most 64
+ * products and A entries, _128 and _256 are skipped; up to 128, _256. The
+ * choice is cached per (A, B) until either changes. */
 int spg_set_spgemm_policy(spg_ctx *ctx, int policy);
 
 #ifdef __cplusplus

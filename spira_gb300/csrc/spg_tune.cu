@@ -141,7 +141,8 @@ __global__ void feat_rows(const uint64_t *__restrict__ off, const uint32_t *__re
 // SpGEMM features of A * B. acc layout (doubles): [0..31] histogram of the
 // products per row (bin 0: none, else 1 + floor(log2 p), capped at 31),
 // 32 sum p, 33 sum p^2, 34 max p, 35 sum of |col / n_cols - row / m| over the
-// first and last entry of every 16th non-empty row of A, 36 their number.
+// first and last entry of every 16th non-empty row of A, 36 their number,
+// 37 the longest row of A (entries).
 // The spread tells local patterns (banded, block-diagonal, stencils: a row's
 // products fall on few columns, the output is several times smaller than
 // the products) from scattered ones (products mostly distinct), which the
@@ -150,10 +151,10 @@ __global__ void feat_rows(const uint64_t *__restrict__ off, const uint32_t *__re
 __global__ void feat_gemm_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ acols,
                                const uint64_t *__restrict__ boff, uint64_t m, uint64_t n_cols_a,
                                double *__restrict__ acc) {
-    __shared__ double s[37];
-    for (int i = threadIdx.x; i < 37; i += blockDim.x) s[i] = 0.0;
+    __shared__ double s[38];
+    for (int i = threadIdx.x; i < 38; i += blockDim.x) s[i] = 0.0;
     __syncthreads();
-    double sp = 0, sp2 = 0, mx = 0, spread = 0, cnt = 0;
+    double sp = 0, sp2 = 0, mx = 0, spread = 0, cnt = 0, mxa = 0;
     for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < m; r += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t a0 = aoff[r], a1 = aoff[r + 1];
         uint64_t p = 0;
@@ -170,6 +171,7 @@ __global__ void feat_gemm_rows(const uint64_t *__restrict__ aoff, const uint32_t
         sp += (double)p;
         sp2 += (double)p * (double)p;
         mx = fmax(mx, (double)p);
+        mxa = fmax(mxa, (double)(a1 - a0));
         if ((r & 15) == 0 && a1 > a0) {
             const double rr = (double)r / (double)m;
             spread += fabs((double)acols[a0] / (double)n_cols_a - rr) + fabs((double)acols[a1 - 1] / (double)n_cols_a - rr);
@@ -181,9 +183,10 @@ __global__ void feat_gemm_rows(const uint64_t *__restrict__ aoff, const uint32_t
     atomicMax(reinterpret_cast<unsigned long long *>(&s[34]), __double_as_longlong(mx));
     atomicAdd(&s[35], spread);
     atomicAdd(&s[36], cnt);
+    atomicMax(reinterpret_cast<unsigned long long *>(&s[37]), __double_as_longlong(mxa));
     __syncthreads();
-    for (int i = threadIdx.x; i < 37; i += blockDim.x) {
-        if (i == 34) atomicMax(reinterpret_cast<unsigned long long *>(&acc[34]), __double_as_longlong(s[34]));
+    for (int i = threadIdx.x; i < 38; i += blockDim.x) {
+        if (i == 34 || i == 37) atomicMax(reinterpret_cast<unsigned long long *>(&acc[i]), __double_as_longlong(s[i]));
         else atomicAdd(&acc[i], s[i]);
     }
 }
@@ -494,19 +497,23 @@ int selector_load_default(Ctx *c) {
 }
 
 // ---------------------------------------------------------------- SpGEMM choice
-int spgemm_features(Ctx *c, const Csr *A, const Csr *B, float *f) {
+// max_products / max_a (may be null): the most products and A entries of any row.
+int spgemm_features(Ctx *c, const Csr *A, const Csr *B, float *f, double *max_products = nullptr,
+                    double *max_a = nullptr) {
     cudaStream_t s = c->stream;
     DevBuf acc;
-    SPG_TRY(acc.alloc(37 * sizeof(double), s));
-    SPG_CUDA_TRY(cudaMemsetAsync(acc.ptr, 0, 37 * sizeof(double), s));
+    SPG_TRY(acc.alloc(38 * sizeof(double), s));
+    SPG_CUDA_TRY(cudaMemsetAsync(acc.ptr, 0, 38 * sizeof(double), s));
     if (A->n_rows) {
         feat_gemm_rows<<<grid_for(A->n_rows, 256, (unsigned)c->n_sms * 8), 256, 0, s>>>(
             A->d_off(), A->d_cols(), B->d_off(), A->n_rows, A->n_cols ? A->n_cols : 1, acc.as<double>());
         SPG_LAUNCH_CHECK();
     }
-    double h[37];
+    double h[38];
     SPG_CUDA_TRY(cudaMemcpyAsync(h, acc.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
     SPG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (max_products) *max_products = h[34];
+    if (max_a) *max_a = h[37];
     const double m = (double)(A->n_rows ? A->n_rows : 1);
     for (int i = 0; i < 32; ++i) f[i] = (float)(h[i] / m);
     const double mean = h[32] / m;
@@ -558,21 +565,27 @@ int spgemm_resolve_auto(Ctx *c, const Csr *A, const Csr *B, int *variant) {
         return SPG_OK;
     }
     int v = SPG_SPGEMM_WARPSORT_128;
-    if (c->spgemm_policy == SPG_POLICY_SELECTOR && c->gemm_model_k > 0) {
+    if (c->spgemm_policy == SPG_POLICY_SELECTOR && c->gemm_model_k == SPG_SPGEMM_N_VARIANTS) {
         float f[F];
-        SPG_TRY(spgemm_features(c, A, B, f));
+        double maxp = 0.0, maxa = 0.0;
+        SPG_TRY(spgemm_features(c, A, B, f, &maxp, &maxa));
         cudaStream_t s = c->stream;
-        DevBuf df, dout, db;
+        DevBuf df, dout;
         SPG_TRY(df.alloc(F * sizeof(float), s));
-        SPG_TRY(dout.alloc(c->gemm_model_k * sizeof(float), s));
-        SPG_TRY(db.alloc(sizeof(int), s));
+        SPG_TRY(dout.alloc(SPG_SPGEMM_N_VARIANTS * sizeof(float), s));
         SPG_CUDA_TRY(cudaMemcpyAsync(df.ptr, f, sizeof(f), cudaMemcpyHostToDevice, s));
         SPG_TRY(selector_predict_dev(c->gemm_model, c->gemm_model_k, df.as<float>(), 1, dout.as<float>(), s));
-        mlp_argmin<<<1, 32, 0, s>>>(dout.as<float>(), 1, c->gemm_model_k, db.as<int>());
-        SPG_LAUNCH_CHECK();
-        SPG_CUDA_TRY(cudaMemcpyAsync(&v, db.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        float sc[SPG_SPGEMM_N_VARIANTS];
+        SPG_CUDA_TRY(cudaMemcpyAsync(sc, dout.ptr, sizeof(sc), cudaMemcpyDeviceToHost, s));
         SPG_CUDA_TRY(cudaStreamSynchronize(s));
-        if (v < 0 || v >= SPG_SPGEMM_N_VARIANTS) v = SPG_SPGEMM_WARPSORT_128;
+        // Dominated by construction, never chosen: when every row has at most 64 products and 64 A
+        // entries, the WARPSORT variants for 128 and 256 do WARPSORT_64's work row for row with more
+        // shared memory per tile (fewer tiles resident); likewise 256 against 128 up to 128.
+        if (maxp <= 64.0 && maxa <= 64.0) sc[SPG_SPGEMM_WARPSORT_128] = sc[SPG_SPGEMM_WARPSORT_256] = INFINITY;
+        else if (maxp <= 128.0 && maxa <= 128.0) sc[SPG_SPGEMM_WARPSORT_256] = INFINITY;
+        v = 0;
+        for (int k = 1; k < SPG_SPGEMM_N_VARIANTS; ++k)
+            if (sc[k] < sc[v]) v = k;
     } else if (c->spgemm_policy != SPG_POLICY_FIXED) {
         SPG_TRY(spgemm_autotune(c, A, B, 3, nullptr, &v));
     }

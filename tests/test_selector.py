@@ -175,3 +175,20 @@ def test_shipped_selector_on_unseen_matrices(ctx, op, first, n, bound):
                     S.DEFAULT_SPMV if op == "spmv" else S.DEFAULT_SPGEMM)
     assert ev["total_time_ratio"] <= bound, ev
     assert ev["total_time_ratio"] < ev["default_total_time_ratio"], ev
+
+
+@pytest.mark.gpu
+def test_spgemm_selector_skips_dominated_variants(ctx):
+    """SPG_SPGEMM_AUTO with the shipped model never picks a WARPSORT variant
+    whose rows a smaller one takes with less shared memory: uniform rows of 8
+    (64 products per row) rule out _128 and _256, rows of 10 (up to 100) _256."""
+    import spira_gb300 as sg
+    from spira_gb300 import gen
+    for k, ruled_out in ((8, {sg.SPGEMM_VARIANTS["warpsort_128"], sg.SPGEMM_VARIANTS["warpsort_256"]}),
+                         (10, {sg.SPGEMM_VARIANTS["warpsort_256"]})):
+        n = 50_000
+        r, c, v = gen.uniform_rows(n, n, k, seed=77 + k)
+        A = sg.Csr(ctx, n, n)
+        A.lock(r, c, v)
+        assert A.spgemm_selected(A) not in ruled_out
+        A.close()
