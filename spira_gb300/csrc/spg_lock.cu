@@ -58,33 +58,15 @@ struct RowGap {
     uint64_t lo, hi, pos;
 };
 
-// off[r] = pos for rows r in [lo, hi), hi clamped to n_rows + 1.
-__device__ __forceinline__ void write_row_starts(uint64_t *__restrict__ off, uint64_t n_rows, uint64_t lo,
-                                                 uint64_t hi, uint64_t pos, RowGap *__restrict__ gaps,
-                                                 unsigned *__restrict__ n_gaps) {
-    hi = min(hi, n_rows + 1);
-    if (lo >= hi) return;
-    if (hi - lo > GAP_LONG) {
-        const unsigned slot = atomicAdd(n_gaps, 1u);
-        if (slot < GAP_SLOTS) {
-            gaps[slot] = {lo, hi, pos};
-            return;
-        }
-    }
-    for (uint64_t r = lo; r < hi; ++r) off[r] = pos;
-}
-
-// With off: also the row offsets the inserts would have if their rows are
-// grouped (each step r1 < r2 between neighbours i, i + 1 starts rows
-// r1 + 1 .. r2 at i + 1), written as the rows stream past; meaningless
-// unless stats[3] stays 0, and every write inside off[0..n_rows].
+// (Writing the staged rows' offsets in this pass as well, speculatively, was
+// tried and removed: on inserts in random order every rising step between
+// neighbours would write its whole gap of rows, ~m n / 3 stores.)
 // VEC: rows and cols 16-byte aligned; each thread reads 4 rows and 4
 // columns per step in two 16-byte loads (the successor of its last pair
 // comes from the next lane, or one more load at the warp's edge).
 template <bool VEC>
 __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols, uint64_t m,
-                             int cbits, unsigned *__restrict__ stats, uint64_t n_rows, uint64_t *__restrict__ off,
-                             RowGap *__restrict__ gaps, unsigned *__restrict__ n_gaps) {
+                             int cbits, unsigned *__restrict__ stats) {
     unsigned mr = 0, mc = 0;
     bool d = false, g = false, e = false;
     if constexpr (VEC) {
@@ -117,14 +99,8 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
                         d |= k1 > k2;
                         e |= k1 >= k2;
                         g |= rr[k] > rr[k + 1];
-                        if (off && rr[k] < rr[k + 1])
-                            write_row_starts(off, n_rows, (uint64_t)rr[k] + 1, (uint64_t)rr[k + 1] + 1, 4 * q + k + 1,
-                                             gaps, n_gaps);
                     }
                 }
-                if (off && q == 0) write_row_starts(off, n_rows, 0, (uint64_t)rr[0] + 1, 0, gaps, n_gaps);
-                if (off && !have_next)  // 4 q + 3 is the last insert
-                    write_row_starts(off, n_rows, (uint64_t)rr[3] + 1, n_rows + 1, m, gaps, n_gaps);
             }
         }
     }
@@ -134,16 +110,12 @@ __global__ void lock_prepare(const uint32_t *__restrict__ rows, const uint32_t *
         const uint64_t k = ((uint64_t)r << cbits) | c;
         mr = max(mr, r);
         mc = max(mc, c);
-        if (off && i == 0) write_row_starts(off, n_rows, 0, (uint64_t)r + 1, 0, gaps, n_gaps);
         if (i + 1 < m) {
             const uint32_t r2 = rows[i + 1];
             const uint64_t k2 = ((uint64_t)r2 << cbits) | cols[i + 1];
             d |= k > k2;
             e |= k >= k2;
             g |= r > r2;
-            if (off && r < r2) write_row_starts(off, n_rows, (uint64_t)r + 1, (uint64_t)r2 + 1, i + 1, gaps, n_gaps);
-        } else if (off) {
-            write_row_starts(off, n_rows, (uint64_t)r + 1, n_rows + 1, m, gaps, n_gaps);
         }
     }
 #pragma unroll
@@ -693,7 +665,6 @@ first_keep_gather(const uint64_t *__restrict__ keys, const uint32_t *__restrict_
 struct Prepared {
     unsigned unsorted = 1, ungrouped = 1, not_strict = 1;
     bool ready = false;
-    DevBuf s_off;  // first lock: the staged rows' offsets (valid when !ungrouped), csr_off_elems(n_rows)
 };
 
 int sort_keys(Ctx *c, const uint32_t *rows, const uint32_t *cols, uint64_t m, uint64_t n_rows, uint64_t n_cols,
@@ -799,12 +770,8 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
                                            zero.as<unsigned>());
         SPG_LAUNCH_CHECK();
         // the offsets go out before the zero check comes back: one host sync
-        if (pre->s_off.ptr) {
-            new_off = std::move(pre->s_off);
-        } else {
-            SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
-            SPG_TRY(launch_row_offsets(c, rows, m, n, new_off.as<uint64_t>(), s));
-        }
+        SPG_TRY(new_off.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
+        SPG_TRY(launch_row_offsets(c, rows, m, n, new_off.as<uint64_t>(), s));
         unsigned hz = 1;
         SPG_CUDA_TRY(cudaMemcpyAsync(&hz, zero.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_TRY(c->phase_sync(s));
@@ -830,12 +797,8 @@ int first_lock(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t *cols, const
         // pass, in place at the row's input positions; a scan of the kept
         // counts gives the offsets, and entries move only if some were dropped.
         DevBuf s_off, kept, scols, svals;
-        if (pre->s_off.ptr) {
-            s_off = std::move(pre->s_off);
-        } else {
-            SPG_TRY(s_off.alloc((n + 1) * sizeof(uint64_t), s));
-            SPG_TRY(launch_row_offsets(c, rows, m, n, s_off.as<uint64_t>(), s));
-        }
+        SPG_TRY(s_off.alloc((n + 1) * sizeof(uint64_t), s));
+        SPG_TRY(launch_row_offsets(c, rows, m, n, s_off.as<uint64_t>(), s));
         SPG_TRY(kept.alloc(csr_off_elems(n) * sizeof(uint64_t), s));
         SPG_TRY(scols.alloc(csr_alloc_elems(m) * sizeof(uint32_t), s));
         SPG_TRY(svals.alloc(csr_alloc_elems(m) * sizeof(double), s));
@@ -918,29 +881,16 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
     // in order.
     Prepared pre;
     if (m) {
-        // [0..4] stats, [5] gap count, then the gap list (first lock)
         DevBuf stats;
-        const size_t gap_at = 8 * sizeof(unsigned);
-        SPG_TRY(stats.alloc(gap_at + GAP_SLOTS * sizeof(RowGap), s));
-        SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 6 * sizeof(unsigned), s));
-        unsigned *n_gaps = stats.as<unsigned>() + 5;
-        RowGap *gaps = reinterpret_cast<RowGap *>(stats.as<char>() + gap_at);
-        uint64_t *off = nullptr;
-        if (!A->built) {  // the first lock's row offsets come with the check
-            SPG_TRY(pre.s_off.alloc(csr_off_elems(A->n_rows) * sizeof(uint64_t), s));
-            off = pre.s_off.as<uint64_t>();
-        }
+        SPG_TRY(stats.alloc(5 * sizeof(unsigned), s));
+        SPG_CUDA_TRY(cudaMemsetAsync(stats.ptr, 0, 5 * sizeof(unsigned), s));
         if (((uintptr_t)rows | (uintptr_t)cols) % 16 == 0)
             lock_prepare<true><<<grid_for((m + 3) / 4, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
-                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>(), A->n_rows, off, gaps, n_gaps);
+                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>());
         else
             lock_prepare<false><<<grid_for(m, LB, (unsigned)c->n_sms * 16), LB, 0, s>>>(
-                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>(), A->n_rows, off, gaps, n_gaps);
+                rows, cols, m, bits_for(A->n_cols), stats.as<unsigned>());
         SPG_LAUNCH_CHECK();
-        if (off) {
-            offsets_fill_gaps<<<c->n_sms * 4, LB, 0, s>>>(gaps, n_gaps, off);
-            SPG_LAUNCH_CHECK();
-        }
         unsigned h[5] = {0u, 0u, 1u, 1u, 1u};
         SPG_CUDA_TRY(cudaMemcpyAsync(h, stats.ptr, 5 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
         SPG_TRY(c->phase_sync(s));
@@ -954,7 +904,6 @@ static int lock_device_impl(Ctx *c, Csr *A, const uint32_t *rows, const uint32_t
         pre.ungrouped = h[3];
         pre.not_strict = h[4];
         pre.ready = true;
-        if (pre.ungrouped) pre.s_off.release();
     }
     const uint64_t n = A->n_rows;
     const bool has_old = A->built;

@@ -308,3 +308,23 @@ def test_lock_device_arrays_at_any_alignment(ctx, offset):
         A = sg.Csr(ctx, n, n)
         A.lock_device(dr, dc, dv, m)
         assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(r, c, v)]))
+
+
+def test_lock_random_order_first_lock_scales(ctx):
+    """A first lock of 2 M inserts in random order over 2 M rows: correct, and
+    linear in the inserts (milliseconds; any per-insert work proportional to
+    the gap between neighbouring rows would take minutes here)."""
+    import time
+    n, m = 2_000_000, 2_000_000
+    ctr = np.arange(m, dtype=np.uint64)
+    r = gen.below(gen.hash3(41, 1, ctr), n)
+    c = gen.below(gen.hash3(41, 2, ctr), n)
+    v = gen.sym_unit(gen.hash3(41, 3, ctr))
+    A = sg.Csr(ctx, n, n)
+    A.lock(r[:1000], c[:1000], v[:1000])  # warm the kernels and the pool
+    A = sg.Csr(ctx, n, n)
+    t0 = time.perf_counter()
+    A.lock(r, c, v)
+    ctx.sync()
+    assert time.perf_counter() - t0 < 2.0
+    assert_csr_equal(A.download(), oracle.lock_epochs(n, n, [(r, c, v)]))
