@@ -275,10 +275,14 @@ inline uint64_t csr_off_elems(uint64_t n_rows) { return n_rows + 3; }
 // Ascending bitonic sort of the 32 * E keys a warp holds, key[e] of lane l
 // being element 32 e + l. Partners 32 or more apart share a lane (registers),
 // nearer ones are exchanged by shuffles.
+// k0 > 2 (warp-uniform) skips the stages below k0: the caller guarantees
+// that every block of k0 / 2 network positions is already sorted, ascending
+// where (position & k0 / 2) == 0 and descending elsewhere.
 template <int E, class K>
-__device__ __forceinline__ void warp_bitonic(K (&key)[E], int lane) {
+__device__ __forceinline__ void warp_bitonic(K (&key)[E], int lane, int k0 = 2) {
 #pragma unroll
     for (int k = 2; k <= 32 * E; k <<= 1) {
+        if (k < k0) continue;
 #pragma unroll
         for (int j = k >> 1; j > 0; j >>= 1) {
             if (j >= 32) {
@@ -308,8 +312,11 @@ __device__ __forceinline__ void warp_bitonic(K (&key)[E], int lane) {
 }
 
 // Spira's ValueTraits<double>::is_zero (traits.hpp:73-80): +0 and -0 are
-// zero, NaN is not.
-__device__ __forceinline__ bool is_zero(double v) { return fabs(v) <= 0.0; }
+// zero, NaN is not; also exactly Spira's SpGEMM drop test `v != V{}`
+// (spgemm.hpp:44) negated. Tested on the bit pattern (every bit but the sign
+// clear): integer ALU work instead of an FP64 compare, which costs as much
+// FP64 pipe time as a multiply on GB300.
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
 
 // Lanes of the (full) warp whose NB-bit value d (a radix digit, or 256 for
 // "no key" when NB = 9) equals this lane's: NB ballots on the ALU pipe,

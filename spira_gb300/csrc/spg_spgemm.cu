@@ -175,7 +175,7 @@ sg_merge_rows(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ ac
                 }
             }
         }
-        if (acc != 0.0) {  // spgemm.hpp:44: v != V{}
+        if (!is_zero(acc)) {  // spgemm.hpp:44: v != V{}
             tcols[base + cnt] = (uint32_t)j;
             tvals[base + cnt] = acc;
             ++cnt;
@@ -286,7 +286,7 @@ __global__ void sg_run_sums(const uint64_t *__restrict__ begin, const uint32_t *
         double acc = 0.0;  // ValueTraits zero; acc[j] default-constructs to V{}
         for (uint64_t q = begin[u]; q < begin[u + 1]; ++q) acc = __dadd_rn(acc, pval[perm[q]]);
         sum[u] = acc;
-        keep[u] = (acc != 0.0) ? 1 : 0;  // spgemm.hpp:44: v != V{}
+        keep[u] = is_zero(acc) ? 0 : 1;  // spgemm.hpp:44: v != V{}
     }
 }
 

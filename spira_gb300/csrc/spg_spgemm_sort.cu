@@ -169,64 +169,123 @@ __global__ void sgs_heavy_index(const uint32_t *__restrict__ crow, uint64_t n, u
 // warp's w_a / w_b / w_own (HB entries each). P <= 32 E, A's row has <= HB
 // entries.
 template <int E, int SB, class K>
-__device__ uint32_t sgs_row(const SgsArgs &g, uint64_t i, uint32_t reg, uint32_t P, uint32_t *s_col, double *s_prod,
+__device__ __forceinline__ uint32_t sgs_row(const SgsArgs &g, uint64_t i, uint32_t reg, uint32_t P, uint32_t *s_col, double *s_prod,
                             double *w_a, int64_t *w_b, uint16_t *w_own, int lane) {
     const uint64_t ab = g.aoff[i];
     const uint32_t r = (uint32_t)(g.aoff[i + 1] - ab);
-    for (uint32_t s = lane; s < P; s += 32) w_own[s] = 0;
-    __syncwarp();
-    // A entries: slot ranges [ex, ex + L) by a warp scan of their B row lengths
-    uint32_t base = 0;
-    for (uint32_t t0 = 0; t0 < r; t0 += 32) {
-        const uint32_t t = t0 + lane;
-        uint32_t L = 0;
-        uint64_t bs = 0;
-        double a = 0.0;
-        if (t < r) {
-            const uint32_t k = g.acols[ab + t];
-            a = g.avals[ab + t];
-            bs = g.boff[k];
-            L = (uint32_t)(g.boff[k + 1] - bs);
+    // A entries: slot ranges [ex, ex + L) by a warp scan of their B row
+    // lengths. Up to 32 entries sit one per lane; then, if r blocks of
+    // 2^lg >= every L fit the network, entry t's products (already ascending
+    // in column: B's rows are sorted) fill block t, reversed in odd blocks,
+    // so every block is sorted in the direction the network's stage 2^lg
+    // leaves it and the sort starts at stage 2^(lg+1).
+    uint32_t L1 = 0, ex1 = 0;
+    uint64_t bs1 = 0;
+    double a1 = 0.0;
+    int lg = 0;
+    bool runs = false;
+    if (r <= 32) {
+        if ((uint32_t)lane < r) {
+            const uint32_t k = g.acols[ab + lane];
+            a1 = g.avals[ab + lane];
+            bs1 = g.boff[k];
+            L1 = (uint32_t)(g.boff[k + 1] - bs1);
         }
-        uint32_t incl = L;
+        uint32_t incl = L1;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += v;
         }
-        const uint32_t ex = base + incl - L;
-        if (t < r) {
-            w_a[t] = a;
-            w_b[t] = (int64_t)bs - (int64_t)ex;  // B entry of slot s = w_b[t] + s
-            if (L) w_own[ex] = (uint16_t)t;       // distinct: entries with products start at distinct slots
+        ex1 = incl - L1;
+        const uint32_t lmax = __reduce_max_sync(0xffffffffu, L1);
+        lg = lmax <= 1u ? 0 : 32 - __clz((int)(lmax - 1u));
+        runs = lg >= 1 && (r << lg) <= 32u * E;
+        if (!runs) {
+            for (uint32_t s = lane; s < P; s += 32) w_own[s] = 0;
+            __syncwarp();
         }
-        base += __shfl_sync(0xffffffffu, incl, 31);
+        if ((uint32_t)lane < r) {
+            w_a[lane] = a1;
+            w_b[lane] = (int64_t)bs1 - (int64_t)ex1;  // B entry of slot s = w_b[t] + s
+            if (!runs && L1) w_own[ex1] = (uint16_t)lane;
+        }
+    } else {
+        for (uint32_t s = lane; s < P; s += 32) w_own[s] = 0;
+        __syncwarp();
+        uint32_t base = 0;
+        for (uint32_t t0 = 0; t0 < r; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            uint32_t L = 0;
+            uint64_t bs = 0;
+            double a = 0.0;
+            if (t < r) {
+                const uint32_t k = g.acols[ab + t];
+                a = g.avals[ab + t];
+                bs = g.boff[k];
+                L = (uint32_t)(g.boff[k + 1] - bs);
+            }
+            uint32_t incl = L;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const uint32_t ex = base + incl - L;
+            if (t < r) {
+                w_a[t] = a;
+                w_b[t] = (int64_t)bs - (int64_t)ex;
+                if (L) w_own[ex] = (uint16_t)t;  // distinct: entries with products start at distinct slots
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
+        }
     }
     __syncwarp();
-    // slots: element 32 e + lane; owner = last entry starting at or before it
     K key[E];
-    uint32_t carry = 0;
+    if (runs) {
+        const uint32_t bm = (1u << lg) - 1u;
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const uint32_t s = 32u * e + lane;
-        uint32_t o = s < P ? (uint32_t)w_own[s] : 0u;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, o, d);
-            if (lane >= d) o = max(o, v);
+        for (int e = 0; e < E; ++e) {
+            const uint32_t q = 32u * e + lane;
+            const uint32_t t = q >> lg;  // < 32 as E is minimal for P; t >= r (padding) in any case
+            const uint32_t u = (t & 1u) ? bm - (q & bm) : (q & bm);
+            const uint32_t ext = __shfl_sync(0xffffffffu, ex1, (int)(t & 31u));
+            const uint32_t Lt = __shfl_sync(0xffffffffu, L1, (int)(t & 31u));
+            if (t < r && u < Lt) {
+                const uint32_t s = ext + u;
+                const uint64_t bi = (uint64_t)(w_b[t] + (int64_t)s);
+                const uint32_t col = g.bcols[bi];
+                s_prod[reg + s] = __dmul_rn(w_a[t], g.bvals[bi]);
+                key[e] = ((K)col << SB) | (K)s;
+            } else {
+                key[e] = ~(K)0;  // above every real key: padding sorts last
+            }
         }
-        o = max(o, carry);
-        carry = __shfl_sync(0xffffffffu, o, 31);
-        if (s < P) {
-            const uint64_t bi = (uint64_t)(w_b[o] + (int64_t)s);
-            const uint32_t col = g.bcols[bi];
-            s_prod[reg + s] = __dmul_rn(w_a[o], g.bvals[bi]);
-            key[e] = ((K)col << SB) | (K)s;
-        } else {
-            key[e] = ~(K)0;  // above every real key: padding sorts last
+    } else {
+        // slots: element 32 e + lane; owner = last entry starting at or before it
+        uint32_t carry = 0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t s = 32u * e + lane;
+            uint32_t o = s < P ? (uint32_t)w_own[s] : 0u;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, o, d);
+                if (lane >= d) o = max(o, v);
+            }
+            o = max(o, carry);
+            carry = __shfl_sync(0xffffffffu, o, 31);
+            if (s < P) {
+                const uint64_t bi = (uint64_t)(w_b[o] + (int64_t)s);
+                const uint32_t col = g.bcols[bi];
+                s_prod[reg + s] = __dmul_rn(w_a[o], g.bvals[bi]);
+                key[e] = ((K)col << SB) | (K)s;
+            } else {
+                key[e] = ~(K)0;  // above every real key: padding sorts last
+            }
         }
     }
-    warp_bitonic<E, K>(key, lane);
+    warp_bitonic<E, K>(key, lane, runs ? 2 << lg : 2);
     __syncwarp();
     double pv[E];
 #pragma unroll
@@ -258,7 +317,7 @@ __device__ uint32_t sgs_row(const SgsArgs &g, uint64_t i, uint32_t reg, uint32_t
                 double acc = pv[e];
                 for (uint32_t r = q + 1; r < P && s_col[reg + r] == col[e]; ++r) acc = __dadd_rn(acc, s_prod[reg + r]);
                 pv[e] = acc;
-                keep[e] = acc != 0.0;  // spgemm.hpp:44: v != V{}
+                keep[e] = !is_zero(acc);  // spgemm.hpp:44: v != V{}
             }
         }
     }

@@ -3,9 +3,12 @@
 Restates the kernel's index arithmetic in Python, step by step, and checks
 it on the CPU: the tile plan (every tile's rows and products fit the block's
 shared memory and summing threads, the launch's tile bound holds), the
-per-row expansion (owner max-scan, slots inside the warp's arrays), the
-bitonic network as the kernel runs it (element 32 e + lane; partners 32 or
-more apart inside a lane, nearer ones by shuffles), the left-to-right run
+per-row expansion (owner max-scan, slots inside the warp's arrays; or, for
+rows of at most 32 A entries whose B rows fit power-of-two blocks, the
+presorted runs placed block by block, odd blocks reversed, and the network
+started at the first stage that merges blocks), the bitonic network as the
+kernel runs it (element 32 e + lane; partners 32 or more apart inside a
+lane, nearer ones by shuffles), the left-to-right run
 sums with in-place compaction, and the ordered copy-out. The result must be
 bit-identical to the oracle's Spira-order SpGEMM. Every shared-memory index
 the model touches is asserted inside its buffer.
@@ -55,11 +58,15 @@ def tile_plan(A, P, hb, tpb):
     return pofs, starts + [m], t_max
 
 
-def bitonic_warp(key, E):
-    """key: list of 32*E ints, element i = 32 e + lane; the kernel's network."""
+def bitonic_warp(key, E, k0=2):
+    """key: list of 32*E ints, element i = 32 e + lane; the kernel's network
+    (stages below k0 skipped)."""
     N = 32 * E
     k = 2
     while k <= N:
+        if k < k0:
+            k <<= 1
+            continue
         j = k >> 1
         while j > 0:
             new = list(key)
@@ -86,7 +93,10 @@ def bitonic_warp(key, E):
     return key
 
 
-def model(A, B, hb, tpb):
+def model(A, B, hb, tpb, n_runs=None):
+    """n_runs: [rows sorted as presorted runs, rows sorted in full], counted."""
+    if n_runs is None:
+        n_runs = [0, 0]
     SB = hb.bit_length() - 1
     P = products(A, B)
     pofs, starts, t_max = tile_plan(A, P, hb, tpb)
@@ -131,6 +141,7 @@ def model(A, B, hb, tpb):
             w_a = np.zeros(hb)
             w_b = np.zeros(hb, np.int64)
             ex = 0
+            exs, Ls = [], []
             for tt in range(r):
                 k = acols[aoff[i] + tt]
                 L = int(boff[k + 1] - boff[k])
@@ -139,19 +150,43 @@ def model(A, B, hb, tpb):
                 if L:
                     assert ex < Pi <= hb
                     own[ex] = tt
+                exs.append(ex)
+                Ls.append(L)
                 ex += L
             assert ex == Pi
+            lmax = max(Ls) if r <= 32 else 0
+            lg = 0 if lmax <= 1 else (lmax - 1).bit_length()
+            runs = r <= 32 and lg >= 1 and (r << lg) <= 32 * E
             keys = []
-            for s in range(32 * E):
-                if s < Pi:
-                    o = int(own[:s + 1].max())  # inclusive max-scan
-                    bi = int(w_b[o] + s)
-                    assert boff[acols[aoff[i] + o]] <= bi < boff[acols[aoff[i] + o] + 1]
-                    s_prod[reg + s] = np.float64(w_a[o]) * np.float64(bvals[bi])
-                    keys.append((int(bcols[bi]) << SB) | s)
-                else:
-                    keys.append((1 << 64) - 1)
-            skeys = bitonic_warp(keys, E)
+            if runs:
+                bm = (1 << lg) - 1
+                for q in range(32 * E):
+                    t = q >> lg
+                    assert t < 32  # the shuffle source lane
+                    u = bm - (q & bm) if t & 1 else q & bm
+                    if t < r and u < Ls[t]:
+                        s = exs[t] + u
+                        assert 0 <= s < Pi
+                        bi = int(w_b[t] + s)
+                        assert boff[acols[aoff[i] + t]] <= bi < boff[acols[aoff[i] + t] + 1]
+                        s_prod[reg + s] = np.float64(w_a[t]) * np.float64(bvals[bi])
+                        keys.append((int(bcols[bi]) << SB) | s)
+                    else:
+                        keys.append((1 << 64) - 1)
+                assert sorted(k for k in keys if k != (1 << 64) - 1) == sorted(set(keys) - {(1 << 64) - 1})
+                n_runs[0] += 1
+            else:
+                for s in range(32 * E):
+                    if s < Pi:
+                        o = int(own[:s + 1].max())  # inclusive max-scan
+                        bi = int(w_b[o] + s)
+                        assert boff[acols[aoff[i] + o]] <= bi < boff[acols[aoff[i] + o] + 1]
+                        s_prod[reg + s] = np.float64(w_a[o]) * np.float64(bvals[bi])
+                        keys.append((int(bcols[bi]) << SB) | s)
+                    else:
+                        keys.append((1 << 64) - 1)
+                n_runs[1] += 1
+            skeys = bitonic_warp(keys, E, (2 << lg) if runs else 2)
             assert skeys == sorted(keys)
             pv = [s_prod[reg + (kk & ((1 << SB) - 1))] for kk in skeys[:Pi]]
             for q in range(Pi):
@@ -202,11 +237,13 @@ def model(A, B, hb, tpb):
 
 def _check(A, B, name):
     hb, tpb = CONFIGS[name]
-    off, cols, vals = model(A, B, hb, tpb)
+    n_runs = [0, 0]
+    off, cols, vals = model(A, B, hb, tpb, n_runs)
     C = oracle.spgemm(A, B)
     np.testing.assert_array_equal(off, C.off.astype(np.uint64))
     np.testing.assert_array_equal(cols, C.cols)
     np.testing.assert_array_equal(vals.view(np.uint64), C.vals.view(np.uint64))
+    return n_runs
 
 
 @pytest.mark.parametrize("name", list(CONFIGS))
@@ -214,7 +251,8 @@ def test_model_uniform_rows(name):
     n = 600
     r, c, v = gen.uniform_rows(n, n, 8, seed=3)
     A = csr(n, n, r, c, v)
-    _check(A, A, name)
+    n_runs = _check(A, A, name)
+    assert n_runs[0] > 0.9 * n  # 8 runs of <= 8: the presorted-run path
 
 
 @pytest.mark.parametrize("name", list(CONFIGS))
@@ -236,7 +274,30 @@ def test_model_mixed_rows_heavy_and_cancellations(name):
     bvals = (gen.below(gen.hash3(9, 2, ctr2), 5).astype(np.int64) - 2).astype(np.float64)
     bvals[::4] = gen.sym_unit(gen.hash3(9, 3, ctr2[::4]))
     B = csr(n_inner, n_cols, brows, bcols, bvals)
-    _check(A, B, name)
+    n_runs = _check(A, B, name)
+    assert n_runs[0] > 0 and n_runs[1] > 0  # both expansions ran
+
+
+@pytest.mark.parametrize("E", [1, 2, 4, 8])
+def test_network_from_presorted_runs(E):
+    """Blocks of 2^lg sorted keys, odd blocks reversed, padding anywhere after
+    a block's real keys: the network started at stage 2^(lg+1) sorts them."""
+    rng = np.random.default_rng(E)
+    N = 32 * E
+    for lg in range(1, N.bit_length()):
+        if (1 << lg) > N:
+            break
+        for _ in range(6):
+            n_blocks = int(rng.integers(1, N // (1 << lg) + 1))
+            keys = [(1 << 64) - 1] * N
+            for t in range(n_blocks):
+                L = int(rng.integers(0, (1 << lg) + 1))
+                run = sorted(int(x) for x in rng.choice(1 << 20, L, replace=False))
+                block = run + [(1 << 64) - 1] * ((1 << lg) - L)
+                if t & 1:
+                    block = block[::-1]
+                keys[t << lg:(t + 1) << lg] = block
+            assert bitonic_warp(keys, E, 2 << lg) == sorted(keys)
 
 
 def test_model_tile_bound_many_empty_rows():
