@@ -504,16 +504,13 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
     if ((uint32_t)tid < nr) g.coff[row0 + tid] = base + excl;
     if (tid == 0 && row1 == g.m) g.coff[g.m] = base + total;
     if (!heavy_tile) {
-        for (uint32_t q = tid; q < total; q += SGS_THREADS) {
-            uint32_t lo = 0, hi = nr;  // last row j with sh_excl[j] <= q
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (sh_excl[mid] <= q) lo = mid;
-                else hi = mid;
+        // a warp per row, lanes over its kept entries (no search for the row)
+        for (uint32_t j = warp; j < nr; j += SGS_WARPS) {
+            const uint32_t e0 = sh_excl[j], n = sh_excl[j + 1] - e0, src = sh_reg[j];
+            for (uint32_t q = lane; q < n; q += 32) {
+                g.ccols[base + e0 + q] = s_col[src + q];
+                g.cvals[base + e0 + q] = s_prod[src + q];
             }
-            const uint32_t src = sh_reg[lo] + (q - sh_excl[lo]);
-            g.ccols[base + q] = s_col[src];
-            g.cvals[base + q] = s_prod[src];
         }
     } else {
         const uint64_t hb0 = total ? g.hbeg[row0] : 0;

@@ -9,7 +9,7 @@ presorted runs placed block by block, odd blocks reversed, and the network
 started at the first stage that merges blocks), the bitonic network as the
 kernel runs it (element 32 e + lane; partners 32 or more apart inside a
 lane, nearer ones by shuffles), the left-to-right run
-sums with in-place compaction, and the ordered copy-out. The result must be
+sums with in-place compaction, and the ordered copy-out (a warp per row). The result must be
 bit-identical to the oracle's Spira-order SpGEMM. Every shared-memory index
 the model touches is asserted inside its buffer.
 """
@@ -215,18 +215,14 @@ def model(A, B, hb, tpb, n_runs=None):
         total = int(excl[-1])
         for j in range(nr):
             out_off[row0 + j] = base + excl[j]
-        oc, ov = np.empty(total, np.int64), np.empty(total)
-        for q in range(total):
-            lo, hi = 0, nr
-            while hi - lo > 1:
-                mid = (lo + hi) >> 1
-                if excl[mid] <= q:
-                    lo = mid
-                else:
-                    hi = mid
-            src = counts[lo][0] + (q - excl[lo])
-            assert 0 <= src < slots
-            oc[q], ov[q] = s_col[src], s_prod[src]
+        oc, ov = np.full(total, -1, np.int64), np.full(total, np.nan)
+        for j in range(nr):  # a warp per row, lanes over its kept entries
+            e0, n = int(excl[j]), int(excl[j + 1] - excl[j])
+            src = counts[j][0]
+            assert 0 <= src and src + n <= slots and e0 + n <= total
+            assert (oc[e0:e0 + n] == -1).all()  # every output entry written once
+            oc[e0:e0 + n], ov[e0:e0 + n] = s_col[src:src + n], s_prod[src:src + n]
+        assert (oc >= 0).all()
         out_cols.append(oc)
         out_vals.append(ov)
         base += total
