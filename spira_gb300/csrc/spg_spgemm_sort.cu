@@ -287,41 +287,65 @@ __device__ __forceinline__ uint32_t sgs_row(const SgsArgs &g, uint64_t i, uint32
     }
     warp_bitonic<E, K>(key, lane, runs ? 2 << lg : 2);
     __syncwarp();
+    // products in sorted order; a run of equal columns starts at a head
+    // element (its predecessor's column differs) and continues while the
+    // successor's column is the same: neighbours' columns by shuffles
     double pv[E];
+    uint32_t col[E];
+    bool head[E], cont = false;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const uint32_t q = 32u * e + lane;
         pv[e] = q < P ? s_prod[reg + (uint32_t)(key[e] & (K)((1u << SB) - 1u))] : 0.0;
+        col[e] = (uint32_t)(key[e] >> SB);
     }
-    __syncwarp();
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const uint32_t q = 32u * e + lane;
-        if (q < P) {
-            s_col[reg + q] = (uint32_t)(key[e] >> SB);
-            s_prod[reg + q] = pv[e];
+        uint32_t pc = __shfl_up_sync(0xffffffffu, col[e], 1);
+        uint32_t nc = __shfl_down_sync(0xffffffffu, col[e], 1);
+        if (e > 0) {
+            const uint32_t v = __shfl_sync(0xffffffffu, col[e > 0 ? e - 1 : 0], 31);
+            if (lane == 0) pc = v;
         }
+        if (e + 1 < E) {
+            const uint32_t v = __shfl_sync(0xffffffffu, col[e + 1 < E ? e + 1 : e], 0);
+            if (lane == 31) nc = v;
+        }
+        head[e] = q < P && (q == 0 || pc != col[e]);
+        cont = cont || (q + 1 < P && nc == col[e]);
     }
-    __syncwarp();
-    // runs: the head lane sums its run in slot order (Spira's order)
-    uint32_t col[E];
     bool keep[E];
+    if (__any_sync(0xffffffffu, cont)) {
+        // some run is longer than one product: the head lane sums it in slot
+        // order (Spira's order) from the sorted copy in shared memory
+        __syncwarp();  // every gather done before the sorted copy lands
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const uint32_t q = 32u * e + lane;
-        keep[e] = false;
-        col[e] = 0;
-        if (q < P) {
-            col[e] = (uint32_t)(key[e] >> SB);
-            if (q == 0 || s_col[reg + q - 1] != col[e]) {
+        for (int e = 0; e < E; ++e) {
+            const uint32_t q = 32u * e + lane;
+            if (q < P) {
+                s_col[reg + q] = col[e];
+                s_prod[reg + q] = pv[e];
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t q = 32u * e + lane;
+            keep[e] = false;
+            if (head[e]) {
                 double acc = pv[e];
                 for (uint32_t r = q + 1; r < P && s_col[reg + r] == col[e]; ++r) acc = __dadd_rn(acc, s_prod[reg + r]);
                 pv[e] = acc;
                 keep[e] = !is_zero(acc);  // spgemm.hpp:44: v != V{}
             }
         }
+    } else {
+        // every run is one product: its sum is the product itself
+#pragma unroll
+        for (int e = 0; e < E; ++e) keep[e] = head[e] && !is_zero(pv[e]);  // spgemm.hpp:44
     }
-    __syncwarp();  // every run read before the compacted writes land
+    __syncwarp();  // every gather and run read before the compacted writes land
     uint32_t kept = 0;
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
