@@ -10,22 +10,27 @@
 // order (a ticket from an atomic counter) and, per tile:
 //
 //   1. per row, one warp: the row's products are expanded over the lanes
-//      (slot s = position in (A entry, B entry) order; the A entry owning a
-//      slot comes from a max-scan of the entries' first slots), multiplied
+//      (slot s = position in (A entry, B entry) order), multiplied
 //      (__dmul_rn, all lanes busy), and their keys (column << SB | slot)
 //      bitonic-sorted in registers. Column order with slot order inside a
-//      column is exactly ascending k for each (i, j). The sorted (column,
-//      product) pairs go to the tile's shared memory;
-//   2. the same warp: the lane holding the first product of a run of equal
-//      columns sums the run left to right (__dadd_rn from the run's first
-//      product: +0.0 + p1 = p1 whenever the sum can be kept, so starting at
-//      p1 changes no kept value); most runs are one product long and cost no
-//      FP64 instruction. The kept sums (not +-0) are ranked with ballots and
-//      compacted in place, and the row's kept count goes to the tile;
+//      column is exactly ascending k for each (i, j). A row of at most 32 A
+//      entries whose B rows fit power-of-two blocks of the network places
+//      each B row (already sorted) in its own block and starts the network
+//      at the first merging stage; other rows take the A entry owning a
+//      slot from a max-scan of the entries' first slots;
+//   2. the same warp: runs of equal columns are found from the neighbours'
+//      columns (shuffles). If the row has none longer than one product (a
+//      warp vote), every product is its own sum; otherwise the sorted
+//      (column, product) pairs go to the tile's shared memory and the lane
+//      holding a run's first product sums it left to right (__dadd_rn from
+//      the run's first product: +0.0 + p1 = p1 whenever the sum can be
+//      kept, so starting at p1 changes no kept value). The kept sums (not
+//      +-0) are ranked with ballots and compacted in place, and the row's
+//      kept count goes to the tile;
 //   3. the tile's kept count goes through an ordered scan (decoupled
 //      look-back over the tiles' published counts, 32 predecessors per step
-//      by one warp, every wait bounded), and
-//      the tile writes its rows' offsets and entries straight into C, so no
+//      by one warp, every wait bounded), and the tile writes its rows'
+//      offsets and entries (a warp per row) straight into C, so no
 //      compaction pass and no second scan follow.
 //
 // A wait that runs out (about a second) sets a bit in the context's status
@@ -39,7 +44,7 @@ namespace {
 
 constexpr int SGS_WARPS = 4;
 constexpr int SGS_THREADS = 32 * SGS_WARPS;
-constexpr uint32_t SGS_RB = SGS_THREADS;  // rows per tile at most: one summing thread each
+constexpr uint32_t SGS_RB = SGS_THREADS;  // rows per tile at most: one thread each in the block scan
 constexpr unsigned SGS_STATUS_TIMEOUT = 0x10u;
 constexpr long long SGS_WAIT_CYCLES = 1ll << 31;  // ~1 s at 2 GHz
 
@@ -420,8 +425,8 @@ __global__ void __launch_bounds__(SGS_THREADS) sgs_tiles(SgsArgs g) {
     static_assert((1 << SB) == HB, "HB is a power of two");
     extern __shared__ __align__(16) unsigned char sgs_smem[];
     // row j of the tile keeps its products at [pofs - p0 + j, + P): one slot of
-    // skew per row, so the summing threads' rows (often of equal length) do
-    // not start in the same shared-memory bank
+    // skew per row, so rows of equal length do not all start in the same
+    // shared-memory bank
     const uint32_t slots = g.tpb + SGS_RB;
     double *s_prod = reinterpret_cast<double *>(sgs_smem);
     uint32_t *s_col = reinterpret_cast<uint32_t *>(s_prod + slots);

@@ -2,14 +2,16 @@
 
 Restates the kernel's index arithmetic in Python, step by step, and checks
 it on the CPU: the tile plan (every tile's rows and products fit the block's
-shared memory and summing threads, the launch's tile bound holds), the
+shared memory and the block scan's threads, the launch's tile bound holds), the
 per-row expansion (owner max-scan, slots inside the warp's arrays; or, for
 rows of at most 32 A entries whose B rows fit power-of-two blocks, the
 presorted runs placed block by block, odd blocks reversed, and the network
 started at the first stage that merges blocks), the bitonic network as the
 kernel runs it (element 32 e + lane; partners 32 or more apart inside a
 lane, nearer ones by shuffles), the left-to-right run
-sums with in-place compaction, and the ordered copy-out (a warp per row). The result must be
+sums (run boundaries from the neighbours' columns; rows without equal
+columns keep every product as its own sum) with in-place compaction, and the
+ordered copy-out (a warp per row). The result must be
 bit-identical to the oracle's Spira-order SpGEMM. Every shared-memory index
 the model touches is asserted inside its buffer.
 """
@@ -21,7 +23,7 @@ import pytest
 import oracle
 from spira_gb300 import gen
 
-RB = 128          # rows per tile (one summing thread each)
+RB = 128          # rows per tile (one thread each in the block scan)
 WARPS = 4
 CONFIGS = {"warpsort_64": (64, 1024), "warpsort_128": (128, 2048), "warpsort_256": (256, 4096)}
 
@@ -94,9 +96,10 @@ def bitonic_warp(key, E, k0=2):
 
 
 def model(A, B, hb, tpb, n_runs=None):
-    """n_runs: [rows sorted as presorted runs, rows sorted in full], counted."""
+    """n_runs: [rows sorted as presorted runs, rows sorted in full, rows with
+    a run longer than one product], counted."""
     if n_runs is None:
-        n_runs = [0, 0]
+        n_runs = [0, 0, 0]
     SB = hb.bit_length() - 1
     P = products(A, B)
     pofs, starts, t_max = tile_plan(A, P, hb, tpb)
@@ -188,29 +191,36 @@ def model(A, B, hb, tpb, n_runs=None):
                 n_runs[1] += 1
             skeys = bitonic_warp(keys, E, (2 << lg) if runs else 2)
             assert skeys == sorted(keys)
+            # the same warp: products gathered into sorted order (registers)
             pv = [s_prod[reg + (kk & ((1 << SB) - 1))] for kk in skeys[:Pi]]
-            for q in range(Pi):
-                s_col[reg + q] = skeys[q] >> SB
-                s_prod[reg + q] = pv[q]
-            counts.append((reg, Pi))
-        # one thread per row: run sums, in-place compaction
-        kept = []
-        for reg, Pi in counts:
+            col = [kk >> SB for kk in skeys[:Pi]]
+            # run boundaries from the neighbours' columns (the kernel's shuffles)
+            head = [q == 0 or col[q - 1] != col[q] for q in range(Pi)]
+            cont = [q + 1 < Pi and col[q + 1] == col[q] for q in range(Pi)]
+            if any(cont):  # the warp vote: some run is longer than one product
+                n_runs[2] += 1
+                for q in range(Pi):  # the sorted copy in shared memory
+                    s_col[reg + q] = col[q]
+                    s_prod[reg + q] = pv[q]
+                keep = [False] * Pi
+                for q in range(Pi):
+                    if head[q]:  # the head lane sums its run left to right
+                        acc, r = pv[q], q + 1
+                        while r < Pi and s_col[reg + r] == col[q]:
+                            acc = np.float64(acc) + np.float64(s_prod[reg + r])
+                            r += 1
+                        pv[q] = acc
+                        keep[q] = not abs(acc) <= 0.0  # spgemm.hpp:44: v != V{}
+            else:
+                keep = [head[q] and not abs(pv[q]) <= 0.0 for q in range(Pi)]
+            # ballot ranking: kept sums in element order, compacted from reg
             w = reg
-            if Pi:
-                cc, acc = s_col[reg], s_prod[reg]
-                for q in range(reg + 1, reg + Pi):
-                    if s_col[q] == cc:
-                        acc = np.float64(acc) + np.float64(s_prod[q])
-                    else:
-                        if acc != 0.0:
-                            s_col[w], s_prod[w] = cc, acc
-                            w += 1
-                        cc, acc = s_col[q], s_prod[q]
-                if acc != 0.0:
-                    s_col[w], s_prod[w] = cc, acc
+            for q in range(Pi):
+                if keep[q]:
+                    s_col[w], s_prod[w] = col[q], pv[q]
                     w += 1
-            kept.append(w - reg)
+            counts.append((reg, w - reg))
+        kept = [k for _, k in counts]
         excl = np.concatenate([[0], np.cumsum(kept)])
         total = int(excl[-1])
         for j in range(nr):
@@ -233,7 +243,7 @@ def model(A, B, hb, tpb, n_runs=None):
 
 def _check(A, B, name):
     hb, tpb = CONFIGS[name]
-    n_runs = [0, 0]
+    n_runs = [0, 0, 0]
     off, cols, vals = model(A, B, hb, tpb, n_runs)
     C = oracle.spgemm(A, B)
     np.testing.assert_array_equal(off, C.off.astype(np.uint64))
@@ -272,6 +282,7 @@ def test_model_mixed_rows_heavy_and_cancellations(name):
     B = csr(n_inner, n_cols, brows, bcols, bvals)
     n_runs = _check(A, B, name)
     assert n_runs[0] > 0 and n_runs[1] > 0  # both expansions ran
+    assert 0 < n_runs[2] < n_runs[0] + n_runs[1]  # rows with and without equal columns
 
 
 @pytest.mark.parametrize("E", [1, 2, 4, 8])
